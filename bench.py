@@ -1,0 +1,336 @@
+"""Benchmark of the CheFSI hot path: the Chebyshev filter / stencil microbenchmark.
+
+Workload (one "step"): a degree-20 Chebyshev filter (bounds a0=-1, cutoff a=0.5, b=50 Ha)
+over 512 orbital vectors on a 96^3 periodic grid (h = 0.35 Bohr, FD order 12), with a local
+potential of 64 seeded Gaussians and a nonlocal part of 64 atoms x 9 projectors on 6 Bohr
+spheres. Synthetic seeded inputs; the block (1.8 GB in FP32, 3.6 GB in FP64) is larger than
+L2, so no flush is needed between steps.
+
+Metric: algorithmic GB/s of the filter, N*Ns*s*(3m-1) bytes per step (the first degree reads X
+and writes Y, each later one reads Y and X and writes the new iterate).
+
+  value  : FP32 filter on device-resident FP32 blocks (sgpu_ChebyshevFiltering_f32)
+  e2e    : the drop-in call with FP64 host arrays (sgpu_ChebyshevFiltering, precision FP32),
+           host<->device copies of X in and X, Y out inside the timed region
+  fp64   : the plain FP64 filter on device-resident blocks (the FP64 drop-in)
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N3 = (96, 96, 96)
+NCOL = 512
+M = 20
+METRIC = "CheFSI SCF time-to-solution at 1e-5 Ha/atom vs plain FP64 GPU; stencil GB/s"
+WORKLOAD = ("chebyshev_filter_microbench: 96^3 periodic grid h=0.35 Bohr, FD order 12, "
+            "512 vectors U[-1,1], degree 20, bounds [-1,50] cutoff 0.5, 64 Gaussian Veff, "
+            "64 atoms x 9 projectors on 6 Bohr spheres")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ncol", type=int, default=NCOL)
+    ap.add_argument("--cpu-cols", type=int, default=16,
+                    help="columns in the bounded CPU-baseline sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxs.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxs),
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_baseline(wl, ncols, threads=None):
+    """The CPU oracle (a port of the reference's filter) on a bounded sample of the same
+    workload: ncols of the 512 vectors, same grid, potential, projectors and degree."""
+    from oracle.oracle import Oracle
+    o = Oracle(wl["grid"], wl["nl"])
+    if threads:
+        o.set_threads(threads)
+    Nd = N3[0] * N3[1] * N3[2]
+    rng = np.random.default_rng(7)
+    X = rng.uniform(-1.0, 1.0, size=(ncols, Nd))
+    t0 = time.perf_counter()
+    o.chebyshev(wl["veff"], M, wl["a"], wl["b"], wl["a0"], X)
+    dt = time.perf_counter() - t0
+    from sparc_gb300.synthetic import filter_bytes
+    gbs = filter_bytes(Nd, ncols, M, 8) / dt / 1e9
+    return {"value": round(gbs, 3), "unit": "GB/s", "cores": o.threads(), "kind": "port",
+            "sample": f"FP64 degree-{M} filter of {ncols} of the {NCOL} vectors on the same "
+                      f"96^3 grid, potential and projectors ({dt:.2f} s)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from sparc_gb300.synthetic import microbench_workload
+    wl = microbench_workload(N=N3, ncol=NCOL, with_vectors=False)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(wl, args.cpu_cols)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(wl, args.cpu_cols))
+    v = statistics.median([c["value"] for c in vals])
+    cb = dict(vals[0])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "vs_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world, rank, local = dist_env()
+    import torch
+    import sparc_gb300 as sg
+    from sparc_gb300.synthetic import filter_bytes, microbench_workload
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    wl = microbench_workload(N=N3, ncol=args.ncol, with_vectors=False)
+    g = wl["grid"]
+    Nd = g["Nx"] * g["Ny"] * g["Nz"]
+    ncol = args.ncol
+    ctx = sg.Context(g["Nx"], g["Ny"], g["Nz"], g["FDn"], g["cx"], g["cy"], g["cz"], g["dV"],
+                     device=local)
+    ctx.set_veff(wl["veff"])
+    nl = wl["nl"]
+    ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
+                     nl["grid_pos"], nl["chi"])
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    X0 = (torch.rand((ncol, Nd), generator=gen, device=dev, dtype=torch.float32) * 2 - 1)
+    X = X0.clone()
+    Y = torch.empty_like(X)
+    a, b, a0 = wl["a"], wl["b"], wl["a0"]
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record()
+        for _ in range(steps):
+            fn()
+        with torch.cuda.stream(stream):
+            e1.record()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
+
+    def step32():
+        with torch.cuda.stream(stream):  # reset the input block (the filter overwrites X)
+            X.copy_(X0)
+        ctx.ChebyshevFiltering_f32(X, Y, M, a, b, a0)
+
+    # --- headline: FP32 filter, device-resident blocks, per-kernel events on
+    ctx.profile_enable(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms32 = timed(step32, args.steps, args.warmup)
+    ck = clocks.stop()
+    st_ms, st_n = ctx.profile_read(sg.KERNEL_STENCIL)
+    pj_ms, pj_n = ctx.profile_read(sg.KERNEL_NL_PROJECT)
+    ap_ms, ap_n = ctx.profile_read(sg.KERNEL_NL_APPLY)
+    _, launches = ctx.profile_read(sg.KERNEL_KINDS)
+    ctx.profile_enable(False)
+    # profile counters cover warm-up and timed steps alike: report per step
+    nsteps_prof = args.steps + args.warmup
+    bytes32 = filter_bytes(Nd, ncol, M, 4)
+    value = world * bytes32 / (ms32 / 1e3) / 1e9
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+    stencil_launch_ms = st_ms / max(st_n, 1)
+    stencil_bytes_per_launch = bytes32 / M  # (3m-1)/m units per launch on average
+    achieved = stencil_bytes_per_launch / (stencil_launch_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "stencil_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        traffic = tj.get("fp32_bytes_per_launch_at_bench")
+
+    # --- e2e: drop-in call with FP64 pinned host arrays (FP32 arithmetic inside)
+    Xh0 = X0[:, :].double().cpu().pin_memory()
+    Xh = torch.empty_like(Xh0).pin_memory()
+    Yh = torch.empty_like(Xh0).pin_memory()
+
+    def step_e2e():
+        Xh.copy_(Xh0)  # host-side reset of the pinned input (outside the device stream)
+        ctx.ChebyshevFiltering(Xh, Yh, M, a, b, a0, precision=sg.SGPU_PREC_FP32)
+
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(1):
+        step_e2e()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step_e2e()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = world * bytes32 / e2e_s / 1e9
+    del Xh0, Xh, Yh
+
+    # --- plain FP64 filter (the FP64 drop-in), device-resident
+    fp64 = None
+    if not args.no_fp64:
+        X64_0 = X0.double()
+        X64 = X64_0.clone()
+        Y64 = torch.empty_like(X64)
+
+        def step64():
+            with torch.cuda.stream(stream):
+                X64.copy_(X64_0)
+            ctx.ChebyshevFiltering(X64, Y64, M, a, b, a0, precision=sg.SGPU_PREC_FP64)
+
+        ms64 = timed(step64, max(1, min(args.steps, 2)), 1)
+        fp64 = {"value": round(world * filter_bytes(Nd, ncol, M, 8) / (ms64 / 1e3) / 1e9, 2),
+                "unit": "GB/s", "ms_per_step": round(ms64, 3)}
+        del X64_0, X64, Y64
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(wl, args.cpu_cols)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms32, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (1.8 GB FP32 block), no flush",
+                       "step": "X reset copy + degree-20 filter over 512 vectors"},
+            "roofline": {"bound": "hbm", "kernel": "k_stencil_orth<float>",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                         "traffic": traffic,
+                         "stencil_ms_per_launch": round(stencil_launch_ms, 4)},
+            "kernels_per_step_ms": {
+                "stencil": round(st_ms / nsteps_prof, 3),
+                "nl_project": round(pj_ms / nsteps_prof, 3),
+                "nl_apply": round(ap_ms / nsteps_prof, 3)},
+            "gpu_launches": int(launches * args.steps / nsteps_prof),
+            "e2e": {"value": round(e2e_val, 2), "unit": "GB/s",
+                    "h2d_bytes_per_step": int(ncol * Nd * 8),
+                    "d2h_bytes_per_step": int(2 * ncol * Nd * 8),
+                    "api": "sgpu_ChebyshevFiltering(host FP64 arrays, SGPU_PREC_FP32)"},
+            "fp64": fp64,
+            "cpu_baseline": cpu,
+            "clocks": ck,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

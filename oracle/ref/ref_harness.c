@@ -1,0 +1,165 @@
+/*
+ * Kernel harness around the reference SPARC objects (test infrastructure only).
+ *
+ * ref_init() runs the reference's own set-up for an input file pair <name>.inpt/<name>.ion
+ * (Initialize, src/initialization.c:229, then the influencing-atom, pseudocharge and nonlocal
+ * projector steps of Calculate_EGS_elecDensEnergy, src/electronicGroundState.c:387-470), and
+ * the ref_* entry points then call the reference's hot-path functions on caller-provided
+ * arrays, so that golden vectors come from the reference code itself:
+ *   Lap_plus_diag_vec_mult_orth  src/lapVecRoutines.c:306
+ *   Vnl_vec_mult                 src/nlocVecRoutines.c:798
+ *   Hamiltonian_vectors_mult     src/hamiltonianVecRoutines.c:45
+ *   ChebyshevFiltering           src/eigenSolver.c:722
+ *   poisson_residual             src/lapVecRoutines.c:69
+ * One system per process: the reference keeps its state in the SPARC_OBJ built here.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <mpi.h>
+
+#include "isddft.h"
+#include "initialization.h"
+#include "electrostatics.h"
+#include "nlocVecRoutines.h"
+#include "lapVecRoutines.h"
+#include "hamiltonianVecRoutines.h"
+#include "eigenSolver.h"
+#include "orbitalElecDensInit.h"
+
+static SPARC_OBJ S;
+static int g_ready = 0;
+
+int ref_init(const char *name)
+{
+    char a0[] = "sparc", a1[] = "-name";
+    char *nm = strdup(name);
+    char *argv[] = {a0, a1, nm, NULL};
+    int argc = 3;
+    char **pargv = argv;
+    MPI_Init(&argc, &pargv);
+    memset(&S, 0, sizeof(S));
+    Initialize(&S, argc, argv);
+    GetInfluencingAtoms(&S);
+    Generate_PseudoChargeDensity(&S);
+    GetInfluencingAtoms_nloc(&S, &S.Atom_Influence_nloc, S.DMVertices_dmcomm, S.dmcomm);
+    CalculateNonlocalProjectors(&S, &S.nlocProj, S.Atom_Influence_nloc, S.DMVertices_dmcomm,
+                                S.dmcomm);
+    Init_electronDensity(&S);
+    g_ready = 1;
+    return 0;
+}
+
+/* out[0..9] = Nx, Ny, Nz, Nd, order, n_atom, Ntypes, Nstates, IP_displ[n_atom], cell_typ */
+void ref_dims(int *out)
+{
+    out[0] = S.Nx; out[1] = S.Ny; out[2] = S.Nz; out[3] = S.Nd;
+    out[4] = S.order; out[5] = S.n_atom; out[6] = S.Ntypes; out[7] = S.Nstates;
+    out[8] = S.IP_displ[S.n_atom]; out[9] = S.cell_typ;
+}
+
+/* out[0..6] = delta_x, delta_y, delta_z, dV, range_x, range_y, range_z */
+void ref_grid(double *out)
+{
+    out[0] = S.delta_x; out[1] = S.delta_y; out[2] = S.delta_z; out[3] = S.dV;
+    out[4] = S.range_x; out[5] = S.range_y; out[6] = S.range_z;
+}
+
+/* FDn+1 weights per direction, already divided by h^2 */
+void ref_d2coeffs(double *cx, double *cy, double *cz)
+{
+    int FDn = S.order / 2;
+    for (int p = 0; p <= FDn; p++) {
+        cx[p] = S.D2_stencil_coeffs_x[p];
+        cy[p] = S.D2_stencil_coeffs_y[p];
+        cz[p] = S.D2_stencil_coeffs_z[p];
+    }
+}
+
+/* per-type pseudopotential summary: lmax, lloc, nproj, ppl[0..lmax]; Gamma (sum ppl) */
+void ref_psd(int ityp, int *ints, double *gamma)
+{
+    int lmax = S.psd[ityp].lmax;
+    ints[0] = lmax;
+    ints[1] = S.localPsd[ityp];
+    ints[2] = S.nlocProj[ityp].nproj;
+    ints[3] = S.nAtomv[ityp];
+    int tot = 0;
+    for (int l = 0; l <= lmax; l++) {
+        ints[4 + l] = S.psd[ityp].ppl[l];
+        tot += S.psd[ityp].ppl[l];
+    }
+    for (int i = 0; i < tot; i++) gamma[i] = S.psd[ityp].Gamma[i];
+}
+
+int ref_nloc_natom(int ityp) { return S.Atom_Influence_nloc[ityp].n_atom; }
+
+/* out[0] = ndc, out[1] = atom_index of image iat of type ityp */
+void ref_nloc_atom(int ityp, int iat, int *out)
+{
+    out[0] = S.Atom_Influence_nloc[ityp].ndc[iat];
+    out[1] = S.Atom_Influence_nloc[ityp].atom_index[iat];
+}
+
+void ref_nloc_copy(int ityp, int iat, int *grid_pos, double *chi)
+{
+    int ndc = S.Atom_Influence_nloc[ityp].ndc[iat];
+    int np = S.nlocProj[ityp].nproj;
+    memcpy(grid_pos, S.Atom_Influence_nloc[ityp].grid_pos[iat], sizeof(int) * ndc);
+    if (np > 0) memcpy(chi, S.nlocProj[ityp].Chi[iat], sizeof(double) * ndc * np);
+}
+
+void ref_atom_positions(double *xyz) { memcpy(xyz, S.atom_pos, sizeof(double) * 3 * S.n_atom); }
+
+/* pseudocharge density b, reference b_ref, initial density (superposition of atoms) */
+void ref_setup_fields(double *b, double *bref, double *rho0, double *scalars)
+{
+    memcpy(b, S.psdChrgDens, sizeof(double) * S.Nd);
+    memcpy(bref, S.psdChrgDens_ref, sizeof(double) * S.Nd);
+    memcpy(rho0, S.electronDens, sizeof(double) * S.Nd);
+    scalars[0] = S.Esc;
+    scalars[1] = 0.0;
+    scalars[2] = S.NegCharge;
+    scalars[3] = S.Nelectron;
+}
+
+static int g_dims1[3] = {1, 1, 1};
+
+void ref_lap_plus_diag(int ncol, double a, double b, double c, const double *v, const double *x,
+                       double *y)
+{
+    Lap_plus_diag_vec_mult_orth(&S, S.Nd, S.DMVertices_dmcomm, ncol, a, b, c, v, x, S.Nd, y,
+                                S.Nd, S.dmcomm, g_dims1);
+}
+
+void ref_vnl(int ncol, double *x, double *hx)
+{
+    Vnl_vec_mult(&S, S.Nd, S.Atom_Influence_nloc, S.nlocProj, ncol, x, S.Nd, hx, S.Nd,
+                 S.dmcomm);
+}
+
+void ref_hamiltonian(int ncol, double *veff, double c, double *x, double *hx)
+{
+    Hamiltonian_vectors_mult(&S, S.Nd, S.DMVertices_dmcomm, veff, S.Atom_Influence_nloc,
+                             S.nlocProj, ncol, c, x, S.Nd, hx, S.Nd, 0, S.dmcomm);
+}
+
+void ref_chebyshev(double *veff, int ncol, int m, double a, double b, double a0, double *X,
+                   double *Y)
+{
+    double t;
+    double *save = S.Veff_loc_dmcomm;
+    int save_spin = S.spin_start_indx;
+    S.Veff_loc_dmcomm = veff;
+    S.spin_start_indx = 0;
+    ChebyshevFiltering(&S, S.DMVertices_dmcomm, X, S.Nd, Y, S.Nd, ncol, m, a, b, a0, 0, 0,
+                       S.dmcomm, &t);
+    S.Veff_loc_dmcomm = save;
+    S.spin_start_indx = save_spin;
+}
+
+void ref_poisson_residual(double c, double *x, double *b, double *r)
+{
+    double t;
+    poisson_residual(&S, S.Nd, c, x, b, r, S.dmcomm, &t);
+}

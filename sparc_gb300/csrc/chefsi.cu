@@ -1,0 +1,114 @@
+// Hamiltonian apply and Chebyshev filter on device-resident blocks.
+//
+// Hamiltonian_vectors_mult (src/hamiltonianVecRoutines.c:45-121) becomes three launches on
+// the context stream: nonlocal projection (alpha = dV * Gamma * Chiᵀ x), the fused stencil
+// (-0.5*Lap + Veff + c, scaled, plus the optional Chebyshev term), and the owner-computes
+// nonlocal apply into the same output.
+//
+// ChebyshevFiltering (src/eigenSolver.c:722-798) keeps the reference's scalar recurrence
+// (e, c, sigma, sigma1, gamma, sigma2, vscal, vscal2) but writes each new iterate in place
+// over the oldest one (its last reader is the thread that writes it), so the filter needs at
+// most one scratch block and no separate scale/axpy/swap pass.
+#include "sgpu_internal.h"
+
+namespace sgpu {
+
+template <typename T>
+static const T *veff_of(sgpu_ctx *ctx, int spin);
+template <>
+const double *veff_of<double>(sgpu_ctx *ctx, int spin)
+{
+    return ctx->veff64 ? ctx->veff64 + (long)spin * ctx->Nd : nullptr;
+}
+template <>
+const float *veff_of<float>(sgpu_ctx *ctx, int spin)
+{
+    return ctx->veff32 ? ctx->veff32 + (long)spin * ctx->Nd : nullptr;
+}
+
+template <typename T>
+int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, long ldx, T *hx,
+                    long ldh, double s1, double s2, const T *z, long ldz, cudaStream_t st)
+{
+    if (spin < 0 || spin >= ctx->nspin_veff) {
+        set_error("Hamiltonian: no local potential set for this spin block");
+        return SGPU_ERR_STATE;
+    }
+    T *alpha = nullptr;
+    if (ctx->has_nl && ctx->nl.ntot > 0) {
+        const size_t bytes = sizeof(T) * (size_t)ctx->nl.ntot * ncol;
+        SGPU_TRY(ws_get(ctx, WS_ALPHA, bytes, (void **)&alpha));
+        SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, bytes, st));
+        SGPU_TRY(launch_nonlocal_project<T>(ctx, ncol, x, ldx, alpha, st));
+    }
+    SGPU_TRY(launch_stencil<T>(ctx, ncol, -0.5, 1.0, c, veff_of<T>(ctx, spin), x, ldx, hx, ldh,
+                               s1, s2, z, ldz, st));
+    if (alpha) SGPU_TRY(launch_nonlocal_apply<T>(ctx, ncol, alpha, s1, hx, ldh, st));
+    return SGPU_OK;
+}
+
+// On return the filtered block is in Y and the degree m-1 iterate in X, as in the reference.
+// Each new iterate is written in place over the oldest one, so iterate j lands in X's buffer
+// for odd j when the first output goes to Y. When m-1 is odd that would leave the result in
+// X, so the first two iterates are routed through one scratch block instead (step 0 into W,
+// step 1 into Y, step 2 into X) and the parities line up with no extra pass.
+template <typename T>
+int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int ncol, int m,
+                  double a, double b, double a0, cudaStream_t st)
+{
+    if (m < 1) {
+        set_error("ChebyshevFiltering: degree must be >= 1");
+        return SGPU_ERR_ARG;
+    }
+    const double e = 0.5 * (b - a);
+    const double c = 0.5 * (b + a);
+    double sigma = e / (a0 - c);
+    const double sigma1 = sigma;
+    const double gamma = 2.0 / sigma1;
+    const long Nd = ctx->Nd;
+
+    T *W = nullptr;
+    const bool route = ((m - 1) % 2) == 1;
+    if (route) SGPU_TRY(ws_get(ctx, WS_STAGE_C, sizeof(T) * (size_t)Nd * ncol, (void **)&W));
+
+    // Y_0 = (sigma1/e) (H - c I) X
+    T *y0 = route ? W : Y;
+    long ly0 = route ? Nd : ldy;
+    SGPU_TRY(hamiltonian_dev<T>(ctx, spin, ncol, -c, X, ldx, y0, ly0, sigma1 / e, 0.0, nullptr,
+                                0, st));
+    // (cur, prev) = (Y_j, Y_{j-1}) with Y_{-1} = X
+    T *cur = y0, *prev = X;
+    long ldc = ly0, ldp = ldx;
+    for (int j = 1; j < m; j++) {
+        const double sigma2 = 1.0 / (gamma - sigma);
+        const double vscal = 2.0 * sigma2 / e;
+        const double vscal2 = sigma * sigma2;
+        // Y_j = vscal (H - c I) Y_{j-1} - vscal2 Y_{j-2}
+        T *dst = prev;
+        long ldd = ldp;
+        if (route && j == 1) { dst = Y; ldd = ldy; }
+        if (route && j == 2) { dst = X; ldd = ldx; }
+        SGPU_TRY(hamiltonian_dev<T>(ctx, spin, ncol, -c, cur, ldc, dst, ldd, vscal, -vscal2,
+                                    prev, ldp, st));
+        prev = cur; ldp = ldc;
+        cur = dst; ldc = ldd;
+        sigma = sigma2;
+    }
+    if (route && m == 2) {  // the degree-1 iterate is still in the scratch block
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(X, sizeof(T) * ldx, W, sizeof(T) * Nd, sizeof(T) * Nd,
+                                        ncol, cudaMemcpyDeviceToDevice, st));
+    }
+    return SGPU_OK;
+}
+
+template int hamiltonian_dev<double>(sgpu_ctx *, int, int, double, const double *, long,
+                                     double *, long, double, double, const double *, long,
+                                     cudaStream_t);
+template int hamiltonian_dev<float>(sgpu_ctx *, int, int, double, const float *, long, float *,
+                                    long, double, double, const float *, long, cudaStream_t);
+template int chebyshev_dev<double>(sgpu_ctx *, int, double *, long, double *, long, int, int,
+                                   double, double, double, cudaStream_t);
+template int chebyshev_dev<float>(sgpu_ctx *, int, float *, long, float *, long, int, int,
+                                  double, double, double, cudaStream_t);
+
+}  // namespace sgpu

@@ -1,0 +1,171 @@
+// Internal declarations of the GB300 CheFSI library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/sparc_gpu.h"
+
+namespace sgpu {
+
+constexpr int kMaxFDn = 6;  // the library is specialised for FD order 12 (radius 6)
+
+// thread-local error text, returned by sgpu_last_error()
+void set_error(const std::string &msg);
+
+#define SGPU_CUDA_TRY(...)                                                                   \
+    do {                                                                                     \
+        cudaError_t err_ = (__VA_ARGS__);                                                    \
+        if (err_ != cudaSuccess) {                                                           \
+            ::sgpu::set_error(std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(err_));  \
+            return SGPU_ERR_CUDA;                                                            \
+        }                                                                                    \
+    } while (0)
+
+#define SGPU_CUBLAS_TRY(call)                                                                \
+    do {                                                                                     \
+        cublasStatus_t st_ = (call);                                                         \
+        if (st_ != CUBLAS_STATUS_SUCCESS) {                                                  \
+            ::sgpu::set_error(std::string(#call) + ": cuBLAS status " + std::to_string(st_)); \
+            return SGPU_ERR_CUDA;                                                            \
+        }                                                                                    \
+    } while (0)
+
+#define SGPU_TRY(...)                                                                        \
+    do {                                                                                     \
+        int rc_ = (__VA_ARGS__);                                                                    \
+        if (rc_ != SGPU_OK) return rc_;                                                      \
+    } while (0)
+
+// Device copy of the nonlocal projector set, in two index orders:
+//  * image order (as the reference's Atom_Influence_nloc / nlocProj): for the projection
+//    alpha = Chiᵀ x, parallel over (image, point chunk);
+//  * point order (a CSR over covered grid points): for the owner-computes apply
+//    Hx[p] += sum over entries (image, i) of Chi_img[i, :] alpha_atom.
+struct Nonlocal {
+    int natom = 0, nimg = 0, ntot = 0, max_np = 0;
+    long nchi = 0, npos = 0;
+    int *ip_displ = nullptr;    // natom + 1
+    int *img_atom = nullptr;    // nimg
+    int *img_ndc = nullptr;     // nimg
+    long *img_off = nullptr;    // nimg, offset of the image's grid positions
+    long *img_chi_off = nullptr;// nimg, offset of the image's Chi block
+    int *grid_pos = nullptr;    // npos
+    double *chi64 = nullptr;    // nchi, per image ndc x np column-major
+    float *chi32 = nullptr;
+    double *gamma64 = nullptr;  // ntot, per projector
+    float *gamma32 = nullptr;
+    // projection work items: (image, first point) chunks of kProjChunk points
+    int nwork = 0;
+    int *work_img = nullptr;
+    int *work_start = nullptr;
+    // point CSR for the apply
+    int ncov = 0;
+    long nent = 0;
+    int *cov_pt = nullptr;      // ncov covered grid points, ascending
+    int *cov_ptr = nullptr;     // ncov + 1
+    int *ent_img = nullptr;     // nent
+    int *ent_i = nullptr;       // nent
+};
+
+constexpr int kProjChunk = 256;
+
+struct Workspace {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace sgpu
+
+struct sgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int Nx = 0, Ny = 0, Nz = 0, FDn = 0;
+    long Nd = 0;
+    double cx[sgpu::kMaxFDn + 1] = {0}, cy[sgpu::kMaxFDn + 1] = {0}, cz[sgpu::kMaxFDn + 1] = {0};
+    double dV = 0.0;
+    int nspin_veff = 0;
+    double *veff64 = nullptr;  // Nd * nspin
+    float *veff32 = nullptr;
+    sgpu::Nonlocal nl;
+    bool has_nl = false;
+    cublasHandle_t cublas = nullptr;
+    cusolverDnHandle_t cusolver = nullptr;
+    sgpu::Workspace ws[8];     // grow-only scratch slots (see enum WsSlot)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_filter_ms = 0.f;
+    // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on
+    // the context stream, resolved by sgpu_profile_read
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_pool;
+    size_t prof_next = 0;
+    struct ProfRec { int kind; cudaEvent_t a, b; };
+    std::vector<ProfRec> prof_pending;
+    double prof_ms[SGPU_KERNEL_KINDS] = {0};
+    long prof_n[SGPU_KERNEL_KINDS] = {0};
+    long launches = 0;  // kernels launched by this context since the last profile reset
+};
+
+namespace sgpu {
+
+enum WsSlot { WS_STAGE_A = 0, WS_STAGE_B, WS_STAGE_C, WS_ALPHA, WS_MISC, WS_EIG, WS_POIS, WS_MIX };
+
+// grow-only device scratch
+int ws_get(sgpu_ctx *ctx, int slot, size_t bytes, void **out);
+
+// profiling: returns an event pair recorded around a launch of `kind` (or nulls when off)
+struct ProfScope {
+    sgpu_ctx *ctx;
+    int kind;
+    cudaStream_t st;
+    cudaEvent_t b = nullptr;
+    ProfScope(sgpu_ctx *c, int k, cudaStream_t s);
+    ~ProfScope();
+};
+
+// memory-kind query: true when p is device (or managed) memory this context can use directly
+bool is_device_ptr(const void *p);
+
+// ---- stencil (stencil.cu)
+// out[:, n] = s1 * ( a*Lap + bv*diag(v) + c*I ) x[:, n]  +  s2 * z[:, n]
+// (z may be null; v may be null). All arrays column-major with the given leading dims.
+template <typename T>
+int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const T *v,
+                   const T *x, long ldx, T *out, long ldo, double s1, double s2, const T *z,
+                   long ldz, cudaStream_t st);
+
+// ---- nonlocal (nonlocal.cu)
+template <typename T>
+int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha,
+                            cudaStream_t st);
+template <typename T>
+int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, double scale, T *out,
+                          long ldo, cudaStream_t st);
+int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double *gamma,
+                    int nimg, const int *img_atom, const int *img_ndc, const int *grid_pos,
+                    const double *chi);
+void nonlocal_free(Nonlocal &nl);
+
+// ---- Hamiltonian and filter (chefsi.cu)
+template <typename T>
+int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, long ldx, T *hx,
+                    long ldh, double s1, double s2, const T *z, long ldz, cudaStream_t st);
+template <typename T>
+int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int ncol, int m,
+                  double a, double b, double a0, cudaStream_t st);
+
+// ---- elementwise helpers (util.cu)
+template <typename T>
+int swap_blocks(T *a, long lda, T *b, long ldb, long rows, int ncol, cudaStream_t st);
+// dst[:, n] = (Tout) src[:, n] for column blocks of `rows` rows
+template <typename Tin, typename Tout>
+int convert_cols(const Tin *src, long lds, Tout *dst, long ldd, long rows, int ncol,
+                 cudaStream_t st);
+
+}  // namespace sgpu

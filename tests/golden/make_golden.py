@@ -1,0 +1,119 @@
+"""Generate the committed golden fixtures from the reference SPARC program.
+
+Needs the reference sources (default /root/reference) and the oracle build
+(`make -C oracle/ref REF=...`). For each system in systems.py it runs the reference's own
+set-up, records grid, FD weights and nonlocal projectors, then calls the reference kernels
+(Lap_plus_diag_vec_mult_orth, Vnl_vec_mult, Hamiltonian_vectors_mult, ChebyshevFiltering,
+poisson_residual) on seeded inputs and stores inputs and outputs in tests/golden/<name>.npz.
+
+usage: python tests/golden/make_golden.py [--ref /path/to/SPARC]
+"""
+import argparse
+import multiprocessing as mp
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import systems  # noqa: E402
+
+
+def flatten_nonlocal(types, images, n_atom):
+    """Flatten reference nonlocal data into the library's layout (see include/sparc_gpu.h)."""
+    # per-atom projector count: atoms are numbered type by type, as in the reference
+    nproj_atom = []
+    gamma_atom = []
+    for t in types:
+        g = []
+        off = 0
+        for l in range(t["lmax"] + 1):
+            if l == t["lloc"]:
+                off += int(t["ppl"][l])
+                continue
+            for p in range(int(t["ppl"][l])):
+                g += [t["gamma"][off + p]] * (2 * l + 1)
+            off += int(t["ppl"][l])
+        for _ in range(t["natom"]):
+            nproj_atom.append(len(g))
+            gamma_atom.append(np.array(g))
+    assert len(nproj_atom) == n_atom
+    ip = np.concatenate([[0], np.cumsum(nproj_atom)]).astype(np.int32)
+    gamma = np.concatenate(gamma_atom) if gamma_atom else np.zeros(0)
+    img_atom = np.array([im["atom_index"] for im in images], dtype=np.int32)
+    img_ndc = np.array([len(im["grid_pos"]) for im in images], dtype=np.int32)
+    grid_pos = np.concatenate([im["grid_pos"] for im in images]).astype(np.int32)
+    chi = np.concatenate([im["chi"].T.reshape(-1) for im in images])  # column-major per image
+    return dict(ip_displ=ip, gamma=gamma, img_atom=img_atom, img_ndc=img_ndc,
+                grid_pos=grid_pos, chi=chi)
+
+
+def smooth_potential(rng, Nx, Ny, Nz, L, ncenters=6, amp=-1.5, width=1.2):
+    """Sum of periodic Gaussians: a seeded, smooth stand-in for a local potential."""
+    x = (np.arange(Nx) + 0.0) * L[0] / Nx
+    y = (np.arange(Ny) + 0.0) * L[1] / Ny
+    z = (np.arange(Nz) + 0.0) * L[2] / Nz
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    v = np.zeros((Nz, Ny, Nx))
+    for c in rng.uniform(0, 1, size=(ncenters, 3)) * np.array(L):
+        d = [np.minimum(np.abs(G - cc), Ld - np.abs(G - cc)) for G, cc, Ld in zip((X, Y, Z), c, L)]
+        v += amp * np.exp(-(d[0] ** 2 + d[1] ** 2 + d[2] ** 2) / (2 * width ** 2))
+    return v.reshape(-1)
+
+
+def capture(sysd, psp_dir, out_path, ncol, seed, cheb_m, cheb_bounds):
+    from ref_capture import RefSystem
+
+    tmp = tempfile.mkdtemp(prefix="sparc_golden_")
+    base = systems.write_system(sysd, tmp, psp_dir)
+    r = RefSystem(base)
+    types, images = r.nonlocal_data()
+    flat = flatten_nonlocal(types, images, r.n_atom)
+    rng = np.random.default_rng(seed)
+    Nd = r.Nd
+    x = rng.uniform(-1.0, 1.0, size=(ncol, Nd))
+    veff = smooth_potential(rng, r.Nx, r.Ny, r.Nz, r.L)
+    fields = r.setup_fields()
+    out = dict(
+        Nx=r.Nx, Ny=r.Ny, Nz=r.Nz, FDn=r.order // 2, h=r.h, L=r.L, dV=r.dV,
+        cx=r.cx, cy=r.cy, cz=r.cz, n_atom=r.n_atom, x=x, veff=veff,
+        lap_plus_diag=r.lap_plus_diag(-0.5, 1.0, 0.3, veff, x),
+        lap=r.lap_plus_diag(1.0, 0.0, 0.0, None, x[:1]),
+        vnl=r.vnl(x),
+        hamiltonian=r.hamiltonian(veff, -1.2, x),
+        b=fields["b"], rho0=fields["rho0"],
+        poisson_residual=r.poisson_residual(0.0, x[0], fields["b"]),
+        cheb_m=cheb_m, cheb_bounds=np.array(cheb_bounds),
+        **{"nl_" + k: v for k, v in flat.items()},
+    )
+    Xo, Yo = r.chebyshev(veff, cheb_m, cheb_bounds[0], cheb_bounds[1], cheb_bounds[2], x)
+    out["cheb_X"] = Xo
+    out["cheb_Y"] = Yo
+    np.savez_compressed(out_path, **out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    psp_dir = os.path.join(args.ref, "psps")
+    jobs = [
+        (systems.si2_small(), os.path.join(HERE, "si2_small_kernels.npz"), 3, 11, 12,
+         (0.5, 40.0, -0.8)),
+        (systems.si8_c1(), os.path.join(HERE, "si8_kernels.npz"), 1, 12, 20, (0.4, 45.0, -1.0)),
+    ]
+    ctx = mp.get_context("spawn")
+    for sysd, path, ncol, seed, m, bounds in jobs:
+        p = ctx.Process(target=capture, args=(sysd, psp_dir, path, ncol, seed, m, bounds))
+        p.start()
+        p.join()
+        if p.exitcode != 0:
+            raise SystemExit(f"capture failed for {sysd['name']}")
+        print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+"""Capture set-up data and kernel outputs from the reference SPARC objects.
+
+Runs only where the reference was compiled (oracle/_ref/libsparc_ref.so, built by
+oracle/ref/Makefile). Each capture runs in its own process because the reference keeps one
+SPARC_OBJ per process. Used by make_golden.py to write the committed fixtures.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_LIB = os.path.join(HERE, "..", "..", "oracle", "_ref", "libsparc_ref.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class RefSystem:
+    """The reference's own set-up of one .inpt/.ion system, with its kernels callable."""
+
+    def __init__(self, base):
+        self.lib = ctypes.CDLL(os.path.abspath(REF_LIB))
+        cwd = os.getcwd()
+        os.chdir(os.path.dirname(base))
+        try:
+            self.lib.ref_init(os.path.basename(base).encode())
+        finally:
+            os.chdir(cwd)
+        dims = np.zeros(10, dtype=np.int32)
+        self.lib.ref_dims(_i(dims))
+        self.Nx, self.Ny, self.Nz, self.Nd, self.order, self.n_atom, self.Ntypes, \
+            self.Nstates, self.nproj_total, self.cell_typ = [int(v) for v in dims]
+        g = np.zeros(7)
+        self.lib.ref_grid(_d(g))
+        self.h = g[0:3].copy()
+        self.dV = float(g[3])
+        self.L = g[4:7].copy()
+        fdn = self.order // 2
+        self.cx, self.cy, self.cz = (np.zeros(fdn + 1) for _ in range(3))
+        self.lib.ref_d2coeffs(_d(self.cx), _d(self.cy), _d(self.cz))
+
+    def nonlocal_data(self):
+        """Per atom image: (type, atom_index, grid_pos, Chi[ndc x nproj] column-major)."""
+        types = []
+        images = []
+        for t in range(self.Ntypes):
+            ints = np.zeros(16, dtype=np.int32)
+            gam = np.zeros(64)
+            self.lib.ref_psd(t, _i(ints), _d(gam))
+            lmax, lloc, nproj, nat = (int(v) for v in ints[:4])
+            ppl = ints[4:4 + lmax + 1].copy()
+            types.append(dict(lmax=lmax, lloc=lloc, nproj=nproj, natom=nat, ppl=ppl,
+                              gamma=gam[:int(ppl.sum())].copy()))
+            for iat in range(self.lib.ref_nloc_natom(t)):
+                info = np.zeros(2, dtype=np.int32)
+                self.lib.ref_nloc_atom(t, iat, _i(info))
+                ndc = int(info[0])
+                gp = np.zeros(ndc, dtype=np.int32)
+                chi = np.zeros(ndc * max(nproj, 1))
+                self.lib.ref_nloc_copy(t, iat, _i(gp), _d(chi))
+                images.append(dict(type=t, atom_index=int(info[1]), grid_pos=gp,
+                                   chi=chi[:ndc * nproj].reshape(nproj, ndc).T.copy()))
+        return types, images
+
+    def setup_fields(self):
+        b, bref, rho0 = (np.zeros(self.Nd) for _ in range(3))
+        sc = np.zeros(4)
+        self.lib.ref_setup_fields(_d(b), _d(bref), _d(rho0), _d(sc))
+        return dict(b=b, bref=bref, rho0=rho0, Esc=sc[0], NegCharge=sc[2], Nelectron=sc[3])
+
+    def atom_positions(self):
+        xyz = np.zeros(3 * self.n_atom)
+        self.lib.ref_atom_positions(_d(xyz))
+        return xyz.reshape(-1, 3)
+
+    # ---- kernels (x, y column-major: shape (ncol, Nd) C-contiguous == Nd x ncol col-major)
+    def lap_plus_diag(self, a, b, c, v, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        vv = np.ascontiguousarray(v, dtype=np.float64) if v is not None else None
+        self.lib.ref_lap_plus_diag(ctypes.c_int(x.shape[0]), ctypes.c_double(a),
+                                   ctypes.c_double(b), ctypes.c_double(c),
+                                   _d(vv) if vv is not None else None, _d(x), _d(y))
+        return y
+
+    def vnl(self, x, hx0=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        hx = np.zeros_like(x) if hx0 is None else np.array(hx0, dtype=np.float64)
+        self.lib.ref_vnl(ctypes.c_int(x.shape[0]), _d(x), _d(hx))
+        return hx
+
+    def hamiltonian(self, veff, c, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        hx = np.zeros_like(x)
+        veff = np.ascontiguousarray(veff, dtype=np.float64)
+        self.lib.ref_hamiltonian(ctypes.c_int(x.shape[0]), _d(veff), ctypes.c_double(c),
+                                 _d(x), _d(hx))
+        return hx
+
+    def chebyshev(self, veff, m, a, b, a0, X):
+        X = np.array(X, dtype=np.float64, order="C")
+        Y = np.zeros_like(X)
+        veff = np.ascontiguousarray(veff, dtype=np.float64)
+        self.lib.ref_chebyshev(_d(veff), ctypes.c_int(X.shape[0]), ctypes.c_int(m),
+                               ctypes.c_double(a), ctypes.c_double(b), ctypes.c_double(a0),
+                               _d(X), _d(Y))
+        return X, Y
+
+    def poisson_residual(self, c, x, b):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        r = np.zeros_like(x)
+        self.lib.ref_poisson_residual(ctypes.c_double(c), _d(x), _d(b), _d(r))
+        return r

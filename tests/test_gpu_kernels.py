@@ -1,0 +1,172 @@
+"""GPU parity of the hot-path kernels, through the C ABI (libsparc_gpu.so).
+
+Reference values: the golden fixtures produced by the reference SPARC program
+(tests/golden/*.npz), and the CPU oracle on fresh seeded inputs at other sizes.
+Tolerances: FP64 paths 1e-12 relative to the largest output magnitude (the reference and the
+GPU differ only by rounding and FMA contraction); FP32 filter 5e-4 relative."""
+import numpy as np
+import pytest
+
+import sparc_gb300 as sg
+from golden_io import CASES, load, rel_err
+from oracle.oracle import Oracle
+from sparc_gb300.synthetic import fd_d2_coeffs, synthetic_nonlocal
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32_H = 2e-6
+TOL32_FILTER = 5e-4
+
+
+def make_ctx(grid, nl, veff):
+    ctx = sg.Context(grid["Nx"], grid["Ny"], grid["Nz"], grid["FDn"], grid["cx"], grid["cy"],
+                     grid["cz"], grid["dV"])
+    if veff is not None:
+        ctx.set_veff(veff)
+    if nl is not None:
+        ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
+                         nl["grid_pos"], nl["chi"])
+    return ctx
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_golden_stencil(gpu_available, case):
+    d, grid, nl = load(case)
+    ctx = make_ctx(grid, nl, d["veff"])
+    x = d["x"]
+    y = np.zeros_like(x)
+    ctx.Lap_plus_diag_vec_mult_orth(-0.5, 1.0, 0.3, d["veff"], x, y)
+    assert rel_err(y, d["lap_plus_diag"]) < TOL64
+    y1 = np.zeros_like(x[:1])
+    ctx.Lap_vec_mult(0.0, np.ascontiguousarray(x[:1]), y1)
+    assert rel_err(y1, d["lap"]) < TOL64
+    r = np.zeros(ctx.Nd)
+    ctx.poisson_residual(0.0, np.ascontiguousarray(x[0]), d["b"], r)
+    assert rel_err(r, d["poisson_residual"]) < TOL64
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_golden_nonlocal_and_hamiltonian(gpu_available, case):
+    d, grid, nl = load(case)
+    ctx = make_ctx(grid, nl, d["veff"])
+    hx = np.zeros_like(d["x"])
+    ctx.Vnl_vec_mult(d["x"], hx)
+    assert rel_err(hx, d["vnl"]) < TOL64
+    hx2 = np.zeros_like(d["x"])
+    ctx.Hamiltonian_vectors_mult(-1.2, d["x"], hx2)
+    assert rel_err(hx2, d["hamiltonian"]) < TOL64
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("prec", [sg.SGPU_PREC_FP64, sg.SGPU_PREC_FP32])
+def test_golden_chebyshev(gpu_available, case, prec):
+    d, grid, nl = load(case)
+    ctx = make_ctx(grid, nl, d["veff"])
+    X = d["x"].copy()
+    Y = np.zeros_like(X)
+    b = d["cheb_bounds"]
+    ctx.ChebyshevFiltering(X, Y, int(d["cheb_m"]), b[0], b[1], b[2], precision=prec)
+    tol = TOL64 if prec == sg.SGPU_PREC_FP64 else TOL32_FILTER
+    assert rel_err(Y, d["cheb_Y"]) < tol
+    assert rel_err(X, d["cheb_X"]) < tol
+
+
+GRIDS = [(13, 17, 19), (32, 8, 12), (40, 33, 7), (6, 6, 6), (64, 24, 30)]
+
+
+def _random_case(shape, seed, natom=3):
+    rng = np.random.default_rng(seed)
+    h = (0.41, 0.37, 0.45)
+    grid = dict(Nx=shape[0], Ny=shape[1], Nz=shape[2], FDn=6, cx=fd_d2_coeffs(6, h[0]),
+                cy=fd_d2_coeffs(6, h[1]), cz=fd_d2_coeffs(6, h[2]), dV=h[0] * h[1] * h[2])
+    Nd = shape[0] * shape[1] * shape[2]
+    veff = rng.normal(0.0, 1.0, Nd)
+    nl = synthetic_nonlocal(rng, shape, 0.4, natom=natom, rc=1.6) if natom else None
+    return grid, nl, veff, rng
+
+
+@pytest.mark.parametrize("shape", GRIDS)
+def test_random_grids_vs_oracle(gpu_available, shape):
+    grid, nl, veff, rng = _random_case(shape, seed=sum(shape))
+    Nd = shape[0] * shape[1] * shape[2]
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    x = rng.uniform(-1, 1, (5, Nd))
+    y = np.zeros_like(x)
+    ctx.Lap_plus_diag_vec_mult_orth(0.7, -0.4, 1.3, veff, x, y)
+    assert rel_err(y, o.lap_plus_diag(0.7, -0.4, 1.3, veff, x)) < TOL64
+    h = np.zeros_like(x)
+    ctx.Hamiltonian_vectors_mult(0.25, x, h)
+    assert rel_err(h, o.hamiltonian(veff, 0.25, x)) < TOL64
+    for m in (1, 2, 3, 8):
+        X = x.copy(); Y = np.zeros_like(x)
+        ctx.ChebyshevFiltering(X, Y, m, 0.2, 30.0, -3.0)
+        Xo, Yo = o.chebyshev(veff, m, 0.2, 30.0, -3.0, x)
+        assert rel_err(Y, Yo) < TOL64, m
+        assert rel_err(X, Xo) < TOL64, m
+
+
+def test_fp32_hamiltonian_and_filter_tolerance(gpu_available):
+    grid, nl, veff, rng = _random_case((48, 40, 36), seed=5, natom=6)
+    Nd = 48 * 40 * 36
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    x = rng.uniform(-1, 1, (4, Nd))
+    X = x.copy(); Y = np.zeros_like(x)
+    ctx.ChebyshevFiltering(X, Y, 20, 0.5, 50.0, -1.0, precision=sg.SGPU_PREC_FP32)
+    Xo, Yo = o.chebyshev(veff, 20, 0.5, 50.0, -1.0, x)
+    assert rel_err(Y, Yo) < TOL32_FILTER
+    assert rel_err(X, Xo) < TOL32_FILTER
+
+
+def test_device_pointers_match_host(gpu_available):
+    import torch
+    grid, nl, veff, rng = _random_case((24, 20, 16), seed=9)
+    Nd = 24 * 20 * 16
+    ctx = make_ctx(grid, nl, veff)
+    x = rng.uniform(-1, 1, (3, Nd))
+    Xh = x.copy(); Yh = np.zeros_like(x)
+    ctx.ChebyshevFiltering(Xh, Yh, 7, 0.3, 25.0, -2.0)
+    Xd = torch.from_numpy(x.copy()).cuda(); Yd = torch.zeros_like(Xd)
+    ctx.ChebyshevFiltering(Xd, Yd, 7, 0.3, 25.0, -2.0)
+    np.testing.assert_array_equal(Yd.cpu().numpy(), Yh)
+    np.testing.assert_array_equal(Xd.cpu().numpy(), Xh)
+
+
+def test_leading_dimension_padding(gpu_available):
+    import ctypes
+    grid, nl, veff, rng = _random_case((16, 18, 14), seed=11)
+    Nd = 16 * 18 * 14
+    ld = Nd + 37
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    xb = rng.uniform(-1, 1, (2, ld))
+    hb = np.full((2, ld), 7.0)
+    rc = sg.lib().sgpu_Hamiltonian_vectors_mult(ctx._h, 0, 2, ctypes.c_double(-0.5),
+                                                sg._ptr(xb), ld, sg._ptr(hb), ld)
+    assert rc == 0
+    ref = o.hamiltonian(veff, -0.5, np.ascontiguousarray(xb[:, :Nd]))
+    assert rel_err(hb[:, :Nd], ref) < TOL64
+    assert np.all(hb[:, Nd:] == 7.0)  # padding untouched
+
+
+def test_bad_arguments_fail_with_status(gpu_available):
+    grid, nl, veff, rng = _random_case((16, 16, 16), seed=2)
+    ctx = make_ctx(grid, nl, veff)
+    X = rng.uniform(-1, 1, (1, ctx.Nd)); Y = np.zeros_like(X)
+    with pytest.raises(sg.SgpuError):
+        ctx.ChebyshevFiltering(X, Y, 5, 0.3, 25.0, -2.0, precision=16)
+    with pytest.raises(sg.SgpuError):
+        ctx.ChebyshevFiltering(X, Y, 5, 30.0, 25.0, -2.0)  # a > b
+    with pytest.raises(sg.SgpuError):
+        sg.Context(16, 16, 16, 4, np.ones(5), np.ones(5), np.ones(5), 1.0)  # FD order 8
+    with pytest.raises(sg.SgpuError):
+        ctx.set_nonlocal([0, 9], np.ones(9), [0], [3], [0, 1, ctx.Nd], np.ones(27))
+
+
+def test_empty_block_is_a_no_op(gpu_available):
+    grid, nl, veff, rng = _random_case((16, 16, 16), seed=4)
+    ctx = make_ctx(grid, nl, veff)
+    X = np.zeros((0, ctx.Nd)); Y = np.zeros((0, ctx.Nd))
+    ctx.ChebyshevFiltering(X, Y, 5, 0.3, 25.0, -2.0)
