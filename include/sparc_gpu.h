@@ -111,6 +111,117 @@ int sgpu_ChebyshevFiltering_f32(sgpu_ctx *ctx, int spin, float *X, int ldi, floa
 int sgpu_poisson_residual(sgpu_ctx *ctx, double c, const double *x, const double *b,
                           double *r);
 
+/* ------------------------------------------------------------- Rayleigh-Ritz step */
+
+/* HY = H Y (spin block spin), Hp = Yᵀ HY and Mp = Yᵀ Y (Ns x Ns = ncol x ncol, column-major,
+ * full symmetric). Replaces DP_Project_Hamiltonian (src/eigenSolver.c:939) on one process,
+ * including its ACCEL_DGEMM hooks (:1003-1017). */
+int sgpu_Project_Hamiltonian(sgpu_ctx *ctx, int spin, const double *Y, int ldi, double *HY,
+                             int ldo, int ncol, double *Hp, double *Mp);
+
+/* Hp q = lambda Mp q for the Ns x Ns pencil (upper triangles referenced). On return Hp holds
+ * the eigenvectors Q (column-major), lambda the eigenvalues in ascending order, and Mp its
+ * Cholesky factor. Replaces DP_Solve_Generalized_EigenProblem (src/eigenSolver.c:1262),
+ * i.e. LAPACKE_dsygvd(COL_MAJOR, 1, 'V', 'U', ...) at :1318. */
+int sgpu_Solve_Generalized_EigenProblem(sgpu_ctx *ctx, int Ns, double *Hp, double *Mp,
+                                        double *lambda);
+
+/* X = Y Q with Q Ns x Ns (ncol = Ns). Replaces DP_Subspace_Rotation (src/eigenSolver.c:1386). */
+int sgpu_Subspace_Rotation(sgpu_ctx *ctx, const double *Y, int ldi, const double *Q, int ncol,
+                           double *X, int ldo);
+
+/* Lanczos estimate of the smallest and largest eigenvalue of H (spin block spin) from start
+ * vector x0 (Nd values), stopping when both change by less than tol between iterations.
+ * Replaces Lanczos (src/eigenSolver.c:1920) as called by Chebyshevfilter_constants (:589). */
+int sgpu_Lanczos(sgpu_ctx *ctx, int spin, const double *x0, double tol, int maxit,
+                 double *eigmin, double *eigmax);
+
+/* ------------------------------------------------------------------- SCF-side rows */
+
+/* rho = (1/dV) sum_n occfac * occ[n] * psi_n^2 (Gamma point, one spin).
+ * Replaces CalculateDensity_psi (src/electronDensity.c:104). occ: ncol values. */
+int sgpu_CalculateDensity_psi(sgpu_ctx *ctx, const double *psi, int ld, int ncol,
+                              const double *occ, double occfac, double *rho);
+
+/* LDA exchange-correlation (Slater exchange + Perdew-Wang 92 correlation) on
+ * max(rho + rho_core, xc_rhotol): vxc (potential) and exc (energy per particle).
+ * rho_core may be NULL (no core correction). Replaces the LDA_PW branch of Calculate_Vxc
+ * (src/exchangeCorrelation.c:36, slater :459, pw :475, add_rho_core :1254). */
+int sgpu_Calculate_Vxc_LDA_PW(sgpu_ctx *ctx, const double *rho, const double *rho_core,
+                              double xc_rhotol, double *vxc, double *exc);
+
+/* Alternating Anderson-Richardson solve of b + (Lap + c) x = 0 with the Jacobi preconditioner
+ * (x: initial guess in, solution out). Replaces AAR (src/linearSolver.c:37) called with
+ * poisson_residual and Jacobi_preconditioner (src/electrostatics.c:1682). Returns
+ * SGPU_ERR_NOT_CONVERGED (x still written) when max_iter is reached. */
+int sgpu_AAR(sgpu_ctx *ctx, double c, double *x, const double *b, double omega, double beta,
+             int m, int p, double tol, int max_iter, int *iters);
+
+/* phi with -Lap phi = 4 pi (b + rho), zero mean; phi holds the initial guess on entry.
+ * Replaces Calculate_elecstPotential (src/electrostatics.c:1593) for a periodic cell
+ * (AAR with omega = beta = 0.6, m = 7, p = 6). */
+int sgpu_Calculate_elecstPotential(sgpu_ctx *ctx, const double *rho, const double *b,
+                                   double *phi, double tol, int max_iter, int *iters);
+
+/* Periodic-Pulay density mixing. sgpu_Mixing_init sets the parameters (the SPARC_OBJ fields
+ * MixingHistory, PulayFrequency, PulayRestartFlag, MixingParameter, MixingParameterSimple,
+ * MixingPrecond == 1 (Kerker), precond_kerker_kTF, precond_kerker_thresh, TOL_PRECOND,
+ * NegCharge) and the first input density (Update_mixing_hist_xk); each
+ * sgpu_Mixing_periodic_pulay call takes the output density of SCF iteration iter_count in
+ * rho and returns the next input density in rho. The history stays on the device.
+ * Replaces Mixing_periodic_pulay (src/mixing.c:213) and Kerker_precond (:462). */
+int sgpu_Mixing_init(sgpu_ctx *ctx, int history, int pulay_frequency, int pulay_restart,
+                     double mixing_parameter, double mixing_parameter_simple, int kerker,
+                     double kTF, double idiemac, double tol_precond, double neg_charge,
+                     const double *rho_in);
+int sgpu_Mixing_periodic_pulay(sgpu_ctx *ctx, int iter_count, double *rho);
+
+/* error = ||rho_out - rho_in|| / ||rho_out||. Replaces Evaluate_scf_error
+ * (src/electronicGroundState.c:1160). */
+int sgpu_Evaluate_scf_error(sgpu_ctx *ctx, const double *rho_out, const double *rho_in,
+                            double *error);
+
+/* Parameters of a single-point SCF (SPARC_OBJ fields of the same meaning). */
+typedef struct {
+    int Nstates;                /* Nstates */
+    int n_atom;                 /* for per-atom reporting only */
+    double Nelectron;           /* Nelectron */
+    double Beta;                /* 1 / smearing (Ha^-1) */
+    int elec_T_type;            /* 0 Fermi-Dirac, 1 Gaussian */
+    int cheb_degree;            /* ChebDegree */
+    int rho_trigger;            /* rhoTrigger: filter passes in the first SCF iteration */
+    int nchefsi;                /* Nchefsi */
+    double tol_scf, tol_poisson, tol_precond, tol_lanczos;
+    int maxit_scf, minit_scf, maxit_poisson;
+    int mixing_history, pulay_freq, pulay_restart;
+    double mixing_param, mixing_param_simple;
+    int kerker;                 /* MixingPrecond == 1 */
+    double kerker_kTF, kerker_idiemac;
+    double xc_rhotol;
+    double Esc;                 /* self and correction energy of the pseudocharges */
+    int precision;              /* SGPU_PREC_FP64, or SGPU_PREC_FP32 for the mixed mode */
+    double fp64_switch_error;   /* mixed mode: SCF error below which filtering becomes FP64 */
+    unsigned long long seed;    /* initial orbitals and Lanczos start vector */
+    int verbose;
+} sgpu_scf_params;
+
+typedef struct {
+    int scf_iters, converged, fp64_switch_iter;
+    double Etot, Eband, E1, E2, E3, Exc, Esc, Entropy, Efermi, scf_error;
+    double time_s;              /* wall time of the call */
+    double filter_ms;           /* device time of filter + projection products */
+} sgpu_scf_result;
+
+/* Single-point SCF for an orthogonal periodic Gamma-point cell, spin-unpolarised, LDA (PW92),
+ * density mixing: the scf()/scf_loop() flow of src/electronicGroundState.c:607-1155 with
+ * eigSolve_CheFSI, Calculate_occupation and Calculate_Free_Energy, on the context's grid and
+ * nonlocal projectors. b: pseudocharge density (psdChrgDens), rho_init: initial density,
+ * rho_core: model core density for the nonlinear core correction (NULL if none). Outputs the
+ * final input density, Nstates eigenvalues and occupations (any may be NULL). */
+int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b,
+             const double *rho_init, const double *rho_core, double *rho_out,
+             double *lambda_out, double *occ_out, sgpu_scf_result *res);
+
 /* Device time of the last sgpu_ChebyshevFiltering call's filter loop, in milliseconds. */
 int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms);
 

@@ -163,3 +163,49 @@ void ref_poisson_residual(double c, double *x, double *b, double *r)
     double t;
     poisson_residual(&S, S.Nd, c, x, b, r, S.dmcomm, &t);
 }
+
+/* ---- SCF-side rows: the reference's own Calculate_Vxc / Calculate_elecstPotential on a
+ * caller-provided density, and the set-up fields an SCF needs. */
+#include "exchangeCorrelation.h"
+
+/* model core density (NLCC, zeros when the psp has none); returns NLCC_flag */
+int ref_core_density(double *rho_core)
+{
+    if (S.NLCC_flag && S.electronDens_core)
+        memcpy(rho_core, S.electronDens_core, sizeof(double) * S.Nd);
+    else
+        memset(rho_core, 0, sizeof(double) * S.Nd);
+    return S.NLCC_flag;
+}
+
+/* scalars of the SCF set-up: out = Beta, TOL_SCF, TOL_POISSON, TOL_PRECOND, TOL_LANCZOS,
+ * xc_rhotol, ChebDegree, rhoTrigger, MixingParameter, MixingParameterSimple, MixingHistory,
+ * PulayFrequency, MixingPrecond, precond_kerker_kTF, precond_kerker_thresh, MAXIT_POISSON,
+ * MINIT_SCF, MAXIT_SCF, elec_T_type, Nchefsi */
+void ref_scf_params(double *out)
+{
+    out[0] = S.Beta; out[1] = S.TOL_SCF; out[2] = S.TOL_POISSON; out[3] = S.TOL_PRECOND;
+    out[4] = S.TOL_LANCZOS; out[5] = S.xc_rhotol; out[6] = S.ChebDegree; out[7] = S.rhoTrigger;
+    out[8] = S.MixingParameter; out[9] = S.MixingParameterSimple; out[10] = S.MixingHistory;
+    out[11] = S.PulayFrequency; out[12] = S.MixingPrecond; out[13] = S.precond_kerker_kTF;
+    out[14] = S.precond_kerker_thresh; out[15] = S.MAXIT_POISSON; out[16] = S.MINIT_SCF;
+    out[17] = S.MAXIT_SCF; out[18] = S.elec_T_type; out[19] = S.Nchefsi;
+}
+
+/* Vxc and e_xc of the reference for density rho (Calculate_Vxc on the LDA path) */
+void ref_vxc(const double *rho, double *vxc, double *exc)
+{
+    memcpy(S.electronDens, rho, sizeof(double) * S.Nd);
+    Calculate_Vxc(&S);
+    memcpy(vxc, S.XCPotential, sizeof(double) * S.Nd);
+    memcpy(exc, S.e_xc, sizeof(double) * S.Nd);
+}
+
+/* electrostatic potential of the reference for density rho; phi holds the initial guess */
+void ref_poisson(const double *rho, double *phi)
+{
+    memcpy(S.electronDens, rho, sizeof(double) * S.Nd);
+    memcpy(S.elecstPotential, phi, sizeof(double) * S.Nd);
+    Calculate_elecstPotential(&S);
+    memcpy(phi, S.elecstPotential, sizeof(double) * S.Nd);
+}

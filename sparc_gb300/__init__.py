@@ -22,8 +22,47 @@ EXPORTED = [
     "sgpu_set_nonlocal", "sgpu_Lap_plus_diag_vec_mult_orth", "sgpu_Lap_vec_mult",
     "sgpu_Vnl_vec_mult", "sgpu_Hamiltonian_vectors_mult", "sgpu_ChebyshevFiltering",
     "sgpu_poisson_residual", "sgpu_last_filter_ms", "sgpu_profile_enable", "sgpu_profile_read",
-    "sgpu_ChebyshevFiltering_f32", "sgpu_get_stream",
+    "sgpu_ChebyshevFiltering_f32", "sgpu_get_stream", "sgpu_Project_Hamiltonian",
+    "sgpu_Solve_Generalized_EigenProblem", "sgpu_Subspace_Rotation", "sgpu_Lanczos",
+    "sgpu_CalculateDensity_psi", "sgpu_Calculate_Vxc_LDA_PW", "sgpu_AAR",
+    "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
+    "sgpu_Evaluate_scf_error", "sgpu_scf",
 ]
+
+SGPU_ERR_NOT_CONVERGED = 5
+
+
+class ScfParams(ctypes.Structure):
+    """sgpu_scf_params (include/sparc_gpu.h)."""
+    _fields_ = [("Nstates", ctypes.c_int), ("n_atom", ctypes.c_int),
+                ("Nelectron", ctypes.c_double), ("Beta", ctypes.c_double),
+                ("elec_T_type", ctypes.c_int), ("cheb_degree", ctypes.c_int),
+                ("rho_trigger", ctypes.c_int), ("nchefsi", ctypes.c_int),
+                ("tol_scf", ctypes.c_double), ("tol_poisson", ctypes.c_double),
+                ("tol_precond", ctypes.c_double), ("tol_lanczos", ctypes.c_double),
+                ("maxit_scf", ctypes.c_int), ("minit_scf", ctypes.c_int),
+                ("maxit_poisson", ctypes.c_int), ("mixing_history", ctypes.c_int),
+                ("pulay_freq", ctypes.c_int), ("pulay_restart", ctypes.c_int),
+                ("mixing_param", ctypes.c_double), ("mixing_param_simple", ctypes.c_double),
+                ("kerker", ctypes.c_int), ("kerker_kTF", ctypes.c_double),
+                ("kerker_idiemac", ctypes.c_double), ("xc_rhotol", ctypes.c_double),
+                ("Esc", ctypes.c_double), ("precision", ctypes.c_int),
+                ("fp64_switch_error", ctypes.c_double), ("seed", ctypes.c_ulonglong),
+                ("verbose", ctypes.c_int)]
+
+
+class ScfResult(ctypes.Structure):
+    """sgpu_scf_result (include/sparc_gpu.h)."""
+    _fields_ = [("scf_iters", ctypes.c_int), ("converged", ctypes.c_int),
+                ("fp64_switch_iter", ctypes.c_int), ("Etot", ctypes.c_double),
+                ("Eband", ctypes.c_double), ("E1", ctypes.c_double), ("E2", ctypes.c_double),
+                ("E3", ctypes.c_double), ("Exc", ctypes.c_double), ("Esc", ctypes.c_double),
+                ("Entropy", ctypes.c_double), ("Efermi", ctypes.c_double),
+                ("scf_error", ctypes.c_double), ("time_s", ctypes.c_double),
+                ("filter_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 KERNEL_STENCIL, KERNEL_NL_PROJECT, KERNEL_NL_APPLY, KERNEL_OTHER, KERNEL_KINDS = range(5)
 
@@ -157,6 +196,93 @@ class Context:
         _check(lib().sgpu_poisson_residual(self._h, ctypes.c_double(c), _ptr(x), _ptr(b),
                                            _ptr(r)))
         return r
+
+    # ---- Rayleigh-Ritz
+    def Project_Hamiltonian(self, Y, HY, Hp, Mp, spin=0):
+        ncol, ld = self._ncol_ld(Y)
+        _check(lib().sgpu_Project_Hamiltonian(self._h, int(spin), _ptr(Y), ld, _ptr(HY), ld,
+                                              ncol, _ptr(Hp), _ptr(Mp)))
+        return Hp, Mp
+
+    def Solve_Generalized_EigenProblem(self, Hp, Mp, lam):
+        _check(lib().sgpu_Solve_Generalized_EigenProblem(self._h, int(Hp.shape[0]), _ptr(Hp),
+                                                         _ptr(Mp), _ptr(lam)))
+        return Hp, lam
+
+    def Subspace_Rotation(self, Y, Q, X):
+        ncol, ld = self._ncol_ld(Y)
+        _check(lib().sgpu_Subspace_Rotation(self._h, _ptr(Y), ld, _ptr(Q), ncol, _ptr(X), ld))
+        return X
+
+    def Lanczos(self, x0, tol=1e-2, maxit=1000, spin=0):
+        lo, hi = ctypes.c_double(), ctypes.c_double()
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        _check(lib().sgpu_Lanczos(self._h, int(spin), _ptr(x0), ctypes.c_double(tol),
+                                  int(maxit), ctypes.byref(lo), ctypes.byref(hi)))
+        return lo.value, hi.value
+
+    # ---- SCF-side rows
+    def CalculateDensity_psi(self, psi, occ, occfac, rho):
+        ncol, ld = self._ncol_ld(psi)
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        _check(lib().sgpu_CalculateDensity_psi(self._h, _ptr(psi), ld, ncol, _ptr(occ),
+                                               ctypes.c_double(occfac), _ptr(rho)))
+        return rho
+
+    def Calculate_Vxc_LDA_PW(self, rho, rho_core, xc_rhotol, vxc, exc):
+        _check(lib().sgpu_Calculate_Vxc_LDA_PW(self._h, _ptr(rho), _ptr(rho_core),
+                                               ctypes.c_double(xc_rhotol), _ptr(vxc), _ptr(exc)))
+        return vxc, exc
+
+    def AAR(self, c, x, b, omega=0.6, beta=0.6, m=7, p=6, tol=1e-8, max_iter=3000):
+        it = ctypes.c_int()
+        rc = lib().sgpu_AAR(self._h, ctypes.c_double(c), _ptr(x), _ptr(b),
+                            ctypes.c_double(omega), ctypes.c_double(beta), int(m), int(p),
+                            ctypes.c_double(tol), int(max_iter), ctypes.byref(it))
+        if rc not in (SGPU_OK, SGPU_ERR_NOT_CONVERGED):
+            _check(rc)
+        return it.value, rc == SGPU_OK
+
+    def Calculate_elecstPotential(self, rho, b, phi, tol, max_iter=3000):
+        it = ctypes.c_int()
+        _check(lib().sgpu_Calculate_elecstPotential(self._h, _ptr(rho), _ptr(b), _ptr(phi),
+                                                    ctypes.c_double(tol), int(max_iter),
+                                                    ctypes.byref(it)))
+        return it.value
+
+    def Mixing_init(self, rho_in, neg_charge, history=7, pulay_frequency=1, pulay_restart=0,
+                    mixing_parameter=0.3, mixing_parameter_simple=0.3, kerker=1, kTF=1.0,
+                    idiemac=0.1, tol_precond=1e-4):
+        _check(lib().sgpu_Mixing_init(self._h, int(history), int(pulay_frequency),
+                                      int(pulay_restart), ctypes.c_double(mixing_parameter),
+                                      ctypes.c_double(mixing_parameter_simple), int(kerker),
+                                      ctypes.c_double(kTF), ctypes.c_double(idiemac),
+                                      ctypes.c_double(tol_precond), ctypes.c_double(neg_charge),
+                                      _ptr(rho_in)))
+
+    def Mixing_periodic_pulay(self, iter_count, rho):
+        _check(lib().sgpu_Mixing_periodic_pulay(self._h, int(iter_count), _ptr(rho)))
+        return rho
+
+    def Evaluate_scf_error(self, rho_out, rho_in):
+        e = ctypes.c_double()
+        _check(lib().sgpu_Evaluate_scf_error(self._h, _ptr(rho_out), _ptr(rho_in),
+                                             ctypes.byref(e)))
+        return e.value
+
+    def scf(self, params, b, rho_init, rho_core=None, Nstates=None):
+        """Run sgpu_scf; returns (result dict, final density, eigenvalues, occupations)."""
+        Ns = params.Nstates
+        rho = np.zeros(self.Nd)
+        lam = np.zeros(Ns)
+        occ = np.zeros(Ns)
+        res = ScfResult()
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        r0 = np.ascontiguousarray(rho_init, dtype=np.float64)
+        rc_ = None if rho_core is None else np.ascontiguousarray(rho_core, dtype=np.float64)
+        _check(lib().sgpu_scf(self._h, ctypes.byref(params), _ptr(b), _ptr(r0), _ptr(rc_),
+                              _ptr(rho), _ptr(lam), _ptr(occ), ctypes.byref(res)))
+        return res.as_dict(), rho, lam, occ
 
     def profile_enable(self, on=True):
         _check(lib().sgpu_profile_enable(self._h, int(bool(on))))

@@ -208,6 +208,7 @@ int sgpu_destroy(sgpu_ctx *ctx)
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx->mix;
     delete ctx;
     return SGPU_OK;
 }
@@ -292,11 +293,12 @@ int sgpu_Vnl_vec_mult(sgpu_ctx *ctx, int ncol, const double *x, int ldi, double 
     long lx, lh;
     SGPU_TRY(stage_in(ctx, WS_STAGE_A, x, ldi, ncol, true, &dx, &lx));
     SGPU_TRY(stage_in(ctx, WS_STAGE_B, Hx, ldo, ncol, true, &dh, &lh));
-    const size_t bytes = sizeof(double) * (size_t)ctx->nl.ntot * ncol;
+    const long lda = nonlocal_alpha_ld(ncol, (int)sizeof(double));
+    const size_t bytes = sizeof(double) * (size_t)ctx->nl.ntot * lda;
     SGPU_TRY(ws_get(ctx, WS_ALPHA, bytes, (void **)&alpha));
     SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, bytes, ctx->stream));
-    SGPU_TRY(launch_nonlocal_project<double>(ctx, ncol, dx, lx, alpha, ctx->stream));
-    SGPU_TRY(launch_nonlocal_apply<double>(ctx, ncol, alpha, 1.0, dh, lh, ctx->stream));
+    SGPU_TRY(launch_nonlocal_project<double>(ctx, ncol, dx, lx, alpha, lda, ctx->stream));
+    SGPU_TRY(launch_nonlocal_apply<double>(ctx, ncol, alpha, lda, 1.0, dh, lh, ctx->stream));
     SGPU_TRY(stage_out(ctx, dh, lh, Hx, ldo, ncol));
     SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return SGPU_OK;

@@ -35,15 +35,16 @@ int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, lon
         return SGPU_ERR_STATE;
     }
     T *alpha = nullptr;
+    const long lda = nonlocal_alpha_ld(ncol, (int)sizeof(T));
     if (ctx->has_nl && ctx->nl.ntot > 0) {
-        const size_t bytes = sizeof(T) * (size_t)ctx->nl.ntot * ncol;
+        const size_t bytes = sizeof(T) * (size_t)ctx->nl.ntot * lda;
         SGPU_TRY(ws_get(ctx, WS_ALPHA, bytes, (void **)&alpha));
         SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, bytes, st));
-        SGPU_TRY(launch_nonlocal_project<T>(ctx, ncol, x, ldx, alpha, st));
+        SGPU_TRY(launch_nonlocal_project<T>(ctx, ncol, x, ldx, alpha, lda, st));
     }
     SGPU_TRY(launch_stencil<T>(ctx, ncol, -0.5, 1.0, c, veff_of<T>(ctx, spin), x, ldx, hx, ldh,
                                s1, s2, z, ldz, st));
-    if (alpha) SGPU_TRY(launch_nonlocal_apply<T>(ctx, ncol, alpha, s1, hx, ldh, st));
+    if (alpha) SGPU_TRY(launch_nonlocal_apply<T>(ctx, ncol, alpha, lda, s1, hx, ldh, st));
     return SGPU_OK;
 }
 

@@ -22,9 +22,6 @@ namespace sgpu {
 namespace {
 
 constexpr int kProjThreads = 256;
-constexpr int kProjNPB = 8;  // projectors per block
-constexpr int kProjCB = 4;   // columns per block
-constexpr int kApplyCB = 4;  // columns per thread in the apply
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v)
@@ -34,100 +31,116 @@ __device__ __forceinline__ T warp_sum(T v)
     return v;
 }
 
-template <typename T>
+// alpha layout: alpha[row * lda + n], row = IP_displ[atom] + j (projector), n = column;
+// lda is a multiple of the apply's column block so rows can be read as vectors.
+//
+// Projection as a gathered GEMM: block = (atom image g, group of NC columns). The image's
+// points are walked in chunks of PCH: the block gathers x[grid_pos[chunk], n0:n0+NC] into
+// shared memory (coalesced along points for each column) together with the chunk's Chi rows,
+// then thread (n, jg) accumulates alpha[j, n] for j = jg, jg + 8, ... over the chunk. One
+// atomic add per (projector, column) output at the end, with dV * Gamma folded in.
+template <typename T, int PCH, int NC, int MAXJ>
 __global__ void __launch_bounds__(kProjThreads)
     k_nl_project(const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
                  const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
                  const int *__restrict__ grid_pos, const T *__restrict__ chi,
-                 const int *__restrict__ ip_displ, const T *__restrict__ gamma, int ntot,
-                 int ncol, const T *__restrict__ x, long ldx, T *__restrict__ alpha, T dV)
+                 const int *__restrict__ ip_displ, const T *__restrict__ gamma, int ncol,
+                 const T *__restrict__ x, long ldx, T *__restrict__ alpha, long lda, T dV)
 {
+    static_assert(kProjThreads == 8 * NC, "thread (n, jg) layout: NC columns x 8 groups");
+    constexpr int JG = 8;
+    constexpr int NJ = (MAXJ + JG - 1) / JG;
+    __shared__ T xs[NC][PCH + 1];     // +1: conflict-free reads across columns
+    __shared__ T cs[MAXJ][PCH];
     const int g = blockIdx.x;
-    const int jg = blockIdx.y * kProjNPB;
-    const int n0 = blockIdx.z * kProjCB;
+    const int n0 = blockIdx.y * NC;
     const int a = img_atom[g];
     const int np = ip_displ[a + 1] - ip_displ[a];
-    if (jg >= np) return;
     const int ndc = img_ndc[g];
     const int *__restrict__ gp = grid_pos + img_off[g];
     const T *__restrict__ ch = chi + img_chi_off[g];
+    const int t = threadIdx.x;
+    const int n = t % NC, jg = t / NC;
+    T acc[NJ];
+#pragma unroll
+    for (int u = 0; u < NJ; u++) acc[u] = T(0);
 
-    T acc[kProjNPB][kProjCB];
+    for (int i0 = 0; i0 < ndc; i0 += PCH) {
+        const int cnt = min(PCH, ndc - i0);
+        __syncthreads();  // previous chunk consumed
+        // gather: PCH points x NC columns, kProjThreads threads
+        for (int e = t; e < PCH * NC; e += kProjThreads) {
+            const int i = e % PCH, c = e / PCH;
+            T v = T(0);
+            if (i < cnt && n0 + c < ncol) v = __ldg(x + (long)(n0 + c) * ldx + gp[i0 + i]);
+            xs[c][i] = v;
+        }
+        for (int e = t; e < PCH * MAXJ; e += kProjThreads) {
+            const int i = e % PCH, j = e / PCH;
+            cs[j][i] = (i < cnt && j < np) ? __ldg(ch + (long)j * ndc + i0 + i) : T(0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int i = 0; i < PCH; i++) {
+            const T xv = xs[n][i];
 #pragma unroll
-    for (int j = 0; j < kProjNPB; j++)
-#pragma unroll
-        for (int c = 0; c < kProjCB; c++) acc[j][c] = T(0);
-
-    for (int ii = threadIdx.x; ii < ndc; ii += kProjThreads) {
-        const long p = gp[ii];
-        T xv[kProjCB];
-#pragma unroll
-        for (int c = 0; c < kProjCB; c++)
-            xv[c] = (n0 + c < ncol) ? __ldg(x + (long)(n0 + c) * ldx + p) : T(0);
-#pragma unroll
-        for (int j = 0; j < kProjNPB; j++) {
-            if (jg + j < np) {
-                const T cv = __ldg(ch + (long)(jg + j) * ndc + ii);
-#pragma unroll
-                for (int c = 0; c < kProjCB; c++) acc[j][c] += cv * xv[c];
-            }
+            for (int u = 0; u < NJ; u++)
+                if (jg + u * JG < MAXJ) acc[u] += cs[jg + u * JG][i] * xv;
         }
     }
-
-    __shared__ T red[kProjThreads / 32][kProjNPB * kProjCB];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (n0 + n < ncol) {
 #pragma unroll
-    for (int j = 0; j < kProjNPB; j++)
-#pragma unroll
-        for (int c = 0; c < kProjCB; c++) {
-            T v = warp_sum(acc[j][c]);
-            if (lane == 0) red[warp][j * kProjCB + c] = v;
-        }
-    __syncthreads();
-    if (threadIdx.x < kProjNPB * kProjCB) {
-        const int j = threadIdx.x / kProjCB, c = threadIdx.x % kProjCB;
-        if (jg + j < np && n0 + c < ncol) {
-            T s = T(0);
-#pragma unroll
-            for (int w = 0; w < kProjThreads / 32; w++) s += red[w][threadIdx.x];
-            const int row = ip_displ[a] + jg + j;
-            atomicAdd(alpha + (long)(n0 + c) * ntot + row, dV * gamma[row] * s);
+        for (int u = 0; u < NJ; u++) {
+            const int j = jg + u * JG;
+            if (j < np) {
+                const int row = ip_displ[a] + j;
+                atomicAdd(alpha + (long)row * lda + n0 + n, dV * gamma[row] * acc[u]);
+            }
         }
     }
 }
 
-template <typename T>
+template <typename T, int CB>
+struct VecOf;
+template <> struct VecOf<float, 4> { using type = float4; };
+template <> struct VecOf<double, 2> { using type = double2; };
+
+// Apply: one thread per covered grid point and CB columns; alpha rows are read as vectors
+// (VW elements per load, broadcast across the warp when neighbouring points share an atom).
+template <typename T, int CB, int VW>
 __global__ void __launch_bounds__(256)
     k_nl_apply(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
-               const int *__restrict__ ent_img, const int *__restrict__ ent_i,
-               const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
-               const long *__restrict__ img_chi_off, const T *__restrict__ chi,
-               const int *__restrict__ ip_displ, int ntot, int ncol,
-               const T *__restrict__ alpha, T scale, T *__restrict__ out, long ldo)
+               const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+               const T *__restrict__ chi, int ncol, const T *__restrict__ alpha, long lda,
+               T scale, T *__restrict__ out, long ldo)
 {
+    using V = typename VecOf<T, VW>::type;
     const int cidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (cidx >= ncov) return;
-    const int n0 = blockIdx.y * kApplyCB;
-    T acc[kApplyCB];
+    const int n0 = blockIdx.y * CB;
+    T acc[CB];
 #pragma unroll
-    for (int c = 0; c < kApplyCB; c++) acc[c] = T(0);
+    for (int c = 0; c < CB; c++) acc[c] = T(0);
     const int e1 = cov_ptr[cidx + 1];
     for (int e = cov_ptr[cidx]; e < e1; e++) {
-        const int g = ent_img[e], ii = ent_i[e];
-        const int a = img_atom[g];
-        const int ip = ip_displ[a], np = ip_displ[a + 1] - ip;
-        const int ndc = img_ndc[g];
-        const T *__restrict__ ch = chi + img_chi_off[g] + ii;
+        const int4 meta = ent_meta[e];  // (first projector row, projector count, image size)
+        const int ip = meta.x, np = meta.y, ndc = meta.z;
+        const T *__restrict__ ch = chi + ent_chi[e];
         for (int j = 0; j < np; j++) {
             const T cv = __ldg(ch + (long)j * ndc);
+            const V *__restrict__ al = reinterpret_cast<const V *>(alpha + (long)(ip + j) * lda + n0);
 #pragma unroll
-            for (int c = 0; c < kApplyCB; c++)
-                if (n0 + c < ncol) acc[c] += cv * __ldg(alpha + (long)(n0 + c) * ntot + ip + j);
+            for (int c = 0; c < CB / VW; c++) {
+                const V av = __ldg(al + c);
+                const T *ae = reinterpret_cast<const T *>(&av);
+#pragma unroll
+                for (int w = 0; w < VW; w++) acc[c * VW + w] += cv * ae[w];
+            }
         }
     }
     const long p = cov_pt[cidx];
 #pragma unroll
-    for (int c = 0; c < kApplyCB; c++)
+    for (int c = 0; c < CB; c++)
         if (n0 + c < ncol) out[(long)(n0 + c) * ldo + p] += scale * acc[c];
 }
 
@@ -147,62 +160,88 @@ const float *gamma_of<float>(const Nonlocal &nl) { return nl.gamma32; }
 }  // namespace
 
 template <typename T>
-int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha,
+static constexpr int apply_cb() { return sizeof(T) == 4 ? 16 : 8; }
+
+long nonlocal_alpha_ld(int ncol, int elem_bytes)
+{
+    const int cb = elem_bytes == 4 ? 16 : 8;
+    return ((long)ncol + cb - 1) / cb * cb;
+}
+
+template <typename T, int MAXJ>
+static void project_launch(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
+                           cudaStream_t st)
+{
+    constexpr int NC = kProjThreads / 8, PCH = sizeof(T) == 4 ? 128 : 64;
+    const Nonlocal &nl = ctx->nl;
+    const int ncb = (ncol + NC - 1) / NC;
+    for (int cb0 = 0; cb0 < ncb; cb0 += 65535) {
+        int nb = std::min(65535, ncb - cb0);
+        dim3 grid(nl.nimg, nb);
+        ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
+        k_nl_project<T, PCH, NC, MAXJ><<<grid, kProjThreads, 0, st>>>(
+            nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, chi_of<T>(nl),
+            nl.ip_displ, gamma_of<T>(nl), ncol - cb0 * NC, x + (long)cb0 * NC * ldx, ldx,
+            alpha + (long)cb0 * NC, lda, (T)ctx->dV);
+    }
+}
+
+template <typename T>
+int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
                             cudaStream_t st)
 {
     const Nonlocal &nl = ctx->nl;
     if (!ctx->has_nl || nl.nimg == 0 || ncol <= 0) return SGPU_OK;
-    const int njg = (nl.max_np + kProjNPB - 1) / kProjNPB;
-    const int ncb = (ncol + kProjCB - 1) / kProjCB;
-    for (int cb0 = 0; cb0 < ncb; cb0 += 65535) {
-        int nb = std::min(65535, ncb - cb0);
-        dim3 grid(nl.nimg, njg, nb);
-        ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
-        k_nl_project<T><<<grid, kProjThreads, 0, st>>>(
-            nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, chi_of<T>(nl),
-            nl.ip_displ, gamma_of<T>(nl), nl.ntot, ncol - cb0 * kProjCB,
-            x + (long)cb0 * kProjCB * ldx, ldx, alpha + (long)cb0 * kProjCB * nl.ntot,
-            (T)ctx->dV);
+    if (nl.max_np <= 9)
+        project_launch<T, 9>(ctx, ncol, x, ldx, alpha, lda, st);
+    else if (nl.max_np <= 18)
+        project_launch<T, 18>(ctx, ncol, x, ldx, alpha, lda, st);
+    else if (nl.max_np <= 32)
+        project_launch<T, 32>(ctx, ncol, x, ldx, alpha, lda, st);
+    else {
+        set_error("nonlocal: more than 32 projectors per atom is not built");
+        return SGPU_ERR_ARG;
     }
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
 }
 
 template <typename T>
-int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, double scale, T *out,
-                          long ldo, cudaStream_t st)
+int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, double scale,
+                          T *out, long ldo, cudaStream_t st)
 {
     const Nonlocal &nl = ctx->nl;
     if (!ctx->has_nl || nl.ncov == 0 || ncol <= 0) return SGPU_OK;
-    const int ncb = (ncol + kApplyCB - 1) / kApplyCB;
+    constexpr int CB = apply_cb<T>();
+    constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+    const int ncb = (ncol + CB - 1) / CB;
     for (int cb0 = 0; cb0 < ncb; cb0 += 65535) {
         int nb = std::min(65535, ncb - cb0);
         dim3 grid((nl.ncov + 255) / 256, nb);
         ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
-        k_nl_apply<T><<<grid, 256, 0, st>>>(
-            nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_img, nl.ent_i, nl.img_atom, nl.img_ndc,
-            nl.img_chi_off, chi_of<T>(nl), nl.ip_displ, nl.ntot, ncol - cb0 * kApplyCB,
-            alpha + (long)cb0 * kApplyCB * nl.ntot, (T)scale, out + (long)cb0 * kApplyCB * ldo,
-            ldo);
+        k_nl_apply<T, CB, VW><<<grid, 256, 0, st>>>(
+            nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, chi_of<T>(nl),
+            ncol - cb0 * CB, alpha + (long)cb0 * CB, lda, (T)scale,
+            out + (long)cb0 * CB * ldo, ldo);
     }
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
 }
 
 template int launch_nonlocal_project<double>(sgpu_ctx *, int, const double *, long, double *,
-                                             cudaStream_t);
-template int launch_nonlocal_project<float>(sgpu_ctx *, int, const float *, long, float *,
+                                             long, cudaStream_t);
+template int launch_nonlocal_project<float>(sgpu_ctx *, int, const float *, long, float *, long,
                                             cudaStream_t);
-template int launch_nonlocal_apply<double>(sgpu_ctx *, int, const double *, double, double *,
-                                           long, cudaStream_t);
-template int launch_nonlocal_apply<float>(sgpu_ctx *, int, const float *, double, float *, long,
-                                          cudaStream_t);
+template int launch_nonlocal_apply<double>(sgpu_ctx *, int, const double *, long, double,
+                                           double *, long, cudaStream_t);
+template int launch_nonlocal_apply<float>(sgpu_ctx *, int, const float *, long, double, float *,
+                                          long, cudaStream_t);
 
 void nonlocal_free(Nonlocal &nl)
 {
     void *ptrs[] = {nl.ip_displ, nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off,
                     nl.grid_pos, nl.chi64,    nl.chi32,   nl.gamma64, nl.gamma32,
-                    nl.work_img, nl.work_start, nl.cov_pt, nl.cov_ptr, nl.ent_img, nl.ent_i};
+                    nl.cov_pt,   nl.cov_ptr,  nl.ent_chi, nl.ent_meta};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     nl = Nonlocal();
@@ -268,13 +307,16 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     }
     std::vector<int> slot(ctx->Nd, -1);
     for (size_t c = 0; c < covpts.size(); c++) slot[covpts[c]] = covptr[c];
-    std::vector<int> ent_img(npos), ent_i(npos);
+    std::vector<long> ent_chi(npos);
+    std::vector<int4> ent_meta(npos);
     for (int g = 0; g < nimg; g++) {
+        const int a = img_atom[g];
+        const int ip = ip_displ[a], np = ip_displ[a + 1] - ip_displ[a];
         for (int ii = 0; ii < img_ndc[g]; ii++) {
             const int p = grid_pos[off[g] + ii];
             const int e = slot[p]++;
-            ent_img[e] = g;
-            ent_i[e] = ii;
+            ent_chi[e] = chioff[g] + ii;
+            ent_meta[e] = make_int4(ip, np, img_ndc[g], g);
         }
     }
     nl.ncov = (int)covpts.size();
@@ -299,8 +341,8 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(gamma32, gamma32.data(), (size_t)nl.ntot);
     UP(cov_pt, covpts.data(), covpts.size());
     UP(cov_ptr, covptr.data(), covptr.size());
-    UP(ent_img, ent_img.data(), ent_img.size());
-    UP(ent_i, ent_i.data(), ent_i.size());
+    UP(ent_chi, ent_chi.data(), ent_chi.size());
+    UP(ent_meta, ent_meta.data(), ent_meta.size());
 #undef UP
     if (rc != SGPU_OK) {
         nonlocal_free(nl);

@@ -61,24 +61,43 @@ struct Nonlocal {
     float *chi32 = nullptr;
     double *gamma64 = nullptr;  // ntot, per projector
     float *gamma32 = nullptr;
-    // projection work items: (image, first point) chunks of kProjChunk points
-    int nwork = 0;
-    int *work_img = nullptr;
-    int *work_start = nullptr;
     // point CSR for the apply
     int ncov = 0;
     long nent = 0;
     int *cov_pt = nullptr;      // ncov covered grid points, ascending
     int *cov_ptr = nullptr;     // ncov + 1
-    int *ent_img = nullptr;     // nent
-    int *ent_i = nullptr;       // nent
+    long *ent_chi = nullptr;    // nent: offset of the entry's Chi row (image block + index)
+    int4 *ent_meta = nullptr;   // nent: (first projector row, projector count, ndc, image)
 };
-
-constexpr int kProjChunk = 256;
 
 struct Workspace {
     void *ptr = nullptr;
     size_t bytes = 0;
+};
+
+// periodic-Pulay density mixing parameters (SPARC_OBJ fields of the same meaning)
+struct MixParams {
+    int m = 7;                 // MixingHistory
+    int pulay_freq = 1;        // PulayFrequency
+    int restart = 0;           // PulayRestartFlag
+    double beta = 0.3;         // MixingParameter
+    double omega = 0.3;        // MixingParameterSimple
+    int kerker = 1;            // MixingPrecond == 1
+    double kTF = 1.0;          // precond_kerker_kTF
+    double idiemac = 0.1;      // precond_kerker_thresh
+    double precond_tol = 1e-4; // TOL_PRECOND
+    double neg_charge = 0.0;   // NegCharge (minus the electron count)
+};
+
+// device-resident mixing history (mixing_hist_* of SPARC_OBJ)
+struct MixState {
+    int m = 0;
+    MixParams prm;
+    double *buf = nullptr;
+    double *x_k = nullptr, *x_km1 = nullptr, *f_k = nullptr, *f_km1 = nullptr;
+    double *Pf = nullptr, *x_wavg = nullptr, *f_wavg = nullptr, *tmp = nullptr;
+    double *R = nullptr, *F = nullptr;
+    ~MixState();
 };
 
 }  // namespace sgpu
@@ -97,7 +116,8 @@ struct sgpu_ctx {
     bool has_nl = false;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
-    sgpu::Workspace ws[8];     // grow-only scratch slots (see enum WsSlot)
+    sgpu::Workspace ws[12];    // grow-only scratch slots (see enum WsSlot)
+    sgpu::MixState *mix = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on
@@ -114,7 +134,10 @@ struct sgpu_ctx {
 
 namespace sgpu {
 
-enum WsSlot { WS_STAGE_A = 0, WS_STAGE_B, WS_STAGE_C, WS_ALPHA, WS_MISC, WS_EIG, WS_POIS, WS_MIX };
+enum WsSlot {
+    WS_STAGE_A = 0, WS_STAGE_B, WS_STAGE_C, WS_ALPHA, WS_MISC, WS_EIG, WS_POIS, WS_MIX,
+    WS_RED, WS_RHS, WS_SCF, WS_SCF2
+};
 
 // grow-only device scratch
 int ws_get(sgpu_ctx *ctx, int slot, size_t bytes, void **out);
@@ -141,12 +164,14 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                    long ldz, cudaStream_t st);
 
 // ---- nonlocal (nonlocal.cu)
+// alpha is (ntot x lda) projector-major: alpha[row * lda + n]; lda from nonlocal_alpha_ld
+long nonlocal_alpha_ld(int ncol, int elem_bytes);
 template <typename T>
-int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha,
+int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
                             cudaStream_t st);
 template <typename T>
-int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, double scale, T *out,
-                          long ldo, cudaStream_t st);
+int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, double scale,
+                          T *out, long ldo, cudaStream_t st);
 int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double *gamma,
                     int nimg, const int *img_atom, const int *img_ndc, const int *grid_pos,
                     const double *chi);
@@ -159,6 +184,42 @@ int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, lon
 template <typename T>
 int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int ncol, int m,
                   double a, double b, double a0, cudaStream_t st);
+
+// ---- Rayleigh-Ritz (subspace.cu)
+int project_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *HY,
+                long ldh, double *Hp, double *Mp, cudaStream_t st);
+int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
+                double *Hp, double *Mp, cudaStream_t st);
+int generalized_eig(sgpu_ctx *ctx, int n, double *Hp, double *Mp, double *lambda_dev,
+                    cudaStream_t st);
+int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *Q, double *X,
+               long ldx, cudaStream_t st);
+int rotate_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const double *Q, float *X,
+               long ldx, cudaStream_t st);
+
+// ---- SCF-side operations (scf_ops.cu), all FP64 vectors of Nd
+int dot_dev(sgpu_ctx *ctx, const double *a, const double *b, long n, double *d_out,
+            cudaStream_t st);  // b == nullptr: plain sum
+int dot_host(sgpu_ctx *ctx, const double *a, const double *b, long n, double *out,
+             cudaStream_t st);
+template <typename T>
+int density_dev(sgpu_ctx *ctx, const T *psi, long ld, int ncol, const double *w_dev,
+                double *rho, cudaStream_t st);
+int lda_pw_dev(sgpu_ctx *ctx, const double *rho, const double *rho_core, double rhotol,
+               double *vxc, double *exc, cudaStream_t st);
+int axpby_dev(sgpu_ctx *ctx, long n, double a, const double *x, double b, const double *y,
+              double *z, cudaStream_t st);
+int remove_mean_dev(sgpu_ctx *ctx, double *x, cudaStream_t st);
+int scf_error_dev(sgpu_ctx *ctx, const double *out, const double *in, double *err,
+                  cudaStream_t st);
+int aar_dev(sgpu_ctx *ctx, double c, double *x, const double *b, double omega, double beta,
+            int m, int p, double tol, int max_iter, int *iters, cudaStream_t st);
+int poisson_dev(sgpu_ctx *ctx, const double *rho, const double *b, double *phi, double tol,
+                int max_iter, int *iters, cudaStream_t st);
+int kerker_dev(sgpu_ctx *ctx, const double *f, double a, double kTF, double idiemac,
+               double tol, double *Pf, cudaStream_t st);
+int mixing_init(sgpu_ctx *ctx, const MixParams &prm, const double *x0);
+int mixing_step(sgpu_ctx *ctx, int iter_count, double *g, cudaStream_t st);
 
 // ---- elementwise helpers (util.cu)
 template <typename T>

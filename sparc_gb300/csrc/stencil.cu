@@ -10,10 +10,12 @@
 // costs no extra pass over HBM.
 //
 // Layout: column-major blocks with leading dimension ld, grid index i + j*Nx + k*Nx*Ny.
-// Each thread block owns a BX x BY tile of an xy-plane for one column and marches along z:
-// the z-neighbours of a thread's point live in a register queue of 2R+1 values, the current
-// plane plus its x/y halo lives in shared memory, and periodic images are resolved by
-// wrapping indices while loading (no ghost-extended copy, unlike the reference's x_ex).
+// Each thread block owns a tile of an xy-plane for one column and marches along z: the
+// z-neighbours of a thread's point live in a register queue of 2R+1 values, the current plane
+// plus its x/y halo lives in shared memory (two buffers, one barrier per plane), and periodic
+// images are resolved by wrapping indices while loading (no ghost-extended copy, unlike the
+// reference's x_ex). Values for the next plane (halo, potential, Chebyshev term) are
+// prefetched into registers one plane ahead.
 #include "sgpu_internal.h"
 
 namespace sgpu {
@@ -37,11 +39,12 @@ __device__ __forceinline__ int wrapi(int i, int n)
     return i < 0 ? i + n : i;
 }
 
+// FP64 (and generic) kernel: one point per thread. On GB300 the FP64 pipe, not HBM, bounds it.
 template <typename T, int R, int BX, int BY>
 __global__ void __launch_bounds__(BX *BY)
     k_stencil_orth(const StencilParams<T> p)
 {
-    __shared__ T s[BY + 2 * R][BX + 2 * R];
+    __shared__ T s[2][BY + 2 * R][BX + 2 * R];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     const int col = blockIdx.z / p.nslab;
@@ -56,55 +59,223 @@ __global__ void __launch_bounds__(BX *BY)
     const long NxNy = (long)p.Nx * p.Ny;
 
     const T *__restrict__ xc = p.x + (long)col * p.ldx;
+    const T *__restrict__ zc = p.z ? p.z + (long)col * p.ldz : nullptr;
+    T *__restrict__ oc = p.out + (long)col * p.ldo;
     const long own = gi + (long)gj * p.Nx;
 
-    // halo source offsets within a plane (x-halo: left/right; y-halo: top/bottom)
+    const bool hx = tx < R, hy = ty < R;
     long hxl = 0, hxr = 0, hyl = 0, hyr = 0;
-    if (tx < R) {
+    if (hx) {
         hxl = wrapi(x0 - R + tx, p.Nx) + (long)gj * p.Nx;
         hxr = wrapi(x0 + BX + tx, p.Nx) + (long)gj * p.Nx;
     }
-    if (ty < R) {
+    if (hy) {
         hyl = gi + (long)wrapi(y0 - R + ty, p.Ny) * p.Nx;
         hyr = gi + (long)wrapi(y0 + BY + ty, p.Ny) * p.Nx;
     }
 
-    T q[2 * R + 1];
+    T q[2 * R + 1];  // q[m] = x at plane k - R + m
 #pragma unroll
-    for (int m = 0; m < 2 * R; m++) q[m] = __ldg(xc + own + (long)wrapi(zs - R + m, p.Nz) * NxNy);
+    for (int m = 0; m < 2 * R; m++)
+        q[m] = __ldg(xc + own + (long)wrapi(zs - R + m, p.Nz) * NxNy);
+
+    T h0 = T(0), h1 = T(0), h2 = T(0), h3 = T(0), vv = T(0), zz = T(0);
+    {
+        const long pk = (long)zs * NxNy;
+        if (hx) { h0 = __ldg(xc + pk + hxl); h1 = __ldg(xc + pk + hxr); }
+        if (hy) { h2 = __ldg(xc + pk + hyl); h3 = __ldg(xc + pk + hyr); }
+        if (p.v) vv = __ldg(p.v + own + pk);
+        if (zc) zz = zc[own + pk];
+    }
 
     for (int k = zs; k < ze; k++) {
+        const int b = k & 1;
         q[2 * R] = __ldg(xc + own + (long)wrapi(k + R, p.Nz) * NxNy);
-        const long pk = (long)k * NxNy;
-        __syncthreads();  // previous plane fully consumed
-        s[ty + R][tx + R] = q[R];
-        if (tx < R) {
-            s[ty + R][tx] = __ldg(xc + pk + hxl);
-            s[ty + R][tx + BX + R] = __ldg(xc + pk + hxr);
-        }
-        if (ty < R) {
-            s[ty][tx + R] = __ldg(xc + pk + hyl);
-            s[ty + BY + R][tx + R] = __ldg(xc + pk + hyr);
+        s[b][ty + R][tx + R] = q[R];
+        if (hx) { s[b][ty + R][tx] = h0; s[b][ty + R][tx + BX + R] = h1; }
+        if (hy) { s[b][ty][tx + R] = h2; s[b][ty + BY + R][tx + R] = h3; }
+        const T vcur = vv, zcur = zz;
+        if (k + 1 < ze) {
+            const long pn = (long)(k + 1) * NxNy;
+            if (hx) { h0 = __ldg(xc + pn + hxl); h1 = __ldg(xc + pn + hxr); }
+            if (hy) { h2 = __ldg(xc + pn + hyl); h3 = __ldg(xc + pn + hyr); }
+            if (p.v) vv = __ldg(p.v + own + pn);
+            if (zc) zz = zc[own + pn];
         }
         __syncthreads();
         if (active) {
             T res = p.c0 * q[R];
 #pragma unroll
             for (int r = 1; r <= R; r++) {
-                T rx = (s[ty + R][tx + R - r] + s[ty + R][tx + R + r]) * p.wx[r];
-                T ry = (s[ty + R - r][tx + R] + s[ty + R + r][tx + R]) * p.wy[r];
+                T rx = (s[b][ty + R][tx + R - r] + s[b][ty + R][tx + R + r]) * p.wx[r];
+                T ry = (s[b][ty + R - r][tx + R] + s[b][ty + R + r][tx + R]) * p.wy[r];
                 T rz = (q[R - r] + q[R + r]) * p.wz[r];
                 res += rx + ry + rz;
             }
-            const long pt = own + pk;
-            if (p.v) res += p.bv * (__ldg(p.v + pt) * q[R]);
+            if (p.v) res += p.bv * (vcur * q[R]);
             T o = p.s1 * res;
-            if (p.z) o += p.s2 * p.z[(long)col * p.ldz + pt];
-            p.out[(long)col * p.ldo + pt] = o;
+            if (zc) o += p.s2 * zcur;
+            oc[own + (long)k * NxNy] = o;
         }
 #pragma unroll
         for (int m = 0; m < 2 * R; m++) q[m] = q[m + 1];
     }
+}
+
+// FP32 kernel: each thread owns two neighbouring x-points. Shared-memory reads are paired
+// (8-byte), the neighbour pair sums use Blackwell's packed f32x2 add, and the weighted sums
+// run as three independent FMA chains (x, y, z) whose weights come straight from the kernel
+// parameter bank. The z-loop is unrolled by the queue length 2R+1, so the register queue
+// rotates by renaming instead of moves. In-column offsets are 32-bit.
+template <int R, int BXP, int BY, int MINB>
+__global__ void __launch_bounds__(BXP / 2 * BY, MINB)
+    k_stencil_f32x2(const StencilParams<float> p)
+{
+    constexpr int Q = 2 * R + 1;
+    constexpr int W = BXP + 2 * R;
+    static_assert(R % 2 == 0 && BXP % 2 == 0, "paired layout needs even radius and tile");
+    static_assert(Q == 13, "the unrolled z-loop below is written for radius 6");
+    __shared__ __align__(16) float s[2][BY + 2 * R][W];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = blockIdx.x * BXP, y0 = blockIdx.y * BY;
+    const int col = blockIdx.z / p.nslab;
+    const int slab = blockIdx.z - col * p.nslab;
+    const int zs = slab * p.zlen;
+    const int ze = min(zs + p.zlen, p.Nz);
+    if (zs >= ze) return;
+
+    const int i0 = x0 + 2 * tx, j = y0 + ty;
+    const bool act0 = (i0 < p.Nx) && (j < p.Ny), act1 = (i0 + 1 < p.Nx) && (j < p.Ny);
+    const int gj = wrapi(j, p.Ny);
+    const int row = gj * p.Nx;
+    const int own0 = wrapi(i0, p.Nx) + row;
+    const int own1 = wrapi(i0 + 1, p.Nx) + row;
+    const int NxNy = p.Nx * p.Ny;
+    const float *__restrict__ xc = p.x + (long)col * p.ldx;
+    const float *__restrict__ zc = p.z ? p.z + (long)col * p.ldz : nullptr;
+    float *__restrict__ oc = p.out + (long)col * p.ldo;
+
+    const bool hx = tx < R / 2, hy = ty < R;
+    int hA0 = 0, hA1 = 0, hB0 = 0, hB1 = 0;  // x-halo (left, right) or y-halo (top, bottom)
+    if (hx) {
+        hA0 = wrapi(x0 - R + 2 * tx, p.Nx) + row;
+        hA1 = wrapi(x0 - R + 2 * tx + 1, p.Nx) + row;
+        hB0 = wrapi(x0 + BXP + 2 * tx, p.Nx) + row;
+        hB1 = wrapi(x0 + BXP + 2 * tx + 1, p.Nx) + row;
+    }
+    int hT0 = 0, hT1 = 0, hD0 = 0, hD1 = 0;
+    if (hy) {
+        const int rt = wrapi(y0 - R + ty, p.Ny) * p.Nx;
+        const int rb = wrapi(y0 + BY + ty, p.Ny) * p.Nx;
+        hT0 = own0 - row + rt; hT1 = own1 - row + rt;
+        hD0 = own0 - row + rb; hD1 = own1 - row + rb;
+    }
+
+    float2 q[Q];
+#pragma unroll
+    for (int m = 0; m < 2 * R; m++) {
+        const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
+        q[m] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl));
+    }
+    float2 hL = make_float2(0.f, 0.f), hR = hL, hT = hL, hB = hL, vv = hL, zz = hL;
+    {
+        const int pk = zs * NxNy;
+        if (hx) {
+            hL = make_float2(__ldg(xc + pk + hA0), __ldg(xc + pk + hA1));
+            hR = make_float2(__ldg(xc + pk + hB0), __ldg(xc + pk + hB1));
+        }
+        if (hy) {
+            hT = make_float2(__ldg(xc + pk + hT0), __ldg(xc + pk + hT1));
+            hB = make_float2(__ldg(xc + pk + hD0), __ldg(xc + pk + hD1));
+        }
+        if (p.v) vv = make_float2(__ldg(p.v + own0 + pk), __ldg(p.v + own1 + pk));
+        if (zc) zz = make_float2(zc[own0 + pk], zc[own1 + pk]);
+    }
+
+    // one plane: U is the unroll slot; the queue slot of plane k-R+m is (U+m) % Q
+#define SGPU_F2_STEP(U)                                                                          \
+    {                                                                                            \
+        const int k = kb + (U);                                                                  \
+        if (k < ze) {                                                                            \
+            const int b = k & 1;                                                                 \
+            {                                                                                    \
+                const int pl = wrapi(k + R, p.Nz) * NxNy;                                        \
+                q[((U) + 2 * R) % Q] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl)); \
+            }                                                                                    \
+            const float2 cen = q[((U) + R) % Q];                                                 \
+            *reinterpret_cast<float2 *>(&s[b][ty + R][R + 2 * tx]) = cen;                        \
+            if (hx) {                                                                            \
+                *reinterpret_cast<float2 *>(&s[b][ty + R][2 * tx]) = hL;                         \
+                *reinterpret_cast<float2 *>(&s[b][ty + R][R + BXP + 2 * tx]) = hR;               \
+            }                                                                                    \
+            if (hy) {                                                                            \
+                *reinterpret_cast<float2 *>(&s[b][ty][R + 2 * tx]) = hT;                         \
+                *reinterpret_cast<float2 *>(&s[b][ty + BY + R][R + 2 * tx]) = hB;                \
+            }                                                                                    \
+            const float2 vcur = vv, zcur = zz;                                                   \
+            if (k + 1 < ze) {                                                                    \
+                const int pn = (k + 1) * NxNy;                                                   \
+                if (hx) {                                                                        \
+                    hL = make_float2(__ldg(xc + pn + hA0), __ldg(xc + pn + hA1));                \
+                    hR = make_float2(__ldg(xc + pn + hB0), __ldg(xc + pn + hB1));                \
+                }                                                                                \
+                if (hy) {                                                                        \
+                    hT = make_float2(__ldg(xc + pn + hT0), __ldg(xc + pn + hT1));                \
+                    hB = make_float2(__ldg(xc + pn + hD0), __ldg(xc + pn + hD1));                \
+                }                                                                                \
+                if (p.v) vv = make_float2(__ldg(p.v + own0 + pn), __ldg(p.v + own1 + pn));       \
+                if (zc) zz = make_float2(zc[own0 + pn], zc[own1 + pn]);                          \
+            }                                                                                    \
+            __syncthreads();                                                                     \
+            if (act0 || act1) {                                                                  \
+                const float *srow = &s[b][ty + R][2 * tx];                                       \
+                float2 L[R + 1];                                                                 \
+                _Pragma("unroll") for (int m = 0; m <= R; m++)                                   \
+                    L[m] = *reinterpret_cast<const float2 *>(srow + 2 * m);                      \
+                float ax0 = p.c0 * cen.x, ax1 = p.c0 * cen.y;                                    \
+                float ay0 = 0.f, ay1 = 0.f, az0 = 0.f, az1 = 0.f;                                \
+                _Pragma("unroll") for (int r = 1; r <= R; r++) {                                 \
+                    float2 lo, hi;                                                               \
+                    if (r % 2 == 0) {                                                            \
+                        lo = L[(R - r) / 2];                                                     \
+                        hi = L[(R + r) / 2];                                                     \
+                    } else {                                                                     \
+                        lo = make_float2(L[(R - r) / 2].y, L[(R - r + 1) / 2].x);                \
+                        hi = make_float2(L[(R + r) / 2].y, L[(R + r + 1) / 2].x);                \
+                    }                                                                            \
+                    const float2 xs = __fadd2_rn(lo, hi);                                        \
+                    const float2 ys = __fadd2_rn(                                                \
+                        *reinterpret_cast<const float2 *>(&s[b][ty + R - r][R + 2 * tx]),       \
+                        *reinterpret_cast<const float2 *>(&s[b][ty + R + r][R + 2 * tx]));      \
+                    const float2 zsum = __fadd2_rn(q[((U) + R - r) % Q], q[((U) + R + r) % Q]);  \
+                    ax0 = fmaf(xs.x, p.wx[r], ax0); ax1 = fmaf(xs.y, p.wx[r], ax1);              \
+                    ay0 = fmaf(ys.x, p.wy[r], ay0); ay1 = fmaf(ys.y, p.wy[r], ay1);              \
+                    az0 = fmaf(zsum.x, p.wz[r], az0); az1 = fmaf(zsum.y, p.wz[r], az1);          \
+                }                                                                                \
+                float r0 = ax0 + (ay0 + az0), r1 = ax1 + (ay1 + az1);                            \
+                if (p.v) {                                                                       \
+                    r0 = fmaf(p.bv, vcur.x * cen.x, r0);                                         \
+                    r1 = fmaf(p.bv, vcur.y * cen.y, r1);                                         \
+                }                                                                                \
+                r0 *= p.s1;                                                                      \
+                r1 *= p.s1;                                                                      \
+                if (zc) {                                                                        \
+                    r0 = fmaf(p.s2, zcur.x, r0);                                                 \
+                    r1 = fmaf(p.s2, zcur.y, r1);                                                 \
+                }                                                                                \
+                const int pk = k * NxNy;                                                         \
+                if (act0) oc[own0 + pk] = r0;                                                    \
+                if (act1) oc[own1 + pk] = r1;                                                    \
+            }                                                                                    \
+        }                                                                                        \
+    }
+
+    for (int kb = zs; kb < ze; kb += Q) {
+        SGPU_F2_STEP(0) SGPU_F2_STEP(1) SGPU_F2_STEP(2) SGPU_F2_STEP(3) SGPU_F2_STEP(4)
+        SGPU_F2_STEP(5) SGPU_F2_STEP(6) SGPU_F2_STEP(7) SGPU_F2_STEP(8) SGPU_F2_STEP(9)
+        SGPU_F2_STEP(10) SGPU_F2_STEP(11) SGPU_F2_STEP(12)
+    }
+#undef SGPU_F2_STEP
 }
 
 }  // namespace
@@ -114,12 +285,17 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                    const T *x, long ldx, T *out, long ldo, double s1, double s2, const T *z,
                    long ldz, cudaStream_t st)
 {
-    constexpr int R = 6, BX = 32, BY = 8;
+    constexpr int R = 6, BX = 32, BY = 8;       // FP64 tile (one point per thread)
+    constexpr int BXP = 32, BYP = 16;          // FP32 tile (two points per thread)
     if (ctx->FDn != R) {
         set_error("stencil: only FD order 12 (radius 6) is built");
         return SGPU_ERR_ARG;
     }
     if (ncol <= 0) return SGPU_OK;
+    if (sizeof(T) == 4 && ctx->Nd >= (1L << 31)) {
+        set_error("stencil: FP32 kernel needs Nx*Ny*Nz < 2^31");
+        return SGPU_ERR_ARG;
+    }
     StencilParams<T> p;
     p.x = x; p.out = out; p.z = z; p.v = v;
     p.ldx = ldx; p.ldo = ldo; p.ldz = ldz;
@@ -139,7 +315,9 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     if (!v || fabs(bv) < 1e-14) p.v = nullptr;
     if (!z || s2 == 0.0) p.z = nullptr;
 
-    const int tilesx = (ctx->Nx + BX - 1) / BX, tilesy = (ctx->Ny + BY - 1) / BY;
+    const bool f32 = sizeof(T) == 4;
+    const int tilesx = f32 ? (ctx->Nx + BXP - 1) / BXP : (ctx->Nx + BX - 1) / BX;
+    const int tilesy = f32 ? (ctx->Ny + BYP - 1) / BYP : (ctx->Ny + BY - 1) / BY;
     // split z into slabs until there are enough blocks to fill 152 SMs several times over
     long blocks1 = (long)tilesx * tilesy * ncol;
     int nslab = 1;
@@ -153,9 +331,12 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
         q.x = x + (long)c0i * ldx;
         q.out = out + (long)c0i * ldo;
         if (q.z) q.z = z + (long)c0i * ldz;
-        dim3 grid(tilesx, tilesy, nc * nslab), block(BX, BY);
+        dim3 grid(tilesx, tilesy, nc * nslab);
         ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
-        k_stencil_orth<T, R, BX, BY><<<grid, block, 0, st>>>(q);
+        if constexpr (sizeof(T) == 4)
+            k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);
+        else
+            k_stencil_orth<T, R, BX, BY><<<grid, dim3(BX, BY), 0, st>>>(q);
     }
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;

@@ -1,0 +1,180 @@
+// Rayleigh-Ritz step of CheFSI: projection, generalized eigensolve, rotation.
+//
+// Reference (USE_DP_SUBEIG path, one process):
+//   DP_Project_Hamiltonian            src/eigenSolver.c:939-1082
+//       HY = H Y (one more Hamiltonian apply, :960), Mp = Yᵀ Y, Hp = Yᵀ HY (cblas_dgemm :1022-1033)
+//   DP_Solve_Generalized_EigenProblem src/eigenSolver.c:1262-1375
+//       LAPACKE_dsygvd(COL_MAJOR, 1, 'V', 'U', Ns, Hp, Ns, Mp, Ns, lambda) (:1318); Q = Hp
+//   DP_Subspace_Rotation              src/eigenSolver.c:1386-1439
+//       X = Y Q (cblas_dgemm :1415)
+//
+// GPU form: the products are plain GEMMs, so they go to cuBLAS: DSYRK/DGEMM in FP64 for the
+// drop-in, and for FP32 blocks (the mixed-precision filter) SGEMM with the BF16x9 FP32
+// emulation on the tensor cores (each FP32 operand split into three BF16 terms, FP32
+// accumulation). The Ns x Ns generalized eigenproblem stays FP64 on cuSOLVER (dsygvd).
+#include <algorithm>
+
+#include "sgpu_internal.h"
+
+namespace sgpu {
+
+static int ensure_handles(sgpu_ctx *ctx)
+{
+    if (!ctx->cublas) {
+        SGPU_CUBLAS_TRY(cublasCreate(&ctx->cublas));
+        SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, ctx->stream));
+    }
+    if (!ctx->cusolver) {
+        if (cusolverDnCreate(&ctx->cusolver) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnCreate failed");
+            return SGPU_ERR_CUDA;
+        }
+        cusolverDnSetStream(ctx->cusolver, ctx->stream);
+    }
+    return SGPU_OK;
+}
+
+namespace {
+// symmetrise an Ns x Ns column-major matrix from its upper triangle
+template <typename T>
+__global__ void k_sym_from_upper(T *A, int n, int lda)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i < n && j < n && i > j) A[(long)j * lda + i] = A[(long)i * lda + j];
+}
+
+__global__ void k_f32_to_f64(const float *__restrict__ a, double *__restrict__ b, long n)
+{
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n;
+         t += (long)gridDim.x * blockDim.x)
+        b[t] = (double)a[t];
+}
+}  // namespace
+
+// Hp = Yᵀ HY and Mp = Yᵀ Y (full symmetric Ns x Ns, column-major, ld = Ns), FP64 blocks.
+int project_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *HY,
+                long ldh, double *Hp, double *Mp, cudaStream_t st)
+{
+    SGPU_TRY(ensure_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    const double one = 1.0, zero = 0.0;
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasDsyrk(ctx->cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, ncol,
+                                    (int)ctx->Nd, &one, Y, (int)ldy, &zero, Mp, ncol));
+    }
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol,
+                                    (int)ctx->Nd, &one, Y, (int)ldy, HY, (int)ldh, &zero, Hp,
+                                    ncol));
+    }
+    dim3 b(16, 16), g((ncol + 15) / 16, (ncol + 15) / 16);
+    k_sym_from_upper<double><<<g, b, 0, st>>>(Mp, ncol, ncol);
+    ctx->launches++;
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
+// The same for FP32 blocks: products on the tensor cores with BF16x9 FP32 emulation,
+// accumulated in FP32, then widened to FP64 for the eigensolver.
+int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
+                double *Hp, double *Mp, cudaStream_t st)
+{
+    SGPU_TRY(ensure_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    float *tmp = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_EIG, sizeof(float) * 2 * (size_t)ncol * ncol, (void **)&tmp));
+    const float one = 1.f, zero = 0.f;
+    for (int w = 0; w < 2; w++) {
+        const float *B = w == 0 ? Y : HY;
+        const long ldb = w == 0 ? ldy : ldh;
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasGemmEx(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol,
+                                     (int)ctx->Nd, &one, Y, CUDA_R_32F, (int)ldy, B, CUDA_R_32F,
+                                     (int)ldb, &zero, tmp + (size_t)w * ncol * ncol, CUDA_R_32F,
+                                     ncol, CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
+                                     CUBLAS_GEMM_DEFAULT));
+    }
+    const long n2 = (long)ncol * ncol;
+    k_f32_to_f64<<<std::max<long>(1, std::min<long>((n2 + 255) / 256, 4096)), 256, 0, st>>>(
+        tmp, Mp, n2);
+    k_f32_to_f64<<<std::max<long>(1, std::min<long>((n2 + 255) / 256, 4096)), 256, 0, st>>>(
+        tmp + n2, Hp, n2);
+    ctx->launches += 2;
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
+// Hp q = lambda Mp q (upper triangles referenced); on return Hp holds Q, lambda ascending.
+// Mp is overwritten by its Cholesky factor.
+int generalized_eig(sgpu_ctx *ctx, int n, double *Hp, double *Mp, double *lambda_dev,
+                    cudaStream_t st)
+{
+    SGPU_TRY(ensure_handles(ctx));
+    cusolverDnSetStream(ctx->cusolver, st);
+    int lwork = 0;
+    if (cusolverDnDsygvd_bufferSize(ctx->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                    CUBLAS_FILL_MODE_UPPER, n, Hp, n, Mp, n, lambda_dev,
+                                    &lwork) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnDsygvd_bufferSize failed");
+        return SGPU_ERR_CUDA;
+    }
+    char *wsp = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_MISC, sizeof(double) * ((size_t)lwork + 1) + 64, (void **)&wsp));
+    double *work = reinterpret_cast<double *>(wsp);
+    int *info = reinterpret_cast<int *>(wsp + sizeof(double) * ((size_t)lwork + 1));
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    if (cusolverDnDsygvd(ctx->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                         CUBLAS_FILL_MODE_UPPER, n, Hp, n, Mp, n, lambda_dev, work, lwork,
+                         info) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnDsygvd failed to launch");
+        return SGPU_ERR_CUDA;
+    }
+    int hinfo = 0;
+    SGPU_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hinfo != 0) {
+        set_error("dsygvd: info = " + std::to_string(hinfo) +
+                  (hinfo > n ? " (Mp is not positive definite)" : " (no convergence)"));
+        return SGPU_ERR_LINALG;
+    }
+    return SGPU_OK;
+}
+
+// X = Y Q (FP64)
+int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *Q, double *X,
+               long ldx, cudaStream_t st)
+{
+    SGPU_TRY(ensure_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    const double one = 1.0, zero = 0.0;
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    SGPU_CUBLAS_TRY(cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, (int)ctx->Nd, ncol, ncol,
+                                &one, Y, (int)ldy, Q, ncol, &zero, X, (int)ldx));
+    return SGPU_OK;
+}
+
+// X = Y Q with FP32 blocks: Q is narrowed to FP32, product with BF16x9 emulation
+int rotate_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const double *Q, float *X,
+               long ldx, cudaStream_t st)
+{
+    SGPU_TRY(ensure_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    float *q32 = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_EIG, sizeof(float) * (size_t)ncol * ncol, (void **)&q32));
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_TRY(convert_cols<double, float>(Q, ncol, q32, ncol, ncol, ncol, st));
+    }
+    const float one = 1.f, zero = 0.f;
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    SGPU_CUBLAS_TRY(cublasGemmEx(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, (int)ctx->Nd, ncol, ncol,
+                                 &one, Y, CUDA_R_32F, (int)ldy, q32, CUDA_R_32F, ncol, &zero, X,
+                                 CUDA_R_32F, (int)ldx, CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
+                                 CUBLAS_GEMM_DEFAULT));
+    return SGPU_OK;
+}
+
+}  // namespace sgpu

@@ -95,6 +95,33 @@ def capture(sysd, psp_dir, out_path, ncol, seed, cheb_m, cheb_bounds):
     np.savez_compressed(out_path, **out)
 
 
+def capture_scf(sysd, psp_dir, out_npz, out_json, sparc_bin):
+    """Reference SCF run of the system (the program itself, single rank) plus the set-up
+    data an SCF needs, so the GPU SCF can start from the reference's own inputs."""
+    import json
+    import subprocess
+    from ref_capture import RefSystem, parse_reference_outputs, scf_setup
+
+    tmp = tempfile.mkdtemp(prefix="sparc_scf_")
+    base = systems.write_system(sysd, tmp, psp_dir)
+    env = dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count() or 1))
+    subprocess.run([sparc_bin, "-name", os.path.basename(base)], cwd=tmp, env=env, check=True,
+                   stdout=subprocess.DEVNULL)
+    ref = parse_reference_outputs(base)
+    r = RefSystem(base)
+    types, images = r.nonlocal_data()
+    flat = flatten_nonlocal(types, images, r.n_atom)
+    fields, params = scf_setup(r)
+    np.savez_compressed(
+        out_npz, Nx=r.Nx, Ny=r.Ny, Nz=r.Nz, FDn=r.order // 2, h=r.h, L=r.L, dV=r.dV,
+        cx=r.cx, cy=r.cy, cz=r.cz, n_atom=r.n_atom, Nstates=r.Nstates,
+        **{k: v for k, v in fields.items()}, **{"nl_" + k: v for k, v in flat.items()})
+    ref["params"] = params
+    ref["system"] = sysd["name"]
+    with open(out_json, "w") as fh:
+        json.dump(ref, fh, indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -113,6 +140,16 @@ def main():
         if p.exitcode != 0:
             raise SystemExit(f"capture failed for {sysd['name']}")
         print("wrote", path, os.path.getsize(path), "bytes")
+    sparc_bin = os.path.join(HERE, "..", "..", "oracle", "_ref", "sparc")
+    for sysd in (systems.si8_c1(),):
+        npz = os.path.join(HERE, f"{sysd['name']}_scf.npz")
+        js = os.path.join(HERE, f"{sysd['name']}_scf_ref.json")
+        p = ctx.Process(target=capture_scf, args=(sysd, psp_dir, npz, js, sparc_bin))
+        p.start()
+        p.join()
+        if p.exitcode != 0:
+            raise SystemExit(f"SCF capture failed for {sysd['name']}")
+        print("wrote", npz, os.path.getsize(npz), "bytes and", js)
 
 
 if __name__ == "__main__":

@@ -121,3 +121,73 @@ class RefSystem:
         r = np.zeros_like(x)
         self.lib.ref_poisson_residual(ctypes.c_double(c), _d(x), _d(b), _d(r))
         return r
+
+
+def scf_setup(r):
+    """SCF inputs from the reference set-up of system r (a RefSystem), plus the reference's
+    own Vxc and electrostatic potential for the initial density."""
+    Nd = r.Nd
+    f = r.setup_fields()
+    core = np.zeros(Nd)
+    nlcc = r.lib.ref_core_density(_d(core))
+    prm = np.zeros(20)
+    r.lib.ref_scf_params(_d(prm))
+    vxc, exc = np.zeros(Nd), np.zeros(Nd)
+    r.lib.ref_vxc(_d(f["rho0"]), _d(vxc), _d(exc))
+    phi = np.zeros(Nd)
+    r.lib.ref_poisson(_d(f["rho0"]), _d(phi))
+    keys = ["Beta", "TOL_SCF", "TOL_POISSON", "TOL_PRECOND", "TOL_LANCZOS", "xc_rhotol",
+            "ChebDegree", "rhoTrigger", "MixingParameter", "MixingParameterSimple",
+            "MixingHistory", "PulayFrequency", "MixingPrecond", "precond_kerker_kTF",
+            "precond_kerker_thresh", "MAXIT_POISSON", "MINIT_SCF", "MAXIT_SCF", "elec_T_type",
+            "Nchefsi"]
+    params = {k: float(v) for k, v in zip(keys, prm)}
+    return dict(b=f["b"], rho0=f["rho0"], rho_core=core, nlcc=int(nlcc), Esc=f["Esc"],
+                NegCharge=f["NegCharge"], Nelectron=f["Nelectron"], vxc0=vxc, exc0=exc,
+                phi0=phi), params
+
+
+def parse_reference_outputs(base):
+    """Energies, SCF count, eigenvalues/occupations and forces from a reference run."""
+    out = {}
+    with open(base + ".out") as fh:
+        for line in fh:
+            if line.startswith("Free energy per atom"):
+                out["Etot_per_atom"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("Total free energy"):
+                out["Etot"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("Total number of SCF"):
+                out["scf_iters"] = int(line.split(":")[1])
+            elif line.startswith("Fermi level"):
+                out["Efermi"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("Total walltime"):
+                out["walltime_s"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("Band structure energy"):
+                out["Eband"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("Exchange correlation energy"):
+                out["Exc"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("Self and correction energy"):
+                out["Esc"] = float(line.split(":")[1].split()[0])
+            elif line.startswith("-Entropy*kb*T"):
+                out["Entropy"] = float(line.split(":")[1].split()[0])
+    lam, occ = [], []
+    with open(base + ".eigen") as fh:
+        for line in fh:
+            p = line.split()
+            if len(p) == 3 and p[0].isdigit():
+                lam.append(float(p[1]))
+                occ.append(float(p[2]))
+    out["lambda"] = lam
+    out["occ"] = occ
+    forces = []
+    with open(base + ".static") as fh:
+        lines = fh.read().splitlines()
+    for i, line in enumerate(lines):
+        if line.startswith("Atomic forces"):
+            for l2 in lines[i + 1:]:
+                p = l2.split()
+                if len(p) != 3:
+                    break
+                forces.append([float(v) for v in p])
+    out["forces"] = forces
+    return out

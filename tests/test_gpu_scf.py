@@ -1,0 +1,170 @@
+"""GPU parity of the Rayleigh-Ritz and SCF-side rows, and of the full SCF, through the C ABI.
+
+References: the reference program's own outputs for the Si8 system (Calculate_Vxc and
+Calculate_elecstPotential on the initial density, the converged SCF energies and
+eigenvalues), numpy/LAPACK for the dense Rayleigh-Ritz step, and the CPU oracle.
+Tolerances: pointwise FP64 maps 1e-12 relative; iterative solves at their stopping tolerance;
+SCF energy 1e-5 Ha/atom and occupied eigenvalues 1e-5 Ha (the spec bars)."""
+import numpy as np
+import pytest
+
+import sparc_gb300 as sg
+from oracle import scf_oracle as so
+from oracle.oracle import Oracle
+from scf_io import load_scf, scf_params
+
+pytestmark = pytest.mark.gpu
+
+
+def make_ctx(grid, nl, veff=None):
+    ctx = sg.Context(grid["Nx"], grid["Ny"], grid["Nz"], grid["FDn"], grid["cx"], grid["cy"],
+                     grid["cz"], grid["dV"])
+    if veff is not None:
+        ctx.set_veff(veff)
+    if nl is not None:
+        ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
+                         nl["grid_pos"], nl["chi"])
+    return ctx
+
+
+def test_vxc_matches_reference(gpu_available):
+    d, grid, nl, ref = load_scf()
+    ctx = make_ctx(grid, None)
+    vxc, exc = np.zeros(ctx.Nd), np.zeros(ctx.Nd)
+    ctx.Calculate_Vxc_LDA_PW(d["rho0"], d["rho_core"], ref["params"]["xc_rhotol"], vxc, exc)
+    assert np.abs(vxc - d["vxc0"]).max() <= 1e-12 * np.abs(d["vxc0"]).max()
+    assert np.abs(exc - d["exc0"]).max() <= 1e-12 * np.abs(d["exc0"]).max()
+
+
+def test_poisson_matches_reference(gpu_available):
+    d, grid, nl, ref = load_scf()
+    ctx = make_ctx(grid, None)
+    phi = np.zeros(ctx.Nd)
+    it = ctx.Calculate_elecstPotential(d["rho0"], d["b"], phi, ref["params"]["TOL_POISSON"])
+    assert np.abs(phi - d["phi0"]).max() < 1e-6 * np.abs(d["phi0"]).max()
+    assert abs(phi.mean()) < 1e-10
+    # same iteration path as the oracle restatement (same AAR schedule and stopping rule)
+    o = Oracle(grid, nl)
+    _, it_o = so.poisson(o, d["rho0"], d["b"], np.zeros_like(phi), ref["params"]["TOL_POISSON"])
+    assert abs(it - it_o) <= 6
+
+
+def test_aar_kerker_shift_vs_oracle(gpu_available):
+    d, grid, nl, ref = load_scf()
+    ctx = make_ctx(grid, None)
+    o = Oracle(grid, nl)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(ctx.Nd)
+    x = np.zeros(ctx.Nd)
+    it, ok = ctx.AAR(-1.0, x, b, tol=1e-10, max_iter=2000)
+    xo, it_o = so.aar(o, -1.0, np.zeros(ctx.Nd), b, tol=1e-10, max_iter=2000)
+    assert ok
+    assert np.abs(x - xo).max() < 1e-8 * np.abs(xo).max()
+    r = o.poisson_residual(-1.0, x, b)
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(b) * 1.0001
+
+
+def test_density_and_scf_error(gpu_available):
+    d, grid, nl, ref = load_scf()
+    ctx = make_ctx(grid, None)
+    rng = np.random.default_rng(5)
+    psi = rng.standard_normal((7, ctx.Nd))
+    occ = rng.uniform(0, 1, 7)
+    rho = np.zeros(ctx.Nd)
+    ctx.CalculateDensity_psi(psi, occ, 2.0, rho)
+    ref_rho = so.density(psi, occ, 2.0, grid["dV"])
+    assert np.abs(rho - ref_rho).max() <= 1e-12 * np.abs(ref_rho).max()
+    err = ctx.Evaluate_scf_error(rho, d["rho0"])
+    assert abs(err - so.scf_error(rho, d["rho0"])) < 1e-12
+
+
+def test_pulay_mixing_vs_oracle(gpu_available):
+    d, grid, nl, ref = load_scf()
+    ctx = make_ctx(grid, None)
+    o = Oracle(grid, nl)
+    neg = -float(d["Nelectron"])
+    tolp = ref["params"]["TOL_PRECOND"]
+    ctx.Mixing_init(d["rho0"], neg, tol_precond=tolp)
+    mx = so.PulayMixer(o, d["rho0"], neg, grid["dV"], precond_tol=tolp)
+    rng = np.random.default_rng(11)
+    g = d["rho0"].copy()
+    for it in range(9):  # past the history length, so the ring buffer wraps
+        g = g * (1.0 + 0.02 * rng.standard_normal(g.size))
+        xg = g.copy()
+        ctx.Mixing_periodic_pulay(it, xg)
+        xo = mx.step(it, g.copy())
+        # Kerker solves stop at TOL_PRECOND; mixed densities agree to that level
+        assert np.abs(xg - xo).max() < 2e-5 * np.abs(xo).max(), it
+        g = 0.7 * g + 0.3 * xo
+
+
+def test_rayleigh_ritz_vs_lapack(gpu_available):
+    import scipy.linalg as sl
+    d, grid, nl, ref = load_scf()
+    rng = np.random.default_rng(2)
+    veff = rng.standard_normal(int(d["Nx"]) ** 3) * 0.1
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    Ns = 12
+    Y = rng.standard_normal((Ns, ctx.Nd))
+    HY = np.zeros_like(Y)
+    Hp = np.zeros((Ns, Ns))
+    Mp = np.zeros((Ns, Ns))
+    ctx.Project_Hamiltonian(Y, HY, Hp, Mp)
+    HYo = o.hamiltonian(veff, 0.0, Y)
+    assert np.abs(HY - HYo).max() < 1e-12 * np.abs(HYo).max()
+    Hpo = Y @ HYo.T
+    Mpo = Y @ Y.T
+    assert np.abs(Hp - Hpo.T).max() < 1e-11 * np.abs(Hpo).max()
+    assert np.abs(Mp - Mpo).max() < 1e-11 * np.abs(Mpo).max()
+    lam = np.zeros(Ns)
+    Q = Hp.copy(order="C")
+    ctx.Solve_Generalized_EigenProblem(Q, Mp.copy(order="C"), lam)
+    lo, vo = sl.eigh(0.5 * (Hpo + Hpo.T), Mpo)
+    assert np.abs(lam - lo).max() < 1e-9 * np.abs(lo).max()
+    X = np.zeros_like(Y)
+    ctx.Subspace_Rotation(Y, Q, X)  # Q is column-major: C-array (Ns, Ns) rows are columns
+    Xo = (Q @ Y)  # X[:, n] = sum_k Y[:, k] Q[k, n] -> row n of X = sum_k Q_colmajor[n][k] Y[k]
+    assert np.abs(X - Xo).max() < 1e-11 * np.abs(Xo).max()
+
+
+def test_lanczos_bounds(gpu_available):
+    d, grid, nl, ref = load_scf()
+    rng = np.random.default_rng(4)
+    veff = rng.standard_normal(int(d["Nx"]) ** 3) * 0.2
+    ctx = make_ctx(grid, nl, veff)
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    o = Oracle(grid, nl)
+    op = LinearOperator((ctx.Nd, ctx.Nd), matvec=lambda v: o.hamiltonian(veff, 0.0, v)[0],
+                        dtype=np.float64)
+    emin = eigsh(op, k=1, which="SA", tol=1e-10)[0][0]
+    emax = eigsh(op, k=1, which="LA", tol=1e-10)[0][0]
+    x0 = rng.uniform(-1, 1, ctx.Nd)
+    # the reference's setting (tol 1e-2 on successive changes): Ritz values lie inside the
+    # spectrum, and the upper bound is the accurate one (the filter adds 1% to it)
+    lo, hi = ctx.Lanczos(x0, tol=1e-2)
+    assert emin - 1e-8 <= lo and hi <= emax + 1e-8
+    assert abs(hi - emax) < 0.01 * emax
+    # converged Lanczos reproduces both extremes
+    lo2, hi2 = ctx.Lanczos(x0, tol=1e-9, maxit=3000)
+    assert abs(lo2 - emin) < 1e-6 and abs(hi2 - emax) < 1e-6 * abs(emax)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_scf_matches_reference_program(gpu_available, precision):
+    d, grid, nl, ref = load_scf()
+    ctx = make_ctx(grid, nl)
+    prm = scf_params(sg, d, ref, precision=precision, switch=1e-4)
+    res, rho, lam, occ = ctx.scf(prm, d["b"], d["rho0"], d["rho_core"])
+    n_atom = int(d["n_atom"])
+    assert res["converged"] == 1
+    assert abs(res["Etot"] / n_atom - ref["Etot_per_atom"]) < 1e-5
+    assert abs(res["Efermi"] - ref["Efermi"]) < 1e-4
+    lam_ref = np.array(ref["lambda"])
+    occ_ref = np.array(ref["occ"])
+    occupied = occ_ref > 1e-3
+    assert np.abs(lam[occupied] - lam_ref[occupied]).max() < 1e-5
+    assert abs(rho.sum() * grid["dV"] - float(d["Nelectron"])) < 1e-8
+    assert abs(res["scf_iters"] - ref["scf_iters"]) <= 6
+    if precision == 32:
+        assert res["fp64_switch_iter"] > 0
