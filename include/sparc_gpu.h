@@ -86,6 +86,18 @@ int sgpu_Lap_vec_mult(sgpu_ctx *ctx, int ncol, double c, const double *x, int ld
 /* Hx += Vnl x. Replaces Vnl_vec_mult (src/nlocVecRoutines.c:798). */
 int sgpu_Vnl_vec_mult(sgpu_ctx *ctx, int ncol, const double *x, int ldi, double *Hx, int ldo);
 
+/* The same Hx += Vnl x for callers that cannot allocate device memory (for example a host
+ * application whose own pool allocator reserves all GPU memory, or a caller that cannot
+ * accept the device-wide synchronisation of cudaFree). No counterpart in the reference.
+ * It allocates nothing: the projection coefficients live in a fixed 8 MiB scratch array
+ * inside the library (held on every GPU that loads the library until exit), so
+ * n_proj * round_up(ncol, 8) must not exceed 1048576 (larger requests return SGPU_ERR_ARG);
+ * x and Hx must be device pointers. The first call on a device looks up the scratch
+ * address on that device; make it before any stream capture. All calls share the scratch
+ * (each clears it first): calls that overlap on the GPU race and must be serialised. */
+int sgpu_Vnl_vec_mult_noalloc(sgpu_ctx *ctx, int ncol, const double *x, int ldi, double *Hx,
+                              int ldo);
+
 /* Hx = (-0.5*Lap + Veff[spin] + c) x + Vnl x. Replaces Hamiltonian_vectors_mult
  * (src/hamiltonianVecRoutines.c:45) for an orthogonal cell without exact exchange,
  * meta-GGA, Hubbard or spin-orbit terms. */

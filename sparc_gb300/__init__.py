@@ -26,7 +26,7 @@ EXPORTED = [
     "sgpu_Solve_Generalized_EigenProblem", "sgpu_Subspace_Rotation", "sgpu_Lanczos",
     "sgpu_CalculateDensity_psi", "sgpu_Calculate_Vxc_LDA_PW", "sgpu_AAR",
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
-    "sgpu_Evaluate_scf_error", "sgpu_scf",
+    "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_Vnl_vec_mult_noalloc",
 ]
 
 SGPU_ERR_NOT_CONVERGED = 5
