@@ -50,6 +50,7 @@ def parse():
                     help="columns in the bounded CPU-baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution block")
     return ap.parse_args()
 
 
@@ -133,6 +134,45 @@ def cpu_baseline(wl, ncols, threads=None):
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": o.threads(), "kind": "port",
             "sample": f"FP64 degree-{M} filter of {ncols} of the {NCOL} vectors on the same "
                       f"96^3 grid, potential and projectors ({dt:.2f} s)"}
+
+
+def scf_block(sg, device=0, repeats=2):
+    """SCF time-to-solution on the 8-atom Si cell (a = 10.26 Bohr, 26^3 grid, LDA, 32 states,
+    degree 20, TOL_SCF 1e-6) from the reference's own set-up fields, in plain FP64 and in the
+    mixed-precision mode; energies and eigenvalues checked against the reference run."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from scf_io import load_scf, scf_params
+    d, grid, nl, ref = load_scf("Si8_c1")
+    ctx = sg.Context(grid["Nx"], grid["Ny"], grid["Nz"], grid["FDn"], grid["cx"], grid["cy"],
+                     grid["cz"], grid["dV"], device=device)
+    ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
+                     nl["grid_pos"], nl["chi"])
+    n_atom = int(d["n_atom"])
+    occ_ref = np.array(ref["occ"])
+    lam_ref = np.array(ref["lambda"])
+    out = {"system": "Si8 diamond cell, 26^3 grid, 32 states, LDA_PW, degree 20",
+           "reference": {"Etot_per_atom": ref["Etot_per_atom"], "scf_iters": ref["scf_iters"],
+                         "walltime_s": ref["walltime_s"],
+                         "where": "reference program, single rank + 8-thread OpenBLAS, "
+                                  "x86 build host (cannot run on the Arm GPU host)"}}
+    for name, prec in (("fp64", 64), ("mixed", 32)):
+        best = None
+        for rep in range(repeats):
+            prm = scf_params(sg, d, ref, precision=prec, switch=1e-4, seed=1 + rep)
+            res, rho, lam, occ = ctx.scf(prm, d["b"], d["rho0"], d["rho_core"])
+            if best is None or res["time_s"] < best[0]["time_s"]:
+                best = (res, lam)
+        res, lam = best
+        occd = occ_ref > 1e-3
+        out[name] = {"time_s": round(res["time_s"], 4), "scf_iters": res["scf_iters"],
+                     "Etot_per_atom": res["Etot"] / n_atom,
+                     "dE_per_atom_vs_ref": abs(res["Etot"] / n_atom - ref["Etot_per_atom"]),
+                     "max_occ_eig_err": float(np.abs(lam[occd] - lam_ref[occd]).max()),
+                     "converged": bool(res["converged"]),
+                     "fp64_switch_iter": res["fp64_switch_iter"]}
+    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["time_s"] / out["mixed"]["time_s"], 3)
+    ctx.close()
+    return out
 
 
 def run_reference(args):
@@ -299,6 +339,9 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(wl, args.cpu_cols)
+    scf = None
+    if rank == 0 and not args.no_scf:
+        scf = scf_block(sg, device=local)
 
     if rank == 0:
         line = {
@@ -324,6 +367,7 @@ def main():
                     "d2h_bytes_per_step": int(2 * ncol * Nd * 8),
                     "api": "sgpu_ChebyshevFiltering(host FP64 arrays, SGPU_PREC_FP32)"},
             "fp64": fp64,
+            "scf": scf,
             "cpu_baseline": cpu,
             "clocks": ck,
         }

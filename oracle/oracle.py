@@ -145,6 +145,68 @@ class Oracle:
         self.lib.orc_poisson_residual(ctypes.byref(self.g), ctypes.c_double(c), _d(x), _d(b), _d(r))
         return r
 
+    # ---- k-point twins: complex blocks (ncol, Nd) complex128; k (3,), L (3,) in Bohr units;
+    # img_coords (nimg, 3) image coordinates of the nonlocal set
+    @staticmethod
+    def _cblk(x):
+        x = np.array(x, dtype=np.complex128, order="C", copy=True)
+        return x.reshape(1, -1) if x.ndim == 1 else x
+
+    def lap_plus_diag_kpt(self, k, L, a, b, c, v, x):
+        x = self._cblk(x)
+        y = np.zeros_like(x)
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        L = np.ascontiguousarray(L, dtype=np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        self.lib.orc_lap_plus_diag_orth_kpt(
+            self.Nx, self.Ny, self.Nz, self.FDn, self.g.cx, self.g.cy, self.g.cz, _d(k), _d(L),
+            ctypes.c_int(x.shape[0]), ctypes.c_double(a), ctypes.c_double(b), ctypes.c_double(c),
+            _d(vv) if vv is not None else None, _d(x.view(np.float64)), ctypes.c_long(self.Nd),
+            _d(y.view(np.float64)), ctypes.c_long(self.Nd))
+        return y
+
+    def _kargs(self, k, L, img_coords):
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        L = np.ascontiguousarray(L, dtype=np.float64)
+        ic = np.ascontiguousarray(img_coords, dtype=np.float64).reshape(-1)
+        self._keep += [k, L, ic]
+        return k, L, ic
+
+    def vnl_kpt(self, k, L, img_coords, x):
+        x = self._cblk(x)
+        out = np.zeros_like(x)
+        k, L, ic = self._kargs(k, L, img_coords)
+        if self.nl is not None:
+            self.lib.orc_vnl_vec_mult_kpt(self._nlp(), _d(ic), _d(k), _d(L),
+                                          ctypes.c_double(self.g.dV), ctypes.c_int(x.shape[0]),
+                                          _d(x.view(np.float64)), ctypes.c_long(self.Nd),
+                                          _d(out.view(np.float64)), ctypes.c_long(self.Nd))
+        return out
+
+    def hamiltonian_kpt(self, k, L, img_coords, veff, c, x):
+        x = self._cblk(x)
+        hx = np.zeros_like(x)
+        k, L, ic = self._kargs(k, L, img_coords)
+        veff = np.ascontiguousarray(veff, dtype=np.float64)
+        self.lib.orc_hamiltonian_kpt(ctypes.byref(self.g), self._nlp(), _d(ic), _d(k), _d(L),
+                                     _d(veff), ctypes.c_int(x.shape[0]), ctypes.c_double(c),
+                                     _d(x.view(np.float64)), ctypes.c_long(self.Nd),
+                                     _d(hx.view(np.float64)), ctypes.c_long(self.Nd))
+        return hx
+
+    def chebyshev_kpt(self, k, L, img_coords, veff, m, a, b, a0, X):
+        X = self._cblk(X)
+        Y = np.zeros_like(X)
+        k, L, ic = self._kargs(k, L, img_coords)
+        veff = np.ascontiguousarray(veff, dtype=np.float64)
+        self.lib.orc_chebyshev_filter_kpt(ctypes.byref(self.g), self._nlp(), _d(ic), _d(k),
+                                          _d(L), _d(veff), _d(X.view(np.float64)),
+                                          ctypes.c_long(self.Nd), _d(Y.view(np.float64)),
+                                          ctypes.c_long(self.Nd), ctypes.c_int(X.shape[0]),
+                                          ctypes.c_int(m), ctypes.c_double(a),
+                                          ctypes.c_double(b), ctypes.c_double(a0))
+        return X, Y
+
     def set_threads(self, n):
         self.lib.orc_set_num_threads(ctypes.c_int(n))
 

@@ -43,8 +43,12 @@ int ref_init(const char *name)
     GetInfluencingAtoms(&S);
     Generate_PseudoChargeDensity(&S);
     GetInfluencingAtoms_nloc(&S, &S.Atom_Influence_nloc, S.DMVertices_dmcomm, S.dmcomm);
-    CalculateNonlocalProjectors(&S, &S.nlocProj, S.Atom_Influence_nloc, S.DMVertices_dmcomm,
-                                S.dmcomm);
+    if (S.isGammaPoint)
+        CalculateNonlocalProjectors(&S, &S.nlocProj, S.Atom_Influence_nloc, S.DMVertices_dmcomm,
+                                    S.dmcomm);
+    else
+        CalculateNonlocalProjectors_kpt(&S, &S.nlocProj, S.Atom_Influence_nloc,
+                                        S.DMVertices_dmcomm, S.dmcomm);
     Init_electronDensity(&S);
     g_ready = 1;
     return 0;
@@ -209,3 +213,5 @@ void ref_poisson(const double *rho, double *phi)
     Calculate_elecstPotential(&S);
     memcpy(phi, S.elecstPotential, sizeof(double) * S.Nd);
 }
+
+SPARC_OBJ *ref_harness_obj(void) { return &S; }

@@ -46,6 +46,26 @@ void orc_chebyshev_filter(const orc_grid *gr, const orc_nonlocal *nl, const doub
                           double b, double a0);
 void orc_poisson_residual(const orc_grid *gr, double c, const double *x, const double *b,
                           double *r);
+#ifndef __cplusplus
+#include <complex.h>
+void orc_lap_plus_diag_orth_kpt(int Nx, int Ny, int Nz, int FDn, const double *cx,
+                                const double *cy, const double *cz, const double *k,
+                                const double *L, int ncol, double a, double b, double c,
+                                const double *v, const double complex *x, long ldi,
+                                double complex *y, long ldo);
+void orc_vnl_vec_mult_kpt(const orc_nonlocal *nl, const double *img_coords, const double *k,
+                          const double *L, double dV, int ncol, const double complex *x,
+                          long ldi, double complex *Hx, long ldo);
+void orc_hamiltonian_kpt(const orc_grid *gr, const orc_nonlocal *nl, const double *img_coords,
+                         const double *k, const double *L, const double *veff, int ncol,
+                         double c, const double complex *x, long ldi, double complex *Hx,
+                         long ldo);
+void orc_chebyshev_filter_kpt(const orc_grid *gr, const orc_nonlocal *nl,
+                              const double *img_coords, const double *k, const double *L,
+                              const double *veff, double complex *X, long ldi,
+                              double complex *Y, long ldo, int ncol, int m, double a, double b,
+                              double a0);
+#endif
 int orc_num_threads(void);
 void orc_set_num_threads(int n);
 

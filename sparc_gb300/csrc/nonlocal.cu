@@ -6,13 +6,15 @@
 //   Hx[grid_pos_J] += Chi_J alpha_J               (dgemm + scatter, :869-884)
 //
 // GPU form:
-//   * project: one thread block per (atom image, projector group, column group); threads
-//     stride over the image's grid points, gather x, accumulate in registers, then one
-//     block-level reduction and one atomic add per output into alpha (ntot x ncol,
-//     projector index fastest). dV and Gamma are folded into that add.
-//   * apply: owner-computes over a CSR of covered grid points, so each output element is
-//     written by exactly one thread (no atomics on the orbital block, overlapping spheres
-//     are summed in registers).
+//   * project: a gathered GEMM. One thread block per segment of at most kSegPts points of
+//     one atom image: the segment's grid positions and Chi rows are staged in shared memory
+//     once, then the block walks all column groups, gathering x[grid_pos, group] into shared
+//     memory chunk by chunk and accumulating alpha[j, n] in registers; one atomic add per
+//     (projector, column) and segment, with dV * Gamma folded in.
+//   * apply: owner-computes over a CSR of covered grid points: one thread per covered point
+//     loops over all column blocks, so each output element is written by exactly one thread
+//     (no atomics on the orbital block; overlapping spheres are summed in registers) and the
+//     thread's Chi values are re-read from L1, not HBM, for every column block after the first.
 #include <algorithm>
 #include <numeric>
 
@@ -22,92 +24,123 @@ namespace sgpu {
 namespace {
 
 constexpr int kProjThreads = 256;
-
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// alpha layout: alpha[row * lda + n], row = IP_displ[atom] + j (projector), n = column;
-// lda is a multiple of the apply's column block so rows can be read as vectors.
-//
-// Projection as a gathered GEMM: block = (atom image g, group of NC columns). The image's
-// points are walked in chunks of PCH: the block gathers x[grid_pos[chunk], n0:n0+NC] into
-// shared memory (coalesced along points for each column) together with the chunk's Chi rows,
-// then thread (n, jg) accumulates alpha[j, n] for j = jg, jg + 8, ... over the chunk. One
-// atomic add per (projector, column) output at the end, with dV * Gamma folded in.
-template <typename T, int PCH, int NC, int MAXJ>
-__global__ void __launch_bounds__(kProjThreads)
-    k_nl_project(const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
-                 const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
-                 const int *__restrict__ grid_pos, const T *__restrict__ chi,
-                 const int *__restrict__ ip_displ, const T *__restrict__ gamma, int ncol,
-                 const T *__restrict__ x, long ldx, T *__restrict__ alpha, long lda, T dV)
-{
-    static_assert(kProjThreads == 8 * NC, "thread (n, jg) layout: NC columns x 8 groups");
-    constexpr int JG = 8;
-    constexpr int NJ = (MAXJ + JG - 1) / JG;
-    __shared__ T xs[NC][PCH + 1];     // +1: conflict-free reads across columns
-    __shared__ T cs[MAXJ][PCH];
-    const int g = blockIdx.x;
-    const int n0 = blockIdx.y * NC;
-    const int a = img_atom[g];
-    const int np = ip_displ[a + 1] - ip_displ[a];
-    const int ndc = img_ndc[g];
-    const int *__restrict__ gp = grid_pos + img_off[g];
-    const T *__restrict__ ch = chi + img_chi_off[g];
-    const int t = threadIdx.x;
-    const int n = t % NC, jg = t / NC;
-    T acc[NJ];
-#pragma unroll
-    for (int u = 0; u < NJ; u++) acc[u] = T(0);
-
-    for (int i0 = 0; i0 < ndc; i0 += PCH) {
-        const int cnt = min(PCH, ndc - i0);
-        __syncthreads();  // previous chunk consumed
-        // gather: PCH points x NC columns, kProjThreads threads
-        for (int e = t; e < PCH * NC; e += kProjThreads) {
-            const int i = e % PCH, c = e / PCH;
-            T v = T(0);
-            if (i < cnt && n0 + c < ncol) v = __ldg(x + (long)(n0 + c) * ldx + gp[i0 + i]);
-            xs[c][i] = v;
-        }
-        for (int e = t; e < PCH * MAXJ; e += kProjThreads) {
-            const int i = e % PCH, j = e / PCH;
-            cs[j][i] = (i < cnt && j < np) ? __ldg(ch + (long)j * ndc + i0 + i) : T(0);
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int i = 0; i < PCH; i++) {
-            const T xv = xs[n][i];
-#pragma unroll
-            for (int u = 0; u < NJ; u++)
-                if (jg + u * JG < MAXJ) acc[u] += cs[jg + u * JG][i] * xv;
-        }
-    }
-    if (n0 + n < ncol) {
-#pragma unroll
-        for (int u = 0; u < NJ; u++) {
-            const int j = jg + u * JG;
-            if (j < np) {
-                const int row = ip_displ[a] + j;
-                atomicAdd(alpha + (long)row * lda + n0 + n, dV * gamma[row] * acc[u]);
-            }
-        }
-    }
-}
+constexpr int kSegPts = 512;  // points of one image handled by one projection block
 
 template <typename T, int CB>
 struct VecOf;
 template <> struct VecOf<float, 4> { using type = float4; };
 template <> struct VecOf<double, 2> { using type = double2; };
 
-// Apply: one thread per covered grid point and CB columns; alpha rows are read as vectors
-// (VW elements per load, broadcast across the warp when neighbouring points share an atom).
-template <typename T, int CB, int VW>
+// alpha layout: alpha[row * lda + n], row = IP_displ[atom] + j (projector), n = column;
+// lda is a multiple of the apply's column block so rows can be read as vectors.
+//
+// Projection kernel: block = one segment (at most kSegPts points) of one atom image. The
+// segment's grid positions and its Chi rows (transposed to point-major, MAXJP values per point
+// so a point's projectors load as 16-byte vectors) are staged in shared memory once. The block
+// then walks column groups of NC: it gathers x[grid_pos, group] chunk by chunk into shared
+// memory, and thread (column n, point half h) accumulates alpha[0..MAXJ-1, n] in registers
+// over its half of each chunk; the two halves are summed through shared memory and added
+// atomically into alpha, with dV * Gamma folded in.
+template <typename T, int PCH, int NC, int MAXJ>
+__global__ void __launch_bounds__(kProjThreads)
+    k_nl_project(const int *__restrict__ seg_img, const int *__restrict__ seg_start,
+                 const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
+                 const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
+                 const int *__restrict__ grid_pos, const T *__restrict__ chi,
+                 const int *__restrict__ ip_displ, const T *__restrict__ gamma, int ncol,
+                 const T *__restrict__ x, long ldx, T *__restrict__ alpha, long lda, T dV)
+{
+    constexpr int HALVES = kProjThreads / NC;
+    static_assert(HALVES * NC == kProjThreads, "threads = columns x point groups");
+    static_assert(kSegPts % PCH == 0 && PCH % HALVES == 0, "whole chunks");
+    constexpr int VW = 16 / sizeof(T);                        // elements per 16-byte vector
+    constexpr int MAXJP = (MAXJ + VW - 1) / VW * VW;          // padded projectors per point
+    constexpr int GX = PCH * NC / kProjThreads;               // gathers per thread and chunk
+    using V = typename VecOf<T, VW>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // x tile [NC][PCH + 1], reused after the chunk loop as the reduction buffer
+    // [HALVES][MAXJ][NC]: the region holds the larger of the two
+    constexpr size_t XS = (size_t)NC * (PCH + 1) > (size_t)HALVES * MAXJ * NC
+                              ? (size_t)NC * (PCH + 1) : (size_t)HALVES * MAXJ * NC;
+    T *cs = reinterpret_cast<T *>(smem_raw);                  // [kSegPts][MAXJP]
+    T *xs = cs + (size_t)MAXJP * kSegPts;
+    int *gps = reinterpret_cast<int *>(xs + XS);              // [kSegPts]
+
+    const int g = seg_img[blockIdx.x];
+    const int sbeg = seg_start[blockIdx.x];
+    const int a = img_atom[g];
+    const int np = ip_displ[a + 1] - ip_displ[a];
+    const int ndc = img_ndc[g];
+    const int cnt_seg = min(ndc - sbeg, kSegPts);
+    const int *__restrict__ gp = grid_pos + img_off[g] + sbeg;
+    const T *__restrict__ ch = chi + img_chi_off[g] + sbeg;
+    const int t = threadIdx.x;
+    const int n = t % NC, h = t / NC;
+
+    for (int i = t; i < kSegPts; i += kProjThreads) gps[i] = i < cnt_seg ? gp[i] : 0;
+    for (int e = t; e < MAXJP * kSegPts; e += kProjThreads) {
+        const int i = e / MAXJP, j = e % MAXJP;
+        cs[e] = (j < np && i < cnt_seg) ? __ldg(ch + (long)j * ndc + i) : T(0);
+    }
+
+    for (int n0 = 0; n0 < ncol; n0 += NC) {
+        T acc[MAXJP];
+#pragma unroll
+        for (int j = 0; j < MAXJP; j++) acc[j] = T(0);
+        for (int i0 = 0; i0 < cnt_seg; i0 += PCH) {
+            const int cnt = min(PCH, cnt_seg - i0);
+            __syncthreads();  // staging done / previous chunk consumed
+            T v[GX];
+#pragma unroll
+            for (int u = 0; u < GX; u++) {
+                const int e = t + u * kProjThreads;
+                const int i = e % PCH, c = e / PCH;
+                v[u] = (i < cnt && n0 + c < ncol)
+                           ? __ldg(x + (long)(n0 + c) * ldx + gps[i0 + i]) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < GX; u++) {
+                const int e = t + u * kProjThreads;
+                xs[(e / PCH) * (PCH + 1) + e % PCH] = v[u];
+            }
+            __syncthreads();
+            const T *xr = xs + n * (PCH + 1);
+#pragma unroll 2
+            for (int i = h; i < PCH; i += HALVES) {
+                const T xv = xr[i];
+                const V *cv = reinterpret_cast<const V *>(cs + (size_t)(i0 + i) * MAXJP);
+#pragma unroll
+                for (int q = 0; q < MAXJP / VW; q++) {
+                    const V c4 = cv[q];
+                    const T *ce = reinterpret_cast<const T *>(&c4);
+#pragma unroll
+                    for (int w = 0; w < VW; w++) acc[q * VW + w] += ce[w] * xv;
+                }
+            }
+        }
+        // sum the point groups, then one atomic add per (projector, column)
+        __syncthreads();
+        T *red = xs;  // reuse: [HALVES][MAXJ][NC]
+#pragma unroll
+        for (int j = 0; j < MAXJ; j++) red[((size_t)h * MAXJ + j) * NC + n] = acc[j];
+        __syncthreads();
+        for (int e = t; e < MAXJ * NC; e += kProjThreads) {
+            const int j = e / NC, c = e % NC;
+            if (j < np && n0 + c < ncol) {
+                T s = T(0);
+#pragma unroll
+                for (int hh = 0; hh < HALVES; hh++) s += red[((size_t)hh * MAXJ + j) * NC + c];
+                const int row = ip_displ[a] + j;
+                atomicAdd(alpha + (long)row * lda + n0 + c, dV * gamma[row] * s);
+            }
+        }
+    }
+}
+
+// Apply: one thread per covered grid point, looping over column blocks of CB; alpha rows are
+// read as vectors (VW elements per load, broadcast across the warp when neighbouring points
+// share an atom).
+template <typename T, int CB, int VW, int NPMAX>
 __global__ void __launch_bounds__(256)
     k_nl_apply(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
                const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
@@ -117,31 +150,42 @@ __global__ void __launch_bounds__(256)
     using V = typename VecOf<T, VW>::type;
     const int cidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (cidx >= ncov) return;
-    const int n0 = blockIdx.y * CB;
-    T acc[CB];
+    const long p = cov_pt[cidx];
+    const int e0 = cov_ptr[cidx], e1 = cov_ptr[cidx + 1];
+    for (int n0 = 0; n0 < ncol; n0 += CB) {
+        T acc[CB], ov[CB];
+        // the output values are read first so their latency overlaps the projector sums
 #pragma unroll
-    for (int c = 0; c < CB; c++) acc[c] = T(0);
-    const int e1 = cov_ptr[cidx + 1];
-    for (int e = cov_ptr[cidx]; e < e1; e++) {
-        const int4 meta = ent_meta[e];  // (first projector row, projector count, image size)
-        const int ip = meta.x, np = meta.y, ndc = meta.z;
-        const T *__restrict__ ch = chi + ent_chi[e];
-        for (int j = 0; j < np; j++) {
-            const T cv = __ldg(ch + (long)j * ndc);
-            const V *__restrict__ al = reinterpret_cast<const V *>(alpha + (long)(ip + j) * lda + n0);
+        for (int c = 0; c < CB; c++) {
+            acc[c] = T(0);
+            ov[c] = n0 + c < ncol ? out[(long)(n0 + c) * ldo + p] : T(0);
+        }
+        for (int e = e0; e < e1; e++) {
+            const int4 meta = ent_meta[e];  // (first projector row, projector count, ndc, image)
+            const int ip = meta.x, np = meta.y, ndc = meta.z;
+            const T *__restrict__ ch = chi + ent_chi[e];
+            T cvs[NPMAX];  // all Chi values of the entry, loads issued together
 #pragma unroll
-            for (int c = 0; c < CB / VW; c++) {
-                const V av = __ldg(al + c);
-                const T *ae = reinterpret_cast<const T *>(&av);
+            for (int j = 0; j < NPMAX; j++) cvs[j] = j < np ? __ldg(ch + (long)j * ndc) : T(0);
 #pragma unroll
-                for (int w = 0; w < VW; w++) acc[c * VW + w] += cv * ae[w];
+            for (int j = 0; j < NPMAX; j++) {
+                if (j >= np) break;
+                const T cv = cvs[j];
+                const V *__restrict__ al =
+                    reinterpret_cast<const V *>(alpha + (long)(ip + j) * lda + n0);
+#pragma unroll
+                for (int c = 0; c < CB / VW; c++) {
+                    const V av = __ldg(al + c);
+                    const T *ae = reinterpret_cast<const T *>(&av);
+#pragma unroll
+                    for (int w = 0; w < VW; w++) acc[c * VW + w] += cv * ae[w];
+                }
             }
         }
-    }
-    const long p = cov_pt[cidx];
 #pragma unroll
-    for (int c = 0; c < CB; c++)
-        if (n0 + c < ncol) out[(long)(n0 + c) * ldo + p] += scale * acc[c];
+        for (int c = 0; c < CB; c++)
+            if (n0 + c < ncol) out[(long)(n0 + c) * ldo + p] = ov[c] + scale * acc[c];
+    }
 }
 
 template <typename T>
@@ -169,21 +213,24 @@ long nonlocal_alpha_ld(int ncol, int elem_bytes)
 }
 
 template <typename T, int MAXJ>
-static void project_launch(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
-                           cudaStream_t st)
+static int project_launch(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
+                          cudaStream_t st)
 {
-    constexpr int NC = kProjThreads / 8, PCH = sizeof(T) == 4 ? 128 : 64;
+    constexpr int NC = sizeof(T) == 4 ? 128 : 64, PCH = 64;
+    constexpr int VW = 16 / sizeof(T), MAXJP = (MAXJ + VW - 1) / VW * VW;
+    constexpr int HALVES = kProjThreads / NC;
+    const size_t xs_elems = std::max((size_t)NC * (PCH + 1), (size_t)HALVES * MAXJ * NC);
+    const size_t smem = sizeof(T) * ((size_t)MAXJP * kSegPts + xs_elems) + sizeof(int) * kSegPts;
+    auto kern = k_nl_project<T, PCH, NC, MAXJ>;
+    SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
     const Nonlocal &nl = ctx->nl;
-    const int ncb = (ncol + NC - 1) / NC;
-    for (int cb0 = 0; cb0 < ncb; cb0 += 65535) {
-        int nb = std::min(65535, ncb - cb0);
-        dim3 grid(nl.nimg, nb);
-        ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
-        k_nl_project<T, PCH, NC, MAXJ><<<grid, kProjThreads, 0, st>>>(
-            nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, chi_of<T>(nl),
-            nl.ip_displ, gamma_of<T>(nl), ncol - cb0 * NC, x + (long)cb0 * NC * ldx, ldx,
-            alpha + (long)cb0 * NC, lda, (T)ctx->dV);
-    }
+    ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
+    kern<<<nl.nseg, kProjThreads, smem, st>>>(
+        nl.seg_img, nl.seg_start, nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off,
+        nl.grid_pos, chi_of<T>(nl), nl.ip_displ, gamma_of<T>(nl), ncol, x, ldx, alpha, lda,
+        (T)ctx->dV);
+    return SGPU_OK;
 }
 
 template <typename T>
@@ -193,11 +240,11 @@ int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *al
     const Nonlocal &nl = ctx->nl;
     if (!ctx->has_nl || nl.nimg == 0 || ncol <= 0) return SGPU_OK;
     if (nl.max_np <= 9)
-        project_launch<T, 9>(ctx, ncol, x, ldx, alpha, lda, st);
+        SGPU_TRY(project_launch<T, 9>(ctx, ncol, x, ldx, alpha, lda, st));
     else if (nl.max_np <= 18)
-        project_launch<T, 18>(ctx, ncol, x, ldx, alpha, lda, st);
+        SGPU_TRY(project_launch<T, 18>(ctx, ncol, x, ldx, alpha, lda, st));
     else if (nl.max_np <= 32)
-        project_launch<T, 32>(ctx, ncol, x, ldx, alpha, lda, st);
+        SGPU_TRY(project_launch<T, 32>(ctx, ncol, x, ldx, alpha, lda, st));
     else {
         set_error("nonlocal: more than 32 projectors per atom is not built");
         return SGPU_ERR_ARG;
@@ -214,16 +261,19 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
     if (!ctx->has_nl || nl.ncov == 0 || ncol <= 0) return SGPU_OK;
     constexpr int CB = apply_cb<T>();
     constexpr int VW = sizeof(T) == 4 ? 4 : 2;
-    const int ncb = (ncol + CB - 1) / CB;
-    for (int cb0 = 0; cb0 < ncb; cb0 += 65535) {
-        int nb = std::min(65535, ncb - cb0);
-        dim3 grid((nl.ncov + 255) / 256, nb);
-        ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
-        k_nl_apply<T, CB, VW><<<grid, 256, 0, st>>>(
-            nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, chi_of<T>(nl),
-            ncol - cb0 * CB, alpha + (long)cb0 * CB, lda, (T)scale,
-            out + (long)cb0 * CB * ldo, ldo);
-    }
+    const dim3 grid((nl.ncov + 255) / 256);
+    ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+#define SGPU_APPLY(NPM)                                                                      \
+    k_nl_apply<T, CB, VW, NPM><<<grid, 256, 0, st>>>(nl.ncov, nl.cov_pt, nl.cov_ptr,         \
+                                                     nl.ent_chi, nl.ent_meta, chi_of<T>(nl), \
+                                                     ncol, alpha, lda, (T)scale, out, ldo)
+    if (nl.max_np <= 9)
+        SGPU_APPLY(9);
+    else if (nl.max_np <= 18)
+        SGPU_APPLY(18);
+    else
+        SGPU_APPLY(32);
+#undef SGPU_APPLY
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
 }
@@ -241,7 +291,8 @@ void nonlocal_free(Nonlocal &nl)
 {
     void *ptrs[] = {nl.ip_displ, nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off,
                     nl.grid_pos, nl.chi64,    nl.chi32,   nl.gamma64, nl.gamma32,
-                    nl.cov_pt,   nl.cov_ptr,  nl.ent_chi, nl.ent_meta};
+                    nl.cov_pt,   nl.cov_ptr,  nl.ent_chi, nl.ent_meta, nl.seg_img,
+                    nl.seg_start};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     nl = Nonlocal();
@@ -321,6 +372,14 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     }
     nl.ncov = (int)covpts.size();
     nl.nent = npos;
+    // projection work split: segments of at most kSegPts points per image
+    std::vector<int> seg_img, seg_start;
+    for (int g = 0; g < nimg; g++)
+        for (int s0 = 0; s0 < img_ndc[g]; s0 += kSegPts) {
+            seg_img.push_back(g);
+            seg_start.push_back(s0);
+        }
+    nl.nseg = (int)seg_img.size();
 
     std::vector<float> chi32(nchi), gamma32(nl.ntot);
     for (long i = 0; i < nchi; i++) chi32[i] = (float)chi[i];
@@ -343,6 +402,8 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(cov_ptr, covptr.data(), covptr.size());
     UP(ent_chi, ent_chi.data(), ent_chi.size());
     UP(ent_meta, ent_meta.data(), ent_meta.size());
+    UP(seg_img, seg_img.data(), seg_img.size());
+    UP(seg_start, seg_start.data(), seg_start.size());
 #undef UP
     if (rc != SGPU_OK) {
         nonlocal_free(nl);

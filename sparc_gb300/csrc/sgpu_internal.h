@@ -68,6 +68,10 @@ struct Nonlocal {
     int *cov_ptr = nullptr;     // ncov + 1
     long *ent_chi = nullptr;    // nent: offset of the entry's Chi row (image block + index)
     int4 *ent_meta = nullptr;   // nent: (first projector row, projector count, ndc, image)
+    // projection work items: (image, first point) segments
+    int nseg = 0;
+    int *seg_img = nullptr;
+    int *seg_start = nullptr;
 };
 
 struct Workspace {

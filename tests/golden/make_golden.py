@@ -95,6 +95,35 @@ def capture(sysd, psp_dir, out_path, ncol, seed, cheb_m, cheb_bounds):
     np.savez_compressed(out_path, **out)
 
 
+def capture_kpt(sysd, psp_dir, out_path, ncol, seed, kpts, cheb_m, cheb_bounds):
+    """Reference k-point kernels (complex orbitals, Bloch phases) on seeded inputs."""
+    from ref_capture import RefKpt, RefSystem
+
+    tmp = tempfile.mkdtemp(prefix="sparc_golden_kpt_")
+    base = systems.write_system(sysd, tmp, psp_dir)
+    r = RefSystem(base)
+    rk = RefKpt(r)
+    types, images = rk.images()
+    flat = flatten_nonlocal(types, images, r.n_atom)
+    coords = np.stack([im["coords"] for im in images]) if images else np.zeros((0, 3))
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (ncol, r.Nd)) + 1j * rng.uniform(-1, 1, (ncol, r.Nd))
+    veff = smooth_potential(rng, r.Nx, r.Ny, r.Nz, r.L)
+    out = dict(Nx=r.Nx, Ny=r.Ny, Nz=r.Nz, FDn=r.order // 2, h=r.h, L=r.L, dV=r.dV, cx=r.cx,
+               cy=r.cy, cz=r.cz, n_atom=r.n_atom, x=x, veff=veff, kpts=rk.kpts[list(kpts)],
+               kpt_index=np.array(kpts), img_coords=coords, cheb_m=cheb_m,
+               cheb_bounds=np.array(cheb_bounds), **{"nl_" + k: v for k, v in flat.items()})
+    for slot, kp in enumerate(kpts):
+        out[f"lap_plus_diag_{slot}"] = rk.lap_plus_diag(kp, -0.5, 1.0, 0.3, veff, x)
+        out[f"vnl_{slot}"] = rk.vnl(kp, x)
+        out[f"hamiltonian_{slot}"] = rk.hamiltonian(kp, veff, -1.2, x)
+        Xo, Yo = rk.chebyshev(kp, veff, cheb_m, cheb_bounds[0], cheb_bounds[1], cheb_bounds[2],
+                              x)
+        out[f"cheb_X_{slot}"] = Xo
+        out[f"cheb_Y_{slot}"] = Yo
+    np.savez_compressed(out_path, **out)
+
+
 def capture_scf(sysd, psp_dir, out_npz, out_json, sparc_bin):
     """Reference SCF run of the system (the program itself, single rank) plus the set-up
     data an SCF needs, so the GPU SCF can start from the reference's own inputs."""
@@ -140,6 +169,14 @@ def main():
         if p.exitcode != 0:
             raise SystemExit(f"capture failed for {sysd['name']}")
         print("wrote", path, os.path.getsize(path), "bytes")
+    kpath = os.path.join(HERE, "si2_kpt_kernels.npz")
+    p = ctx.Process(target=capture_kpt, args=(systems.si2_kpt(), psp_dir, kpath, 2, 13, (0, 8),
+                                              12, (0.5, 40.0, -0.8)))
+    p.start()
+    p.join()
+    if p.exitcode != 0:
+        raise SystemExit("k-point capture failed")
+    print("wrote", kpath, os.path.getsize(kpath), "bytes")
     sparc_bin = os.path.join(HERE, "..", "..", "oracle", "_ref", "sparc")
     for sysd in (systems.si8_c1(),):
         npz = os.path.join(HERE, f"{sysd['name']}_scf.npz")

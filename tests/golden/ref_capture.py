@@ -123,6 +123,83 @@ class RefSystem:
         return r
 
 
+class RefKpt:
+    """k-point (complex) kernels of a RefSystem built from a system with a k-point grid.
+    Complex blocks are numpy complex128 arrays of shape (ncol, Nd)."""
+
+    def __init__(self, r):
+        self.r = r
+        self.lib = r.lib
+        self.lib.ref_nloc_copy_kpt.restype = ctypes.c_double
+        k = np.zeros(3 * 4096)
+        w = np.zeros(4096)
+        nk = self.lib.ref_kpoints(_d(k), _d(w))
+        self.kpts = k[:3 * nk].reshape(nk, 3).copy()
+        self.wts = w[:nk].copy()
+
+    def images(self):
+        """Per image: atom index, grid_pos, real Chi (ndc x nproj) and image coordinates."""
+        types = []
+        out = []
+        for t in range(self.r.Ntypes):
+            ints = np.zeros(16, dtype=np.int32)
+            gam = np.zeros(64)
+            self.lib.ref_psd(t, _i(ints), _d(gam))
+            lmax, lloc, np_, nat = (int(v) for v in ints[:4])
+            ppl = ints[4:4 + lmax + 1].copy()
+            types.append(dict(lmax=lmax, lloc=lloc, nproj=np_, natom=nat, ppl=ppl,
+                              gamma=gam[:int(ppl.sum())].copy()))
+            for iat in range(self.lib.ref_nloc_natom(t)):
+                info = np.zeros(2, dtype=np.int32)
+                self.lib.ref_nloc_atom(t, iat, _i(info))
+                ndc = int(info[0])
+                gp = np.zeros(ndc, dtype=np.int32)
+                chi = np.zeros(max(ndc * np_, 1))
+                mi = self.lib.ref_nloc_copy_kpt(t, iat, _i(gp), _d(chi))
+                assert mi == 0.0, "complex projectors are expected to be real-valued"
+                xyz = np.zeros(3)
+                self.lib.ref_nloc_image_coords(t, iat, _d(xyz))
+                out.append(dict(atom_index=int(info[1]), grid_pos=gp,
+                                chi=chi[:ndc * np_].reshape(np_, ndc).T.copy(), coords=xyz))
+        return types, out
+
+    def lap_plus_diag(self, kpt, a, b, c, v, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.zeros_like(x)
+        vv = np.ascontiguousarray(v, dtype=np.float64) if v is not None else None
+        self.lib.ref_lap_plus_diag_kpt(ctypes.c_int(kpt), ctypes.c_int(x.shape[0]),
+                                       ctypes.c_double(a), ctypes.c_double(b),
+                                       ctypes.c_double(c), _d(vv) if vv is not None else None,
+                                       _d(x.view(np.float64)), _d(y.view(np.float64)))
+        return y
+
+    def vnl(self, kpt, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        hx = np.zeros_like(x)
+        self.lib.ref_vnl_kpt(ctypes.c_int(kpt), ctypes.c_int(x.shape[0]),
+                             _d(x.view(np.float64)), _d(hx.view(np.float64)))
+        return hx
+
+    def hamiltonian(self, kpt, veff, c, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        hx = np.zeros_like(x)
+        veff = np.ascontiguousarray(veff, dtype=np.float64)
+        self.lib.ref_hamiltonian_kpt(ctypes.c_int(kpt), ctypes.c_int(x.shape[0]), _d(veff),
+                                     ctypes.c_double(c), _d(x.view(np.float64)),
+                                     _d(hx.view(np.float64)))
+        return hx
+
+    def chebyshev(self, kpt, veff, m, a, b, a0, X):
+        X = np.array(X, dtype=np.complex128, order="C")
+        Y = np.zeros_like(X)
+        veff = np.ascontiguousarray(veff, dtype=np.float64)
+        self.lib.ref_chebyshev_kpt(ctypes.c_int(kpt), _d(veff), ctypes.c_int(X.shape[0]),
+                                   ctypes.c_int(m), ctypes.c_double(a), ctypes.c_double(b),
+                                   ctypes.c_double(a0), _d(X.view(np.float64)),
+                                   _d(Y.view(np.float64)))
+        return X, Y
+
+
 def scf_setup(r):
     """SCF inputs from the reference set-up of system r (a RefSystem), plus the reference's
     own Vxc and electrostatic potential for the initial density."""

@@ -54,6 +54,15 @@ def si2_small(seed=7):
     )
 
 
+def si2_kpt(seed=8):
+    """The 2-atom Si box with a 3x3x3 k-point grid (complex Bloch orbitals): a fast case for
+    the k-point kernels (Bloch phases at the periodic faces and on atom images)."""
+    d = si2_small(seed)
+    d["name"] = "Si2_kpt"
+    d["kpoint_grid"] = (3, 3, 3)
+    return d
+
+
 def write_system(sysd, outdir, psp_dir):
     """Write <name>.inpt and <name>.ion for the system into outdir."""
     os.makedirs(outdir, exist_ok=True)
@@ -61,7 +70,7 @@ def write_system(sysd, outdir, psp_dir):
     L = sysd["L"]
     lines = [f"LATVEC_SCALE: {L[0]:.10f} {L[1]:.10f} {L[2]:.10f}",
              "LATVEC:", "1 0 0", "0 1 0", "0 0 1",
-             "BC: P P P", "KPOINT_GRID: 1 1 1"]
+             "BC: P P P", "KPOINT_GRID: %d %d %d" % tuple(sysd.get("kpoint_grid", (1, 1, 1)))]
     for k, v in sysd["keys"].items():
         lines.append(f"{k}: {v}")
     with open(os.path.join(outdir, name + ".inpt"), "w") as f:
