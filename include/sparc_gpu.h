@@ -123,6 +123,38 @@ int sgpu_ChebyshevFiltering_f32(sgpu_ctx *ctx, int spin, float *X, int ldi, floa
 int sgpu_poisson_residual(sgpu_ctx *ctx, double c, const double *x, const double *b,
                           double *r);
 
+/* ------------------------------------------------------------ k-point (Bloch) rows */
+
+/* Cell lengths (range_x/y/z) and the coordinates of the n_img atom images of the nonlocal
+ * set, in the order given to sgpu_set_nonlocal (Atom_Influence_nloc.coords,
+ * src/include/isddft.h:202-216); needed for the Bloch factors of the k-point calls. */
+int sgpu_set_kpoint_geometry(sgpu_ctx *ctx, double Lx, double Ly, double Lz, int n_img,
+                             const double *img_coords);
+
+/* Complex blocks below are interleaved (re, im) doubles, i.e. SPARC's double _Complex arrays;
+ * k = (k1_loc[kpt], k2_loc[kpt], k3_loc[kpt]) in 1/Bohr. */
+
+/* y = (a*Lap + b*diag(v) + c*I) x for Bloch columns at k. Replaces
+ * Lap_plus_diag_vec_mult_orth_kpt (src/lapVecRoutinesKpt.c:179). */
+int sgpu_Lap_plus_diag_vec_mult_orth_kpt(sgpu_ctx *ctx, const double *k, int ncol, double a,
+                                         double b, double c, const double *v, const double *x,
+                                         int ldi, double *y, int ldo);
+
+/* Hx += Vnl x at k. Replaces Vnl_vec_mult_kpt (src/nlocVecRoutines.c:889). */
+int sgpu_Vnl_vec_mult_kpt(sgpu_ctx *ctx, const double *k, int ncol, const double *x, int ldi,
+                          double *Hx, int ldo);
+
+/* Hx = (-0.5*Lap + Veff[spin] + c) x + Vnl x at k. Replaces Hamiltonian_vectors_mult_kpt
+ * (src/hamiltonianVecRoutines.c:132). */
+int sgpu_Hamiltonian_vectors_mult_kpt(sgpu_ctx *ctx, int spin, const double *k, int ncol,
+                                      double c, const double *x, int ldi, double *Hx, int ldo);
+
+/* Chebyshev filter of Bloch columns at k (complex128, or complex64 arithmetic with
+ * SGPU_PREC_FP32). Replaces ChebyshevFiltering_kpt (src/eigenSolverKpt.c:458). */
+int sgpu_ChebyshevFiltering_kpt(sgpu_ctx *ctx, int spin, const double *k, double *X, int ldi,
+                                double *Y, int ldo, int ncol, int m, double a, double b,
+                                double a0, int precision);
+
 /* ------------------------------------------------------------- Rayleigh-Ritz step */
 
 /* HY = H Y (spin block spin), Hp = Yᵀ HY and Mp = Yᵀ Y (Ns x Ns = ncol x ncol, column-major,

@@ -27,6 +27,8 @@ EXPORTED = [
     "sgpu_CalculateDensity_psi", "sgpu_Calculate_Vxc_LDA_PW", "sgpu_AAR",
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
     "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_Vnl_vec_mult_noalloc",
+    "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
+    "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt",
 ]
 
 SGPU_ERR_NOT_CONVERGED = 5
@@ -196,6 +198,48 @@ class Context:
         _check(lib().sgpu_poisson_residual(self._h, ctypes.c_double(c), _ptr(x), _ptr(b),
                                            _ptr(r)))
         return r
+
+    # ---- k-point rows (complex128 numpy arrays (ncol, Nd) or complex torch tensors)
+    def set_kpoint_geometry(self, L, img_coords):
+        ic = np.ascontiguousarray(img_coords, dtype=np.float64).reshape(-1)
+        _check(lib().sgpu_set_kpoint_geometry(self._h, ctypes.c_double(L[0]),
+                                              ctypes.c_double(L[1]), ctypes.c_double(L[2]),
+                                              int(ic.size // 3), _ptr(ic)))
+
+    @staticmethod
+    def _kvec(k):
+        return np.ascontiguousarray(k, dtype=np.float64)
+
+    def Lap_plus_diag_vec_mult_orth_kpt(self, k, a, b, c, v, x, y):
+        ncol, ld = self._ncol_ld(x)
+        kv = self._kvec(k)
+        _check(lib().sgpu_Lap_plus_diag_vec_mult_orth_kpt(
+            self._h, _ptr(kv), ncol, ctypes.c_double(a), ctypes.c_double(b), ctypes.c_double(c),
+            _ptr(v), _ptr(x), ld, _ptr(y), ld))
+        return y
+
+    def Vnl_vec_mult_kpt(self, k, x, hx):
+        ncol, ld = self._ncol_ld(x)
+        kv = self._kvec(k)
+        _check(lib().sgpu_Vnl_vec_mult_kpt(self._h, _ptr(kv), ncol, _ptr(x), ld, _ptr(hx), ld))
+        return hx
+
+    def Hamiltonian_vectors_mult_kpt(self, k, c, x, hx, spin=0):
+        ncol, ld = self._ncol_ld(x)
+        kv = self._kvec(k)
+        _check(lib().sgpu_Hamiltonian_vectors_mult_kpt(self._h, int(spin), _ptr(kv), ncol,
+                                                       ctypes.c_double(c), _ptr(x), ld, _ptr(hx),
+                                                       ld))
+        return hx
+
+    def ChebyshevFiltering_kpt(self, k, X, Y, m, a, b, a0, spin=0, precision=SGPU_PREC_FP64):
+        ncol, ld = self._ncol_ld(X)
+        kv = self._kvec(k)
+        _check(lib().sgpu_ChebyshevFiltering_kpt(self._h, int(spin), _ptr(kv), _ptr(X), ld,
+                                                 _ptr(Y), ld, ncol, int(m), ctypes.c_double(a),
+                                                 ctypes.c_double(b), ctypes.c_double(a0),
+                                                 int(precision)))
+        return X, Y
 
     # ---- Rayleigh-Ritz
     def Project_Hamiltonian(self, Y, HY, Hp, Mp, spin=0):

@@ -209,6 +209,7 @@ int sgpu_destroy(sgpu_ctx *ctx)
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx->mix;
+    kpoint_free(ctx);
     delete ctx;
     return SGPU_OK;
 }

@@ -79,6 +79,9 @@ struct Workspace {
     size_t bytes = 0;
 };
 
+struct KpointState;  // kpoint.cu
+void kpoint_free(sgpu_ctx *ctx);
+
 // periodic-Pulay density mixing parameters (SPARC_OBJ fields of the same meaning)
 struct MixParams {
     int m = 7;                 // MixingHistory
@@ -122,6 +125,7 @@ struct sgpu_ctx {
     cusolverDnHandle_t cusolver = nullptr;
     sgpu::Workspace ws[12];    // grow-only scratch slots (see enum WsSlot)
     sgpu::MixState *mix = nullptr;
+    sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on
