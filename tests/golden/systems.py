@@ -40,6 +40,22 @@ def si8_c1(seed=20261203):
     )
 
 
+def si216_c4(seed=20261204):
+    """216-atom diamond Si (3x3x3 cells, a = 30.78 Bohr), displacements N(0, 0.1^2) Bohr,
+    h = 0.40 (77^3 grid), LDA_PW, 520 states, Chebyshev degree 24, Gamma point."""
+    a = 10.26
+    rng = np.random.default_rng(seed)
+    pos = diamond_supercell(a, 3) + rng.normal(0.0, 0.1, size=(216, 3))
+    L = 3 * a
+    return dict(
+        name="Si216_c4", L=(L, L, L), species=[("Si", pos)],
+        keys=dict(MESH_SPACING="0.40", FD_ORDER="12", EXCHANGE_CORRELATION="LDA_PW",
+                  ELEC_TEMP_TYPE="fermi-dirac", SMEARING="0.001", NSTATES="520",
+                  CHEB_DEGREE="24", MIXING_VARIABLE="density", MIXING_HISTORY="7",
+                  TOL_SCF="1e-6", PRINT_FORCES="1", PRINT_EIGEN="1"),
+    )
+
+
 def si2_small(seed=7):
     """2-atom Si in a 7.0 Bohr cubic box at h=0.5 (14^3 grid): a fast kernel-level case."""
     a = 7.0
