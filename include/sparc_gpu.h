@@ -225,6 +225,54 @@ int sgpu_Mixing_periodic_pulay(sgpu_ctx *ctx, int iter_count, double *rho);
 int sgpu_Evaluate_scf_error(sgpu_ctx *ctx, const double *rho_out, const double *rho_in,
                             double *error);
 
+/* ----------------------------------------------------------------- set-up (per geometry) */
+
+/* Radial tables of one atom type, as read_pseudopotential_PSP (src/readfiles.c:1957) leaves
+ * them in PSD_OBJ (src/include/isddft.h): UdV holds sum(ppl) rows of `size` values (u_l/r,
+ * rows of l == lloc unused), rVloc = r*Vloc(r), densities already divided by 4 pi, and rc[l]
+ * the projector radii after the reader's extension to the last |UdV| > 1e-8. */
+typedef struct {
+    int size;                   /* radial points */
+    int lmax, lloc;             /* psd.lmax, localPsd */
+    int Znucl;                  /* valence charge (SPARC's Znucl) */
+    const int *ppl;             /* projectors per l, lmax+1 */
+    const double *rc;           /* lmax+1 */
+    double Vloc_0, fchrg;       /* Vloc(0); model-core charge flag (> 0: NLCC) */
+    const double *RadialGrid, *UdV, *rVloc, *rhoIsoAtom, *rho_c_table, *Gamma;
+} sgpu_psd;
+
+/* Store the tables of ntypes (<= 8) atom types on the device with their spline slopes
+ * (getYD_gen, src/tools.c:372; src/initialization.c:3470-3492). lmax <= 3. */
+int sgpu_set_psd(sgpu_ctx *ctx, int ntypes, const sgpu_psd *psd);
+
+/* Pseudocharge cut-off radii per type by the reference's bisection on the integrated charge
+ * (Calculate_PseudochargeCutoff, src/electrostatics.c:44). cell: range_x/y/z; tol:
+ * TOL_PSEUDOCHARGE. cutoff receives CUTOFF_x/y/z per type (3*ntypes values). */
+int sgpu_Calculate_PseudochargeCutoff(sgpu_ctx *ctx, const double *cell, double tol,
+                                      double *cutoff);
+
+/* Pseudocharge density b (psdChrgDens), its reference-potential twin b_ref
+ * (psdChrgDens_ref), the atomic superposition density scaled to the electron count
+ * (electronDens_at, the initial density) and the model core density (electronDens_core),
+ * computed on the device for atoms at atom_pos (3*n_atom, type-major, nAtomv per type).
+ * cutoff: 3 per type (NULL: the values of the last cut-off call); ref_cutoff:
+ * REFERENCE_CUTOFF; net_charge: NetCharge. scalars (3, may be NULL) = Esc, PosCharge,
+ * NegCharge. b_ref and rho_core may be NULL; arrays may be host or device memory. Replaces
+ * GetInfluencingAtoms and Generate_PseudoChargeDensity (src/electrostatics.c:578, :772). */
+int sgpu_Generate_PseudoChargeDensity(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                                      const double *atom_pos, const double *cutoff,
+                                      double ref_cutoff, int net_charge, double *b,
+                                      double *b_ref, double *rho_at, double *rho_core,
+                                      double *scalars);
+
+/* Build the nonlocal projectors of the atoms on the device (spline of UdV times real
+ * spherical harmonics over the grid points of each image's rc-sphere) and install them as
+ * sgpu_set_nonlocal would, together with the image coordinates for the k-point calls.
+ * Replaces GetInfluencingAtoms_nloc and CalculateNonlocalProjectors
+ * (src/nlocVecRoutines.c:43, :394). */
+int sgpu_CalculateNonlocalProjectors(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                                     const double *atom_pos);
+
 /* Parameters of a single-point SCF (SPARC_OBJ fields of the same meaning). */
 typedef struct {
     int Nstates;                /* Nstates */

@@ -122,9 +122,50 @@ void ref_setup_fields(double *b, double *bref, double *rho0, double *scalars)
     memcpy(bref, S.psdChrgDens_ref, sizeof(double) * S.Nd);
     memcpy(rho0, S.electronDens, sizeof(double) * S.Nd);
     scalars[0] = S.Esc;
-    scalars[1] = 0.0;
+    scalars[1] = S.PosCharge;
     scalars[2] = S.NegCharge;
     scalars[3] = S.Nelectron;
+}
+
+/* Parsed pseudopotential tables of type ityp (PSD_OBJ, src/include/isddft.h), as
+ * read_pseudopotential_PSP (src/readfiles.c:1957) left them: ints = size, lmax, lloc,
+ * is_r_uniform, Znucl, ppl[0..lmax]; scal = Vloc_0, fchrg, rc[0..lmax]; tables of `size`
+ * points (UdV: sum(ppl) rows of `size`). Pass NULL table pointers to query ints only. */
+void ref_psd_tables(int ityp, int *ints, double *scal, double *grid, double *udv,
+                    double *rvloc, double *rhoiso, double *rhoc, double *gamma)
+{
+    PSD_OBJ *p = &S.psd[ityp];
+    int lmax = p->lmax, n = p->size, tot = 0;
+    ints[0] = n; ints[1] = lmax; ints[2] = S.localPsd[ityp]; ints[3] = p->is_r_uniform;
+    ints[4] = S.Znucl[ityp];
+    for (int l = 0; l <= lmax; l++) { ints[5 + l] = p->ppl[l]; tot += p->ppl[l]; }
+    scal[0] = p->Vloc_0; scal[1] = p->fchrg;
+    for (int l = 0; l <= lmax; l++) scal[2 + l] = p->rc[l];
+    if (!grid) return;
+    memcpy(grid, p->RadialGrid, sizeof(double) * n);
+    memcpy(udv, p->UdV, sizeof(double) * n * tot);
+    memcpy(rvloc, p->rVloc, sizeof(double) * n);
+    memcpy(rhoiso, p->rhoIsoAtom, sizeof(double) * n);
+    memcpy(rhoc, p->rho_c_table, sizeof(double) * n);
+    memcpy(gamma, p->Gamma, sizeof(double) * tot);
+}
+
+/* pseudocharge cutoffs of type ityp (CUTOFF_x/y/z from Calculate_PseudochargeCutoff,
+ * src/electrostatics.c:44), the atom count of the type and the set-up tolerances:
+ * out = CUTOFF_x, CUTOFF_y, CUTOFF_z, nAtomv, TOL_PSEUDOCHARGE, REFERENCE_CUTOFF, NetCharge */
+void ref_cutoff(int ityp, double *out)
+{
+    out[0] = S.CUTOFF_x[ityp]; out[1] = S.CUTOFF_y[ityp]; out[2] = S.CUTOFF_z[ityp];
+    out[3] = S.nAtomv[ityp];
+    out[4] = S.TOL_PSEUDOCHARGE; out[5] = S.REFERENCE_CUTOFF; out[6] = S.NetCharge;
+}
+
+/* pseudocharge density of the reference potentials (psdChrgDens_ref) and the atomic
+ * superposition density before the charge scaling is undone: electronDens_at */
+void ref_setup_fields2(double *bref, double *rho_at)
+{
+    memcpy(bref, S.psdChrgDens_ref, sizeof(double) * S.Nd);
+    memcpy(rho_at, S.electronDens_at, sizeof(double) * S.Nd);
 }
 
 static int g_dims1[3] = {1, 1, 1};

@@ -28,8 +28,20 @@ EXPORTED = [
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
     "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_Vnl_vec_mult_noalloc",
     "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
-    "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt",
+    "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
+    "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
+    "sgpu_CalculateNonlocalProjectors",
 ]
+
+
+class Psd(ctypes.Structure):
+    """sgpu_psd (include/sparc_gpu.h): one atom type's radial tables."""
+    _fields_ = [("size", ctypes.c_int), ("lmax", ctypes.c_int), ("lloc", ctypes.c_int),
+                ("Znucl", ctypes.c_int), ("ppl", ctypes.c_void_p), ("rc", ctypes.c_void_p),
+                ("Vloc_0", ctypes.c_double), ("fchrg", ctypes.c_double),
+                ("RadialGrid", ctypes.c_void_p), ("UdV", ctypes.c_void_p),
+                ("rVloc", ctypes.c_void_p), ("rhoIsoAtom", ctypes.c_void_p),
+                ("rho_c_table", ctypes.c_void_p), ("Gamma", ctypes.c_void_p)]
 
 SGPU_ERR_NOT_CONVERGED = 5
 
@@ -143,6 +155,54 @@ class Context:
         _check(lib().sgpu_set_nonlocal(self._h, len(arrs[0]) - 1, _ptr(arrs[0]), _ptr(arrs[1]),
                                        len(arrs[2]), _ptr(arrs[2]), _ptr(arrs[3]), _ptr(arrs[4]),
                                        _ptr(arrs[5])))
+
+    # ---- per-geometry set-up (pseudopotential tables from sparc_gb300.psp8.read_psp8)
+    def set_psd(self, tables):
+        """Store the radial tables of each atom type (a list of read_psp8 dicts)."""
+        keep, structs = [], []
+        for t in tables:
+            arrs = dict(ppl=np.ascontiguousarray(t["ppl"], dtype=np.int32))
+            for k in ("rc", "RadialGrid", "UdV", "rVloc", "rhoIsoAtom", "rho_c_table", "Gamma"):
+                arrs[k] = np.ascontiguousarray(t[k], dtype=np.float64)
+            keep.append(arrs)
+            structs.append(Psd(int(t["size"]), int(t["lmax"]), int(t["lloc"]), int(t["Znucl"]),
+                               arrs["ppl"].ctypes.data, arrs["rc"].ctypes.data,
+                               float(t["Vloc_0"]), float(t["fchrg"]),
+                               *(arrs[k].ctypes.data for k in ("RadialGrid", "UdV", "rVloc",
+                                                               "rhoIsoAtom", "rho_c_table",
+                                                               "Gamma"))))
+        arr = (Psd * len(structs))(*structs)
+        _check(lib().sgpu_set_psd(self._h, len(structs), arr))
+        self._psd_keep = keep
+
+    def Calculate_PseudochargeCutoff(self, cell, tol):
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        out = np.zeros(3 * len(self._psd_keep))
+        _check(lib().sgpu_Calculate_PseudochargeCutoff(self._h, _ptr(cell), ctypes.c_double(tol),
+                                                       _ptr(out)))
+        return out.reshape(-1, 3)
+
+    def Generate_PseudoChargeDensity(self, cell, nAtomv, atom_pos, ref_cutoff=0.5,
+                                     net_charge=0, cutoff=None, want_bref=False):
+        """Returns dict(b, b_ref, rho_at, rho_core, Esc, PosCharge, NegCharge) (host arrays)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        nat = np.ascontiguousarray(nAtomv, dtype=np.int32)
+        pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
+        cut = None if cutoff is None else np.ascontiguousarray(cutoff, dtype=np.float64)
+        b, rho, core = (np.zeros(self.Nd) for _ in range(3))
+        bref = np.zeros(self.Nd) if want_bref else None
+        sc = np.zeros(3)
+        _check(lib().sgpu_Generate_PseudoChargeDensity(
+            self._h, _ptr(cell), _ptr(nat), _ptr(pos), _ptr(cut), ctypes.c_double(ref_cutoff),
+            int(net_charge), _ptr(b), _ptr(bref), _ptr(rho), _ptr(core), _ptr(sc)))
+        return dict(b=b, b_ref=bref, rho_at=rho, rho_core=core, Esc=float(sc[0]),
+                    PosCharge=float(sc[1]), NegCharge=float(sc[2]))
+
+    def CalculateNonlocalProjectors(self, cell, nAtomv, atom_pos):
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        nat = np.ascontiguousarray(nAtomv, dtype=np.int32)
+        pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
+        _check(lib().sgpu_CalculateNonlocalProjectors(self._h, _ptr(cell), _ptr(nat), _ptr(pos)))
 
     # ---- hot path (x, y: (ncol, Nd) C-contiguous == Nd x ncol column-major, ld = Nd)
     def _ncol_ld(self, x):

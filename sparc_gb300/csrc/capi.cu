@@ -210,6 +210,7 @@ int sgpu_destroy(sgpu_ctx *ctx)
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx->mix;
     kpoint_free(ctx);
+    setup_free(ctx);
     delete ctx;
     return SGPU_OK;
 }

@@ -81,6 +81,8 @@ struct Workspace {
 
 struct KpointState;  // kpoint.cu
 void kpoint_free(sgpu_ctx *ctx);
+struct SetupState;   // setup.cu
+void setup_free(sgpu_ctx *ctx);
 
 // periodic-Pulay density mixing parameters (SPARC_OBJ fields of the same meaning)
 struct MixParams {
@@ -126,6 +128,7 @@ struct sgpu_ctx {
     sgpu::Workspace ws[12];    // grow-only scratch slots (see enum WsSlot)
     sgpu::MixState *mix = nullptr;
     sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)
+    sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on

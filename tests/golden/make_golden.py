@@ -151,11 +151,57 @@ def capture_scf(sysd, psp_dir, out_npz, out_json, sparc_bin):
         json.dump(ref, fh, indent=1)
 
 
+def capture_setup(sysd, psp_dir, out_npz):
+    """Inputs and outputs of the reference's per-geometry set-up: parsed pseudopotential
+    tables, atom positions as read, pseudocharge cut-offs, pseudocharge densities, initial and
+    core densities, Esc, and the nonlocal projectors."""
+    from ref_capture import RefSystem
+
+    tmp = tempfile.mkdtemp(prefix="sparc_setup_")
+    base = systems.write_system(sysd, tmp, psp_dir)
+    r = RefSystem(base)
+    types, images = r.nonlocal_data()
+    flat = flatten_nonlocal(types, images, r.n_atom)
+    out = dict(Nx=r.Nx, Ny=r.Ny, Nz=r.Nz, FDn=r.order // 2, h=r.h, L=r.L, dV=r.dV, cx=r.cx,
+               cy=r.cy, cz=r.cz, n_atom=r.n_atom, Ntypes=r.Ntypes,
+               atom_pos=r.atom_positions(), **{"nl_" + k: v for k, v in flat.items()})
+    nat = []
+    for t in range(r.Ntypes):
+        tab = r.psd_tables(t)
+        out.update({f"t{t}_{k}": v for k, v in tab.items()})
+        cut = r.cutoff(t)
+        out[f"t{t}_cutoff"] = cut["cutoff"]
+        nat.append(cut["natom"])
+        out.update(tol_pseudocharge=cut["tol"], ref_cutoff=cut["ref_cutoff"],
+                   net_charge=cut["net_charge"])
+    out["nAtomv"] = np.array(nat, dtype=np.int32)
+    f = r.setup_fields()
+    f2 = r.setup_fields2()
+    out.update(b=f["b"], b_ref=f2["b_ref"], rho0=f["rho0"], rho_at=f2["rho_at"],
+               rho_core=r.core_density(), Esc=f["Esc"], PosCharge=f["PosCharge"],
+               NegCharge=f["NegCharge"], Nelectron=f["Nelectron"])
+    np.savez_compressed(out_npz, **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "setup"], default=None,
+                    help="regenerate one group of fixtures only")
     args = ap.parse_args()
     psp_dir = os.path.join(args.ref, "psps")
+    ctx = mp.get_context("spawn")
+    if args.only in (None, "setup"):
+        for sysd in (systems.si2_small(), systems.si8_c1(), systems.al4_small()):
+            path = os.path.join(HERE, f"{sysd['name']}_setup.npz")
+            p = ctx.Process(target=capture_setup, args=(sysd, psp_dir, path))
+            p.start()
+            p.join()
+            if p.exitcode != 0:
+                raise SystemExit(f"set-up capture failed for {sysd['name']}")
+            print("wrote", path, os.path.getsize(path), "bytes")
+        if args.only == "setup":
+            return
     jobs = [
         (systems.si2_small(), os.path.join(HERE, "si2_small_kernels.npz"), 3, 11, 12,
          (0.5, 40.0, -0.8)),

@@ -75,7 +75,41 @@ class RefSystem:
         b, bref, rho0 = (np.zeros(self.Nd) for _ in range(3))
         sc = np.zeros(4)
         self.lib.ref_setup_fields(_d(b), _d(bref), _d(rho0), _d(sc))
-        return dict(b=b, bref=bref, rho0=rho0, Esc=sc[0], NegCharge=sc[2], Nelectron=sc[3])
+        return dict(b=b, bref=bref, rho0=rho0, Esc=sc[0], PosCharge=sc[1], NegCharge=sc[2],
+                    Nelectron=sc[3])
+
+    def setup_fields2(self):
+        bref, rho_at = np.zeros(self.Nd), np.zeros(self.Nd)
+        self.lib.ref_setup_fields2(_d(bref), _d(rho_at))
+        return dict(b_ref=bref, rho_at=rho_at)
+
+    def core_density(self):
+        core = np.zeros(self.Nd)
+        self.lib.ref_core_density(_d(core))
+        return core
+
+    def psd_tables(self, ityp):
+        """The reference's parsed pseudopotential tables of one type (PSD_OBJ)."""
+        ints = np.zeros(16, dtype=np.int32)
+        sc = np.zeros(16)
+        self.lib.ref_psd_tables(ityp, _i(ints), _d(sc), None, None, None, None, None, None)
+        n, lmax = int(ints[0]), int(ints[1])
+        ppl = ints[5:6 + lmax].copy()
+        tot = int(ppl.sum())
+        g, u, rv, ri, rc, ga = (np.zeros(n), np.zeros(n * tot), np.zeros(n), np.zeros(n),
+                                np.zeros(n), np.zeros(tot))
+        self.lib.ref_psd_tables(ityp, _i(ints), _d(sc), _d(g), _d(u), _d(rv), _d(ri), _d(rc),
+                                _d(ga))
+        return dict(size=n, lmax=lmax, lloc=int(ints[2]), is_r_uniform=int(ints[3]),
+                    Znucl=int(ints[4]), ppl=ppl, Vloc_0=sc[0], fchrg=sc[1],
+                    rc=sc[2:3 + lmax].copy(), RadialGrid=g, UdV=u.reshape(tot, n), rVloc=rv,
+                    rhoIsoAtom=ri, rho_c_table=rc, Gamma=ga)
+
+    def cutoff(self, ityp):
+        out = np.zeros(8)
+        self.lib.ref_cutoff(ityp, _d(out))
+        return dict(cutoff=out[:3].copy(), natom=int(out[3]), tol=out[4], ref_cutoff=out[5],
+                    net_charge=int(out[6]))
 
     def atom_positions(self):
         xyz = np.zeros(3 * self.n_atom)

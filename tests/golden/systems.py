@@ -70,6 +70,23 @@ def si2_small(seed=7):
     )
 
 
+def al4_small(seed=9):
+    """4-atom FCC Al conventional cell, a = 7.65 Bohr, displacements N(0, 0.05^2) Bohr,
+    h = 0.5 (16^3 grid): a second species for the set-up checks (its psp8 carries a model
+    core charge and a different projector radius per l)."""
+    a = 7.65
+    rng = np.random.default_rng(seed)
+    fcc = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
+    pos = fcc * a + rng.normal(0.0, 0.05, size=(4, 3))
+    return dict(
+        name="Al4_small", L=(a, a, a), species=[("Al", pos)],
+        keys=dict(MESH_SPACING="0.50", FD_ORDER="12", EXCHANGE_CORRELATION="LDA_PW",
+                  ELEC_TEMP_TYPE="fermi-dirac", SMEARING="0.001", NSTATES="12",
+                  CHEB_DEGREE="16", MIXING_VARIABLE="density", MIXING_HISTORY="7",
+                  TOL_SCF="1e-6", PRINT_FORCES="1", PRINT_EIGEN="1"),
+    )
+
+
 def si2_kpt(seed=8):
     """The 2-atom Si box with a 3x3x3 k-point grid (complex Bloch orbitals): a fast case for
     the k-point kernels (Bloch phases at the periodic faces and on atom images)."""
