@@ -292,7 +292,12 @@ typedef struct {
     double xc_rhotol;
     double Esc;                 /* self and correction energy of the pseudocharges */
     int precision;              /* SGPU_PREC_FP64, or SGPU_PREC_FP32 for the mixed mode */
-    double fp64_switch_error;   /* mixed mode: SCF error below which filtering becomes FP64 */
+    double fp64_switch_error;   /* mixed mode: SCF error below which filtering becomes FP64
+                                   (also left early when the FP32 error stops falling) */
+    int graded_tail;            /* mixed mode after the switch: 0 = plain FP64 CheFSI; 1 = FP32
+                                   filter whose last tail_fp64_degrees degrees run in FP64,
+                                   with the Rayleigh-Ritz step in FP64 */
+    int tail_fp64_degrees;      /* 0 .. cheb_degree-1 (graded_tail = 1) */
     unsigned long long seed;    /* initial orbitals and Lanczos start vector */
     int verbose;
 } sgpu_scf_params;

@@ -61,7 +61,8 @@ class ScfParams(ctypes.Structure):
                 ("kerker", ctypes.c_int), ("kerker_kTF", ctypes.c_double),
                 ("kerker_idiemac", ctypes.c_double), ("xc_rhotol", ctypes.c_double),
                 ("Esc", ctypes.c_double), ("precision", ctypes.c_int),
-                ("fp64_switch_error", ctypes.c_double), ("seed", ctypes.c_ulonglong),
+                ("fp64_switch_error", ctypes.c_double), ("graded_tail", ctypes.c_int),
+                ("tail_fp64_degrees", ctypes.c_int), ("seed", ctypes.c_ulonglong),
                 ("verbose", ctypes.c_int)]
 
 

@@ -9,6 +9,8 @@
 // (e, c, sigma, sigma1, gamma, sigma2, vscal, vscal2) but writes each new iterate in place
 // over the oldest one (its last reader is the thread that writes it), so the filter needs at
 // most one scratch block and no separate scale/axpy/swap pass.
+#include <utility>
+
 #include "sgpu_internal.h"
 
 namespace sgpu {
@@ -98,6 +100,53 @@ int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int n
     if (route && m == 2) {  // the degree-1 iterate is still in the scratch block
         SGPU_CUDA_TRY(cudaMemcpy2DAsync(X, sizeof(T) * ldx, W, sizeof(T) * Nd, sizeof(T) * Nd,
                                         ncol, cudaMemcpyDeviceToDevice, st));
+    }
+    return SGPU_OK;
+}
+
+// Precision-graded filter: degrees 0 .. m-k64-1 in FP32 on (X32, Y32), the last k64 degrees
+// in FP64, the filtered block landing in Y64 (X64 gets the previous iterate). A rounding error
+// made at degree j is multiplied by the remaining m-1-j degrees of the filter like any other
+// component: its part outside the wanted subspace is damped and its part inside is harmless
+// to the Rayleigh-Ritz step, so only the last degrees need FP64 for an FP64-quality subspace.
+// k64 == 0 gives a pure FP32 filter whose result is widened into Y64. All blocks have ld Nd.
+int chebyshev_graded(sgpu_ctx *ctx, int spin, float *X32, float *Y32, double *X64,
+                     double *Y64, int ncol, int m, int k64, double a, double b, double a0,
+                     cudaStream_t st)
+{
+    if (m < 1 || k64 < 0 || k64 >= m) {
+        set_error("ChebyshevFiltering (graded): need 0 <= FP64 degrees < m");
+        return SGPU_ERR_ARG;
+    }
+    const long Nd = ctx->Nd;
+    const double e = 0.5 * (b - a);
+    const double c = 0.5 * (b + a);
+    double sigma = e / (a0 - c);
+    const double sigma1 = sigma;
+    const double gamma = 2.0 / sigma1;
+    const int m32 = m - k64;
+    SGPU_TRY(hamiltonian_dev<float>(ctx, spin, ncol, -c, X32, Nd, Y32, Nd, sigma1 / e, 0.0,
+                                    nullptr, 0, st));
+    float *cur = Y32, *prev = X32;
+    for (int j = 1; j < m32; j++) {
+        const double sigma2 = 1.0 / (gamma - sigma);
+        SGPU_TRY(hamiltonian_dev<float>(ctx, spin, ncol, -c, cur, Nd, prev, Nd,
+                                        2.0 * sigma2 / e, -sigma * sigma2, prev, Nd, st));
+        std::swap(cur, prev);
+        sigma = sigma2;
+    }
+    // widen; the first FP64 step writes over the widened previous iterate, so put that one
+    // where the final iterate must end (Y64) when k64 is odd
+    double *A = (k64 % 2 == 1) ? X64 : Y64, *B = (k64 % 2 == 1) ? Y64 : X64;
+    SGPU_TRY(convert_cols<float, double>(cur, Nd, A, Nd, Nd, ncol, st));
+    SGPU_TRY(convert_cols<float, double>(prev, Nd, B, Nd, Nd, ncol, st));
+    double *cur64 = A, *prev64 = B;
+    for (int j = m32; j < m; j++) {
+        const double sigma2 = 1.0 / (gamma - sigma);
+        SGPU_TRY(hamiltonian_dev<double>(ctx, spin, ncol, -c, cur64, Nd, prev64, Nd,
+                                         2.0 * sigma2 / e, -sigma * sigma2, prev64, Nd, st));
+        std::swap(cur64, prev64);
+        sigma = sigma2;
     }
     return SGPU_OK;
 }

@@ -13,8 +13,10 @@
 // Mixed precision (SGPU_PREC_FP32): while the SCF error is above fp64_switch_error the orbital
 // block is FP32, the filter runs in FP32 and the projection / rotation products use cuBLAS's
 // BF16x9 FP32 emulation on the tensor cores; the eigenproblem, Poisson, XC, mixing and all
-// energy reductions stay FP64. Below the threshold the block is widened to FP64 and the
-// remaining iterations are the plain FP64 path.
+// energy reductions stay FP64. Below the threshold (or once the FP32 error stalls) the block
+// is widened to FP64 and the remaining iterations are either the plain FP64 path or, with
+// graded_tail, an FP32 filter whose last degrees run in FP64 followed by an FP64
+// Rayleigh-Ritz step (chebyshev_graded).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -492,6 +494,11 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         set_error("sgpu_scf: precision must be SGPU_PREC_FP64 or SGPU_PREC_FP32");
         return SGPU_ERR_ARG;
     }
+    if (prm->graded_tail &&
+        (prm->tail_fp64_degrees < 0 || prm->tail_fp64_degrees >= prm->cheb_degree)) {
+        set_error("sgpu_scf: tail_fp64_degrees must lie in [0, cheb_degree)");
+        return SGPU_ERR_ARG;
+    }
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = ctx->stream;
     const long N = ctx->Nd;
@@ -554,6 +561,10 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
     double eigmin = 0.0, eigmax = 0.0, efermi = 0.0, error = prm->tol_scf + 1.0;
     double Etot = 0, Eband = 0, E1 = 0, E2 = 0, E3 = 0, Exc = 0, Entropy = 0;
     int scf = 0, switch_iter = mixed ? -1 : 0;
+    // after the switch: plain FP64, or the graded filter with FP64 Rayleigh-Ritz
+    bool graded = false;
+    double best_error = 1e300;
+    int stall = 0;
     double filter_ms = 0.0;
     const int m = prm->cheb_degree;
     while (scf < prm->maxit_scf) {
@@ -583,6 +594,11 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 // HY into X (the reference reuses Xorb for HY), then project in FP32 products
                 SGPU_TRY(hamiltonian_dev<float>(ctx, 0, Ns, 0.0, Y32, N, X32, N, 1.0, 0.0, nullptr, 0, st));
                 SGPU_TRY(project_f32(ctx, Ns, Y32, N, X32, N, d_Hp, d_Mp, st));
+            } else if (graded) {
+                SGPU_TRY(chebyshev_graded(ctx, 0, X32, Y32, X64, Y64, Ns, m,
+                                          prm->tail_fp64_degrees, cutoff, eigmax, eigmin, st));
+                SGPU_TRY(hamiltonian_dev<double>(ctx, 0, Ns, 0.0, Y64, N, X64, N, 1.0, 0.0, nullptr, 0, st));
+                SGPU_TRY(project_f64(ctx, Ns, Y64, N, X64, N, d_Hp, d_Mp, st));
             } else {
                 SGPU_TRY(chebyshev_dev<double>(ctx, 0, X64, N, Y64, N, Ns, m, cutoff, eigmax, eigmin, st));
                 SGPU_TRY(hamiltonian_dev<double>(ctx, 0, Ns, 0.0, Y64, N, X64, N, 1.0, 0.0, nullptr, 0, st));
@@ -593,10 +609,13 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
             float ms = 0.f;
             SGPU_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
             filter_ms += ms;
-            if (mixed)
+            if (mixed) {
                 SGPU_TRY(rotate_f32(ctx, Ns, Y32, N, d_Hp, X32, N, st));
-            else
+            } else {
                 SGPU_TRY(rotate_f64(ctx, Ns, Y64, N, d_Hp, X64, N, st));
+                // the graded filter starts from an FP32 copy of the rotated orbitals
+                if (graded) SGPU_TRY(convert_cols<double, float>(X64, nb, X32, nb, nb, 1, st));
+            }
             SGPU_CUDA_TRY(cudaMemcpyAsync(lam.data(), d_lam, sizeof(double) * Ns,
                                           cudaMemcpyDeviceToHost, st));
             SGPU_CUDA_TRY(cudaStreamSynchronize(st));
@@ -662,14 +681,23 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         scf++;
         if (prm->verbose)
             printf("sgpu_scf: iter %3d  Etot/atom %.10f  error %.3e  %s\n", scf,
-                   Etot / std::max(1, prm->n_atom), error, mixed ? "fp32" : "fp64");
+                   Etot / std::max(1, prm->n_atom), error,
+                   mixed ? "fp32" : (graded ? "graded" : "fp64"));
         if (error < prm->tol_scf && scf >= prm->minit_scf) break;
-        if (mixed && error < prm->fp64_switch_error) {
-            // widen the orbital block and continue in FP64
-            SGPU_TRY(convert_cols<float, double>(X32, nb, X64, nb, nb, 1, st));
-            ctx->launches++;
-            mixed = false;
-            switch_iter = scf;
+        if (mixed) {
+            // leave FP32 below the threshold, or once the FP32 error has stopped falling
+            // (two iterations in a row without a 20 % gain on the best so far): the FP32
+            // Rayleigh-Ritz step sets a floor on the error that depends on the system
+            stall = (scf >= 4 && error > 0.8 * best_error) ? stall + 1 : 0;
+            best_error = std::min(best_error, error);
+            if (error < prm->fp64_switch_error || stall >= 2) {
+                // widen the orbital block and continue in FP64 (or graded)
+                SGPU_TRY(convert_cols<float, double>(X32, nb, X64, nb, nb, 1, st));
+                ctx->launches++;
+                mixed = false;
+                graded = prm->graded_tail != 0;
+                switch_iter = scf;
+            }
         }
     }
     if (rho_out) SGPU_CUDA_TRY(cudaMemcpyAsync(rho_out, d_rho, sizeof(double) * N, cudaMemcpyDefault, st));

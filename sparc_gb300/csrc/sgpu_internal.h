@@ -195,6 +195,10 @@ int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, lon
 template <typename T>
 int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int ncol, int m,
                   double a, double b, double a0, cudaStream_t st);
+// first m-k64 degrees in FP32 on (X32, Y32), last k64 in FP64; result in Y64 (ld = Nd)
+int chebyshev_graded(sgpu_ctx *ctx, int spin, float *X32, float *Y32, double *X64,
+                     double *Y64, int ncol, int m, int k64, double a, double b, double a0,
+                     cudaStream_t st);
 
 // ---- Rayleigh-Ritz (subspace.cu)
 int project_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *HY,

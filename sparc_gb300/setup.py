@@ -68,7 +68,8 @@ class CellSystem:
         self.nlcc = any(float(t["fchrg"]) > 1e-12 for t in self.tables)
 
     def scf_params(self, Nstates, cheb_degree, smearing=1e-3, precision=SGPU_PREC_FP64,
-                   fp64_switch_error=1e-4, seed=1, verbose=0, maxit_scf=100):
+                   fp64_switch_error=1e-4, graded_tail=0, tail_fp64_degrees=0, seed=1,
+                   verbose=0, maxit_scf=100):
         """sgpu_scf_params with the reference's defaults for this cell (Fermi-Dirac smearing
         in Ha, density mixing with Kerker preconditioning, Pulay history 7)."""
         h_eff = float(self.h[0]) if np.ptp(self.h) < 1e-12 else \
@@ -101,6 +102,8 @@ class CellSystem:
         p.Esc = self.fields["Esc"]
         p.precision = precision
         p.fp64_switch_error = fp64_switch_error
+        p.graded_tail = int(graded_tail)
+        p.tail_fp64_degrees = int(tail_fp64_degrees)
         p.seed = seed
         p.verbose = verbose
         return p
