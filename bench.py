@@ -13,6 +13,10 @@ and writes Y, each later one reads Y and X and writes the new iterate).
   e2e    : the drop-in call with FP64 host arrays (sgpu_ChebyshevFiltering, precision FP32),
            host<->device copies of X in and X, Y out inside the timed region
   fp64   : the plain FP64 filter on device-resident blocks (the FP64 drop-in)
+  scf    : SCF time-to-solution, Si8 (26^3, 32 states) from the reference's set-up fields
+  scf_c4 : SCF time-to-solution, Si216 (77^3, 520 states, degree 24) set up on the device from
+           the psp8 tables: plain FP64 CheFSI vs the mixed-precision mode, with energy and
+           eigenvalue differences against the FP64 run and the reference program's run
 
 usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -50,7 +54,8 @@ def parse():
                     help="columns in the bounded CPU-baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution block")
+    ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution blocks")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 216-atom SCF block")
     return ap.parse_args()
 
 
@@ -175,6 +180,64 @@ def scf_block(sg, device=0, repeats=2):
     return out
 
 
+def scf_c4_block(sg, device=0):
+    """SCF time-to-solution on the 216-atom Si cell (3x3x3 diamond cells, a = 30.78 Bohr,
+    77^3 grid, 520 states, degree 24, LDA, TOL_SCF 1e-6), set up on the device from the Si
+    psp8 tables (sparc_gb300.setup): plain FP64 CheFSI against the mixed-precision mode (FP32
+    filter and BF16x9 products while the SCF error falls, then the FP32 filter with an FP64
+    Rayleigh-Ritz step). Energies and eigenvalues against the reference program's run of the
+    same input where that run is committed (tests/golden/Si216_c4_scf_ref.json)."""
+    golden = os.path.join(ROOT, "tests", "golden")
+    sys.path.insert(0, golden)
+    import systems
+    from sparc_gb300.psp8 import load_tables
+    from sparc_gb300.setup import CellSystem, grid_from_mesh
+    sysd = systems.si216_c4()
+    N = grid_from_mesh(sysd["L"], float(sysd["keys"]["MESH_SPACING"]))
+    t0 = time.perf_counter()
+    cs = CellSystem(sysd["L"], N, sysd["species"],
+                    {"Si": load_tables(os.path.join(golden, "psp_Si.npz"))}, device=device)
+    setup_s = time.perf_counter() - t0
+    ref = None
+    rpath = os.path.join(golden, "Si216_c4_scf_ref.json")
+    if os.path.exists(rpath):
+        with open(rpath) as f:
+            ref = json.load(f)
+    out = {"system": "Si216: 3x3x3 diamond Si, a=30.78 Bohr, sigma 0.1 Bohr displacements, "
+                     "77^3 grid h=0.40, 520 states, LDA_PW, degree 24, TOL_SCF 1e-6",
+           "setup_s": round(setup_s, 3)}
+    if ref:
+        out["reference"] = {"Etot_per_atom": ref["Etot_per_atom"], "scf_iters": ref["scf_iters"],
+                            "walltime_s": ref.get("walltime_s"),
+                            "where": ref.get("where", "reference program, x86 build host")}
+    runs = {"fp64": dict(precision=64),
+            "mixed": dict(precision=32, fp64_switch_error=1e-4, graded_tail=1,
+                          tail_fp64_degrees=0)}
+    e64 = None
+    for name, kw in runs.items():
+        prm = cs.scf_params(Nstates=520, cheb_degree=24, **kw)
+        res, rho, lam, occ = cs.scf(prm)
+        e = res["Etot"] / cs.n_atom
+        rec = {"time_s": round(res["time_s"], 3), "scf_iters": res["scf_iters"],
+               "converged": bool(res["converged"]), "Etot_per_atom": e,
+               "fp64_switch_iter": res["fp64_switch_iter"]}
+        if name == "fp64":
+            e64, lam64 = e, lam
+        else:
+            rec["dE_per_atom_vs_fp64_gpu"] = abs(e - e64)
+            occd = occ > 1e-3
+            rec["max_occ_eig_diff_vs_fp64_gpu"] = float(np.abs(lam[occd] - lam64[occd]).max())
+        if ref:
+            rec["dE_per_atom_vs_ref"] = abs(e - ref["Etot_per_atom"])
+            lr, orr = np.array(ref["lambda"]), np.array(ref["occ"])
+            occd = orr > 1e-3
+            rec["max_occ_eig_err_vs_ref"] = float(np.abs(lam[occd] - lr[occd]).max())
+        out[name] = rec
+    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["time_s"] / out["mixed"]["time_s"], 3)
+    cs.close()
+    return out
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -226,6 +289,10 @@ def main():
     ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
                      nl["grid_pos"], nl["chi"])
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    # pick the FP32 stencil variant for this grid (all variants give identical results)
+    variant, variant_ms = ctx.autotune(ncol=min(ncol, 64))
+    kernel_name = ["k_stencil_f32x2<32x16>", "k_stencil_f32_b22<32x16>",
+                   "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>"][variant]
 
     gen = torch.Generator(device=dev)
     gen.manual_seed(1234 + rank)
@@ -339,9 +406,11 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(wl, args.cpu_cols)
-    scf = None
+    scf = scf_c4 = None
     if rank == 0 and not args.no_scf:
         scf = scf_block(sg, device=local)
+        if not args.no_c4:
+            scf_c4 = scf_c4_block(sg, device=local)
 
     if rank == 0:
         line = {
@@ -351,8 +420,10 @@ def main():
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (1.8 GB FP32 block), no flush",
-                       "step": "X reset copy + degree-20 filter over 512 vectors"},
-            "roofline": {"bound": "hbm", "kernel": "k_stencil_orth<float>",
+                       "step": "X reset copy + degree-20 filter over 512 vectors",
+                       "stencil_variant": {"chosen": kernel_name,
+                                           "autotune_ms": [round(float(v), 4) for v in variant_ms]}},
+            "roofline": {"bound": "hbm", "kernel": kernel_name,
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_src,
                          "traffic": traffic,
@@ -368,6 +439,7 @@ def main():
                     "api": "sgpu_ChebyshevFiltering(host FP64 arrays, SGPU_PREC_FP32)"},
             "fp64": fp64,
             "scf": scf,
+            "scf_c4": scf_c4,
             "cpu_baseline": cpu,
             "clocks": ck,
         }

@@ -326,6 +326,18 @@ int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms);
  * a caller can order its own work or record timing events against it. */
 int sgpu_get_stream(sgpu_ctx *ctx, void **stream);
 
+/* ------------------------------------------------------------------- kernel tuning */
+
+/* Time every FP32 stencil kernel variant (tile shape and register blocking) on ncol scratch
+ * columns of this context's grid, keep the fastest for later calls, and return its index in
+ * *variant and per-variant milliseconds in ms (4 values; may be NULL). All variants give
+ * identical results. sgpu_scf runs this once per context before its first FP32 filter.
+ * No counterpart in the reference. */
+int sgpu_autotune(sgpu_ctx *ctx, int ncol, int *variant, double *ms);
+
+/* Fix the FP32 stencil variant (0..3) without timing. */
+int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
+
 /* ------------------------------------------------------------------- measurement */
 
 /* kernel kinds reported by sgpu_profile_read */

@@ -30,7 +30,7 @@ EXPORTED = [
     "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
     "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
     "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
-    "sgpu_CalculateNonlocalProjectors",
+    "sgpu_CalculateNonlocalProjectors", "sgpu_autotune", "sgpu_set_stencil_variant",
 ]
 
 
@@ -388,6 +388,16 @@ class Context:
         _check(lib().sgpu_scf(self._h, ctypes.byref(params), _ptr(b), _ptr(r0), _ptr(rc_),
                               _ptr(rho), _ptr(lam), _ptr(occ), ctypes.byref(res)))
         return res.as_dict(), rho, lam, occ
+
+    def autotune(self, ncol=64):
+        """Time the FP32 stencil variants; returns (chosen variant, per-variant ms)."""
+        v = ctypes.c_int()
+        ms = np.zeros(4)
+        _check(lib().sgpu_autotune(self._h, int(ncol), ctypes.byref(v), _ptr(ms)))
+        return int(v.value), ms
+
+    def set_stencil_variant(self, variant):
+        _check(lib().sgpu_set_stencil_variant(self._h, int(variant)))
 
     def profile_enable(self, on=True):
         _check(lib().sgpu_profile_enable(self._h, int(bool(on))))

@@ -129,6 +129,8 @@ struct sgpu_ctx {
     sgpu::MixState *mix = nullptr;
     sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)
     sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
+    int stencil_variant = 0;   // FP32 stencil kernel variant (autotune.cu)
+    bool stencil_tuned = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on

@@ -278,6 +278,228 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
 #undef SGPU_F2_STEP
 }
 
+// ---------------------------------------------------------------------------------------------
+// FP32 kernel with 2x2 register blocking: each thread owns points (i0, i0+1) x (j0, j0+1), so
+// one column of 14 shared-memory pairs serves the y-neighbours of both rows and the z-queue
+// holds two pairs per plane. Halo values reach shared memory by cp.async (no staging
+// registers), one plane ahead, into the buffer the previous plane has finished with. VEC
+// selects 8-byte global accesses (even Nx, even leading dimensions, 8-byte aligned bases);
+// without it every access is a 4-byte one. Per point the arithmetic is the same sequence of
+// IEEE operations as k_stencil_f32x2, so the two kernels give identical results.
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+template <bool VEC>
+__device__ __forceinline__ float2 ld_pair(const float *__restrict__ base, int o0, int o1)
+{
+    if constexpr (VEC)
+        return __ldg(reinterpret_cast<const float2 *>(base + o0));
+    else
+        return make_float2(__ldg(base + o0), __ldg(base + o1));
+}
+
+template <int R, int BX, int BY, int MINB, bool VEC>
+__global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
+    k_stencil_f32_b22(const StencilParams<float> p)
+{
+    constexpr int Q = 2 * R + 1;
+    constexpr int W = BX + 2 * R;
+    static_assert(Q == 13 && R % 2 == 0, "the unrolled z-loop below is written for radius 6");
+    __shared__ __align__(16) float s[2][BY + 2 * R][W];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+    const int col = blockIdx.z / p.nslab;
+    const int slab = blockIdx.z - col * p.nslab;
+    const int zs = slab * p.zlen;
+    const int ze = min(zs + p.zlen, p.Nz);
+    if (zs >= ze) return;
+
+    const int i0 = x0 + 2 * tx, j0 = y0 + 2 * ty;
+    const bool in0 = i0 < p.Nx, in1 = i0 + 1 < p.Nx;
+    const bool r0ok = j0 < p.Ny, r1ok = j0 + 1 < p.Ny;
+    const int gx0 = wrapi(i0, p.Nx), gx1 = wrapi(i0 + 1, p.Nx);
+    const int row0 = wrapi(j0, p.Ny) * p.Nx, row1 = wrapi(j0 + 1, p.Ny) * p.Nx;
+    const int NxNy = p.Nx * p.Ny;
+    const float *__restrict__ xc = p.x + (long)col * p.ldx;
+    const float *__restrict__ zc = p.z ? p.z + (long)col * p.ldz : nullptr;
+    float *__restrict__ oc = p.out + (long)col * p.ldo;
+
+    // halo sources (offsets within a plane) and shared-memory slots
+    const bool hx = tx < R / 2, hy = ty < R / 2;
+    int hxo[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};  // (left, right) x (row 0, row 1)
+    int hyo[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};  // top rows 0,1 then bottom rows 0,1
+    if (hx) {
+        const int lx = x0 - R + 2 * tx, rx = x0 + BX + 2 * tx;
+        const int rows[2] = {row0, row1};
+        for (int r = 0; r < 2; r++) {
+            hxo[r][0] = wrapi(lx, p.Nx) + rows[r];
+            hxo[r][1] = wrapi(lx + 1, p.Nx) + rows[r];
+            hxo[2 + r][0] = wrapi(rx, p.Nx) + rows[r];
+            hxo[2 + r][1] = wrapi(rx + 1, p.Nx) + rows[r];
+        }
+    }
+    if (hy) {
+        const int ty0 = y0 - R + 2 * ty, by0 = y0 + BY + 2 * ty;
+        const int rr[4] = {wrapi(ty0, p.Ny) * p.Nx, wrapi(ty0 + 1, p.Ny) * p.Nx,
+                           wrapi(by0, p.Ny) * p.Nx, wrapi(by0 + 1, p.Ny) * p.Nx};
+        for (int r = 0; r < 4; r++) {
+            hyo[r][0] = gx0 + rr[r];
+            hyo[r][1] = gx1 + rr[r];
+        }
+    }
+    auto issue_halo = [&](int k, int b) {
+        const float *pl = xc + k * NxNy;
+        if (hx) {
+            for (int r = 0; r < 2; r++) {
+                float *dl = &s[b][2 * ty + R + r][2 * tx];
+                float *dr = &s[b][2 * ty + R + r][R + BX + 2 * tx];
+                if constexpr (VEC) {
+                    cp_async8(dl, pl + hxo[r][0]);
+                    cp_async8(dr, pl + hxo[2 + r][0]);
+                } else {
+                    cp_async4(dl, pl + hxo[r][0]); cp_async4(dl + 1, pl + hxo[r][1]);
+                    cp_async4(dr, pl + hxo[2 + r][0]); cp_async4(dr + 1, pl + hxo[2 + r][1]);
+                }
+            }
+        }
+        if (hy) {
+            const int srow[4] = {2 * ty, 2 * ty + 1, BY + R + 2 * ty, BY + R + 2 * ty + 1};
+            for (int r = 0; r < 4; r++) {
+                float *d = &s[b][srow[r]][R + 2 * tx];
+                if constexpr (VEC) {
+                    cp_async8(d, pl + hyo[r][0]);
+                } else {
+                    cp_async4(d, pl + hyo[r][0]); cp_async4(d + 1, pl + hyo[r][1]);
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    float2 qa[Q], qb[Q];  // z-queues of rows j0 and j0+1: slot of plane k-R+m is (U+m) % Q
+#pragma unroll
+    for (int m = 0; m < 2 * R; m++) {
+        const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
+        qa[m] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);
+        qb[m] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);
+    }
+    float2 va = make_float2(0.f, 0.f), vb = va, za = va, zb = va;
+    {
+        const int pk = zs * NxNy;
+        if (p.v) {
+            va = ld_pair<VEC>(p.v, pk + gx0 + row0, pk + gx1 + row0);
+            vb = ld_pair<VEC>(p.v, pk + gx0 + row1, pk + gx1 + row1);
+        }
+        if (zc) {
+            za = ld_pair<VEC>(zc, pk + gx0 + row0, pk + gx1 + row0);
+            zb = ld_pair<VEC>(zc, pk + gx0 + row1, pk + gx1 + row1);
+        }
+    }
+    issue_halo(zs, zs & 1);
+
+#define SGPU_B22_STEP(U)                                                                         \
+    {                                                                                            \
+        const int k = kb + (U);                                                                  \
+        if (k < ze) {                                                                            \
+            const int b = k & 1;                                                                 \
+            {                                                                                    \
+                const int pl = wrapi(k + R, p.Nz) * NxNy;                                        \
+                qa[((U) + 2 * R) % Q] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);      \
+                qb[((U) + 2 * R) % Q] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);      \
+            }                                                                                    \
+            const float2 ca = qa[((U) + R) % Q], cb = qb[((U) + R) % Q];                         \
+            *reinterpret_cast<float2 *>(&s[b][2 * ty + R][R + 2 * tx]) = ca;                     \
+            *reinterpret_cast<float2 *>(&s[b][2 * ty + R + 1][R + 2 * tx]) = cb;                 \
+            const float2 vca = va, vcb = vb, zca = za, zcb = zb;                                 \
+            cp_async_wait_all();                                                                 \
+            __syncthreads();                                                                     \
+            if (k + 1 < ze) {                                                                    \
+                issue_halo(k + 1, b ^ 1);                                                        \
+                const int pn = (k + 1) * NxNy;                                                   \
+                if (p.v) {                                                                       \
+                    va = ld_pair<VEC>(p.v, pn + gx0 + row0, pn + gx1 + row0);                    \
+                    vb = ld_pair<VEC>(p.v, pn + gx0 + row1, pn + gx1 + row1);                    \
+                }                                                                                \
+                if (zc) {                                                                        \
+                    za = ld_pair<VEC>(zc, pn + gx0 + row0, pn + gx1 + row0);                     \
+                    zb = ld_pair<VEC>(zc, pn + gx0 + row1, pn + gx1 + row1);                     \
+                }                                                                                \
+            }                                                                                    \
+            float2 yv[2 * R + 2];                                                                \
+            _Pragma("unroll") for (int t = 0; t < 2 * R + 2; t++)                                \
+                yv[t] = *reinterpret_cast<const float2 *>(&s[b][2 * ty + t][R + 2 * tx]);        \
+            _Pragma("unroll") for (int rr = 0; rr < 2; rr++) {                                   \
+                const float2 cen = rr ? cb : ca;                                                 \
+                const float *srow = &s[b][2 * ty + R + rr][2 * tx];                              \
+                float2 L[R + 1];                                                                 \
+                _Pragma("unroll") for (int m = 0; m <= R; m++)                                   \
+                    L[m] = *reinterpret_cast<const float2 *>(srow + 2 * m);                      \
+                float ax0 = p.c0 * cen.x, ax1 = p.c0 * cen.y;                                    \
+                float ay0 = 0.f, ay1 = 0.f, az0 = 0.f, az1 = 0.f;                                \
+                _Pragma("unroll") for (int r = 1; r <= R; r++) {                                 \
+                    float2 lo, hi;                                                               \
+                    if (r % 2 == 0) {                                                            \
+                        lo = L[(R - r) / 2];                                                     \
+                        hi = L[(R + r) / 2];                                                     \
+                    } else {                                                                     \
+                        lo = make_float2(L[(R - r) / 2].y, L[(R - r + 1) / 2].x);                \
+                        hi = make_float2(L[(R + r) / 2].y, L[(R + r + 1) / 2].x);                \
+                    }                                                                            \
+                    const float2 xs = __fadd2_rn(lo, hi);                                        \
+                    const float2 ys = __fadd2_rn(yv[R + rr - r], yv[R + rr + r]);                \
+                    const float2 zsum = rr ? __fadd2_rn(qb[((U) + R - r) % Q], qb[((U) + R + r) % Q]) \
+                                           : __fadd2_rn(qa[((U) + R - r) % Q], qa[((U) + R + r) % Q]); \
+                    ax0 = fmaf(xs.x, p.wx[r], ax0); ax1 = fmaf(xs.y, p.wx[r], ax1);              \
+                    ay0 = fmaf(ys.x, p.wy[r], ay0); ay1 = fmaf(ys.y, p.wy[r], ay1);              \
+                    az0 = fmaf(zsum.x, p.wz[r], az0); az1 = fmaf(zsum.y, p.wz[r], az1);          \
+                }                                                                                \
+                float o0 = ax0 + (ay0 + az0), o1 = ax1 + (ay1 + az1);                            \
+                if (p.v) {                                                                       \
+                    const float2 vcur = rr ? vcb : vca;                                          \
+                    o0 = fmaf(p.bv, vcur.x * cen.x, o0);                                         \
+                    o1 = fmaf(p.bv, vcur.y * cen.y, o1);                                         \
+                }                                                                                \
+                o0 *= p.s1;                                                                      \
+                o1 *= p.s1;                                                                      \
+                if (zc) {                                                                        \
+                    const float2 zcur = rr ? zcb : zca;                                          \
+                    o0 = fmaf(p.s2, zcur.x, o0);                                                 \
+                    o1 = fmaf(p.s2, zcur.y, o1);                                                 \
+                }                                                                                \
+                const bool rok = rr ? r1ok : r0ok;                                               \
+                const int orow = (rr ? row1 : row0) + k * NxNy;                                  \
+                if (VEC && rok && in1) {                                                         \
+                    *reinterpret_cast<float2 *>(oc + orow + gx0) = make_float2(o0, o1);          \
+                } else if (rok) {                                                                \
+                    if (in0) oc[orow + gx0] = o0;                                                \
+                    if (in1) oc[orow + gx1] = o1;                                                \
+                }                                                                                \
+            }                                                                                    \
+        }                                                                                        \
+    }
+
+    for (int kb = zs; kb < ze; kb += Q) {
+        SGPU_B22_STEP(0) SGPU_B22_STEP(1) SGPU_B22_STEP(2) SGPU_B22_STEP(3) SGPU_B22_STEP(4)
+        SGPU_B22_STEP(5) SGPU_B22_STEP(6) SGPU_B22_STEP(7) SGPU_B22_STEP(8) SGPU_B22_STEP(9)
+        SGPU_B22_STEP(10) SGPU_B22_STEP(11) SGPU_B22_STEP(12)
+    }
+#undef SGPU_B22_STEP
+    cp_async_wait_all();
+}
+
 }  // namespace
 
 template <typename T>
@@ -316,14 +538,24 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     if (!z || s2 == 0.0) p.z = nullptr;
 
     const bool f32 = sizeof(T) == 4;
-    const int tilesx = f32 ? (ctx->Nx + BXP - 1) / BXP : (ctx->Nx + BX - 1) / BX;
-    const int tilesy = f32 ? (ctx->Ny + BYP - 1) / BYP : (ctx->Ny + BY - 1) / BY;
+    // FP32 variants (see stencil_variant_count): 0 paired 32x16, 1 2x2-blocked 32x16,
+    // 2 2x2-blocked 64x8, 3 paired 64x8
+    const int variant = f32 ? ctx->stencil_variant : 0;
+    const int tbx = f32 ? (variant >= 2 ? 64 : BXP) : BX;
+    const int tby = f32 ? (variant >= 2 ? 8 : BYP) : BY;
+    const int tilesx = (ctx->Nx + tbx - 1) / tbx;
+    const int tilesy = (ctx->Ny + tby - 1) / tby;
     // split z into slabs until there are enough blocks to fill 152 SMs several times over
     long blocks1 = (long)tilesx * tilesy * ncol;
     int nslab = 1;
     while (blocks1 * nslab < 152L * 8 && ctx->Nz / (nslab * 2) >= 8) nslab *= 2;
     p.zlen = (ctx->Nz + nslab - 1) / nslab;
     p.nslab = nslab;
+    // FP32 variant (chosen by sgpu_autotune or sgpu_set_stencil_variant); the 2x2 kernel uses
+    // 8-byte global accesses when every base is 8-byte aligned and every stride is even
+    auto al8 = [](const void *ptr) { return ((uintptr_t)ptr & 7u) == 0; };
+    const bool vec = (ctx->Nx % 2 == 0) && al8(x) && al8(out) && ldx % 2 == 0 && ldo % 2 == 0 &&
+                     (!p.z || (al8(z) && ldz % 2 == 0)) && (!p.v || al8(v));
     const int maxz = 65535 / nslab;
     for (int c0i = 0; c0i < ncol; c0i += maxz) {
         int nc = ncol - c0i < maxz ? ncol - c0i : maxz;
@@ -333,10 +565,29 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
         if (q.z) q.z = z + (long)c0i * ldz;
         dim3 grid(tilesx, tilesy, nc * nslab);
         ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
-        if constexpr (sizeof(T) == 4)
-            k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);
-        else
+        if constexpr (sizeof(T) == 4) {
+            switch (variant) {
+            case 1:
+                if (vec)
+                    k_stencil_f32_b22<R, 32, 16, 4, true><<<grid, dim3(16, 8), 0, st>>>(q);
+                else
+                    k_stencil_f32_b22<R, 32, 16, 3, false><<<grid, dim3(16, 8), 0, st>>>(q);
+                break;
+            case 2:
+                if (vec)
+                    k_stencil_f32_b22<R, 64, 8, 4, true><<<grid, dim3(32, 4), 0, st>>>(q);
+                else
+                    k_stencil_f32_b22<R, 64, 8, 3, false><<<grid, dim3(32, 4), 0, st>>>(q);
+                break;
+            case 3:
+                k_stencil_f32x2<R, 64, 8, 3><<<grid, dim3(32, 8), 0, st>>>(q);
+                break;
+            default:
+                k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);
+            }
+        } else {
             k_stencil_orth<T, R, BX, BY><<<grid, dim3(BX, BY), 0, st>>>(q);
+        }
     }
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;

@@ -120,6 +120,27 @@ def test_fp32_hamiltonian_and_filter_tolerance(gpu_available):
     assert rel_err(X, Xo) < TOL32_FILTER
 
 
+@pytest.mark.parametrize("shape", [(48, 40, 36), (45, 19, 30)])
+def test_fp32_stencil_variants_identical(gpu_available, shape):
+    """Every FP32 stencil variant (tiles, 2x2 register blocking, 8-byte or 4-byte accesses)
+    gives bit-identical filter output; the autotuner picks one of them."""
+    grid, nl, veff, rng = _random_case(shape, seed=11, natom=4)
+    Nd = shape[0] * shape[1] * shape[2]
+    ctx = make_ctx(grid, nl, veff)
+    x = rng.uniform(-1, 1, (3, Nd)).astype(np.float32)
+    outs = []
+    for v in range(4):
+        ctx.set_stencil_variant(v)
+        X = x.copy(); Y = np.zeros_like(x)
+        ctx.ChebyshevFiltering_f32(X, Y, 7, 0.5, 50.0, -1.0)
+        outs.append((X, Y))
+    for X, Y in outs[1:]:
+        np.testing.assert_array_equal(Y, outs[0][1])
+        np.testing.assert_array_equal(X, outs[0][0])
+    best, ms = ctx.autotune(ncol=3)
+    assert 0 <= best < 4 and np.all(ms > 0)
+
+
 def test_device_pointers_match_host(gpu_available):
     import torch
     grid, nl, veff, rng = _random_case((24, 20, 16), seed=9)
