@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution blocks")
     ap.add_argument("--no-c4", action="store_true", help="skip the 216-atom SCF block")
+    ap.add_argument("--no-c3", action="store_true", help="skip the batched k-point/spin block")
     return ap.parse_args()
 
 
@@ -238,6 +239,95 @@ def scf_c4_block(sg, device=0):
     return out
 
 
+def al32_system():
+    """32-atom FCC Al (2x2x2 conventional cells, a = 7.65 Bohr, L = 15.3 Bohr), seeded
+    N(0, 0.05^2) Bohr displacements."""
+    rng = np.random.default_rng(20261205)
+    fcc = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
+    a = 7.65
+    pos = np.concatenate([(fcc + np.array([i, j, k])) * a for i in range(2) for j in range(2)
+                          for k in range(2)], axis=0)
+    return 2 * a, pos + rng.normal(0.0, 0.05, size=pos.shape)
+
+
+def batched_c3_block(sg, torch, dev, device=0, steps=3):
+    """Batched complex filter over (k-point, spin) blocks: 32-atom Al, 34^3 grid (h = 0.45),
+    the 10 symmetry-distinct points of a 4x4x4 k-grid times 2 spins = 20 blocks of 64 states,
+    degree 18, projectors and local potential from the device set-up (Al psp8 tables; the two
+    spin potentials are the initial potential shifted by +-0.02 Ha, a stand-in for the spin
+    splitting). Times one batched call (all blocks, one CUDA graph) against one k-point filter
+    call per block, in complex128 and complex64."""
+    golden = os.path.join(ROOT, "tests", "golden")
+    from sparc_gb300.psp8 import load_tables
+    from sparc_gb300.setup import CellSystem
+    from sparc_gb300.synthetic import filter_bytes
+    L, pos = al32_system()
+    N = (34, 34, 34)
+    cs = CellSystem((L, L, L), N, [("Al", pos)],
+                    {"Al": load_tables(os.path.join(golden, "psp_Al.npz"))}, device=device)
+    ctx = cs.ctx
+    Nd = N[0] * N[1] * N[2]
+    f = cs.fields
+    phi = np.zeros(Nd)
+    ctx.Calculate_elecstPotential(f["rho_at"], f["b"], phi, 1e-8)
+    vxc, exc = np.zeros(Nd), np.zeros(Nd)
+    ctx.Calculate_Vxc_LDA_PW(f["rho_at"], f["rho_core"], 1e-14, vxc, exc)
+    v0 = phi + vxc
+    ctx.set_veff(np.concatenate([v0 + 0.02, v0 - 0.02]), nspin=2)
+    kred = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (1, 1, 0), (2, 1, 0), (2, 2, 0), (1, 1, 1),
+            (2, 1, 1), (2, 2, 1), (2, 2, 2)]  # in units of (2 pi / L) / 4
+    ncol, m = 64, 18
+    a0, a, b = -0.6, 0.35, 45.0
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(77)
+    out = {"system": "Al32 FCC 2x2x2 (L=15.3 Bohr), 34^3 grid, 10 k x 2 spins = 20 blocks "
+                     "of 64 states, degree 18", "blocks": 20}
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    for name, prec, cdt in (("complex128", 64, torch.complex128), ("complex64", 32, torch.complex64)):
+        blocks = []
+        for kk in kred:
+            for spin in (0, 1):
+                x = torch.complex(torch.rand((ncol, Nd), generator=gen, device=dev, dtype=torch.float64),
+                                  torch.rand((ncol, Nd), generator=gen, device=dev, dtype=torch.float64)).to(cdt)
+                blocks.append(dict(spin=spin, k=[2 * np.pi / L * q / 4 for q in kk], X=x,
+                                   Y=torch.empty_like(x), X0=x.clone(), a=a, b=b, a0=a0))
+
+        def reset():
+            with torch.cuda.stream(stream):
+                for bl in blocks:
+                    bl["X"].copy_(bl["X0"])
+
+        def batched():
+            reset()
+            ctx.ChebyshevFiltering_batched(blocks, m, precision=prec)
+
+        def per_block():  # one sgpu_ChebyshevFiltering_kpt call per block (complex128 only)
+            reset()
+            for bl in blocks:
+                ctx.ChebyshevFiltering_kpt(bl["k"], bl["X"], bl["Y"], m, a, b, a0,
+                                           spin=bl["spin"], precision=prec)
+
+        res = {}
+        runs = [("batched_graph", batched)] + ([("per_block_calls", per_block)] if prec == 64 else [])
+        for tag, fn in runs:
+            fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                fn()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / steps
+            gbs = 20 * filter_bytes(Nd, ncol, m, 16 if prec == 64 else 8) / dt / 1e9
+            res[tag] = {"ms": round(dt * 1e3, 3), "GBs": round(gbs, 1)}
+        if "per_block_calls" in res:
+            res["speedup_batched"] = round(res["per_block_calls"]["ms"] /
+                                           res["batched_graph"]["ms"], 3)
+        out[name] = res
+        del blocks
+    cs.close()
+    return out
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -411,6 +501,9 @@ def main():
         scf = scf_block(sg, device=local)
         if not args.no_c4:
             scf_c4 = scf_c4_block(sg, device=local)
+    c3 = None
+    if rank == 0 and not args.no_c3:
+        c3 = batched_c3_block(sg, torch, dev, device=local)
 
     if rank == 0:
         line = {
@@ -440,6 +533,7 @@ def main():
             "fp64": fp64,
             "scf": scf,
             "scf_c4": scf_c4,
+            "batched_c3": c3,
             "cpu_baseline": cpu,
             "clocks": ck,
         }

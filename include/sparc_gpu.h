@@ -54,6 +54,12 @@ int sgpu_create(sgpu_ctx **ctx, int device, int Nx, int Ny, int Nz, int FDn,
                 const double *D2_stencil_coeffs_z, double dV);
 int sgpu_destroy(sgpu_ctx *ctx);
 
+/* Replace the FD weights and dV of a context whose cell lengths changed at a fixed grid (a
+ * strained geometry): the same data sgpu_create takes. */
+int sgpu_set_grid_coeffs(sgpu_ctx *ctx, const double *D2_stencil_coeffs_x,
+                         const double *D2_stencil_coeffs_y, const double *D2_stencil_coeffs_z,
+                         double dV);
+
 /* Local effective potential, nspin contiguous blocks of Nd values
  * (pSPARC->Veff_loc_dmcomm, src/include/isddft.h:540). */
 int sgpu_set_veff(sgpu_ctx *ctx, int nspin, const double *Veff_loc);
@@ -225,6 +231,29 @@ int sgpu_Mixing_periodic_pulay(sgpu_ctx *ctx, int iter_count, double *rho);
 int sgpu_Evaluate_scf_error(sgpu_ctx *ctx, const double *rho_out, const double *rho_in,
                             double *error);
 
+/* One (k-point, spin, band-block) unit of a batched filter call. X and Y are device arrays of
+ * complex values (re, im interleaved), complex128 for SGPU_PREC_FP64 and complex64 (float
+ * pairs) for SGPU_PREC_FP32, Nd x ncol column-major with leading dimensions ldi, ldo. */
+typedef struct {
+    int spin;                   /* local-potential block (sgpu_set_veff nspin) */
+    double k[3];                /* Bloch vector, Cartesian, 1/Bohr */
+    void *X;
+    int ldi;
+    void *Y;
+    int ldo;
+    int ncol;                   /* may differ between blocks */
+    double a, b, a0;            /* this block's filter interval and lower bound */
+} sgpu_filter_block;
+
+/* ChebyshevFiltering_kpt (src/eigenSolverKpt.c:458) over all blocks at once, degree m for
+ * every block: each degree is one projection, one stencil and one apply launch covering all
+ * blocks, and the m degrees run as one CUDA graph captured on the first call and replayed
+ * while the blocks' shapes and buffers repeat. Same outputs as one sgpu_ChebyshevFiltering_kpt
+ * call per block. The reference filters its (k, spin) blocks one after another
+ * (src/eigenSolverKpt.c:165-215). */
+int sgpu_ChebyshevFiltering_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks,
+                                    int m, int precision);
+
 /* ----------------------------------------------------------------- set-up (per geometry) */
 
 /* Radial tables of one atom type, as read_pseudopotential_PSP (src/readfiles.c:1957) leaves
@@ -325,6 +354,38 @@ int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms);
 /* The context's CUDA stream (cudaStream_t), on which every call of this context runs, so that
  * a caller can order its own work or record timing events against it. */
 int sgpu_get_stream(sgpu_ctx *ctx, void **stream);
+
+/* ------------------------------------------------------ learned initial density */
+/* No counterpart in the reference, which starts each SCF from the superposition of atomic
+ * densities (Init_electronDensity, src/orbitalElecDensInit.c:145). A network trained on
+ * converged densities predicts rho_SCF - rho_at per grid point from descriptors of the atomic
+ * environment; the caller adds it to rho_at, clips at zero and restores the electron count. */
+
+/* 24 descriptors per grid point (point-major, desc[p*24 + f], device memory): for 8 Gaussian
+ * radial bins of width `width` centred on 0 .. rcut and a cosine cut-off at rcut, the sums
+ * over atom images within rcut of g_b(r), |sum g_b(r) r/|r||^2 and sum_m (sum g_b(r) Y_2m)^2. */
+int sgpu_density_descriptors(sgpu_ctx *ctx, const double *cell, int n_atom,
+                             const double *atom_pos, double rcut, double width, float *desc);
+
+/* Multilayer perceptron nin -> 3 hidden layers of `width` (SiLU) -> 1, FP32 master parameters
+ * and Adam moments, BF16 weights in the forward and backward products, FP32 accumulation.
+ * Parameter order: W1 (nin x width), b1, W2 (width x width), b2, W3, b3, w4 (width), b4. */
+typedef struct sgpu_mlp sgpu_mlp;
+int sgpu_mlp_create(int device, int nin, int width, unsigned long long seed, sgpu_mlp **net);
+int sgpu_mlp_destroy(sgpu_mlp *net);
+int sgpu_mlp_nparam(sgpu_mlp *net, long *nparam);
+/* which: 0 parameters, 1 accumulated gradient (get only), 2 input shift, 3 input scale; the
+ * network normalises its input as (x - shift) * scale. Host arrays. */
+int sgpu_mlp_get(sgpu_mlp *net, int which, float *out);
+int sgpu_mlp_set(sgpu_mlp *net, int which, const float *in);
+/* y[n] = net(x[n x nin]) (device arrays) */
+int sgpu_mlp_forward(sgpu_mlp *net, const float *x, long n, float *y);
+/* loss = mean (net(x) - tscale*target)^2 over the n rows; adds d loss / d params to the
+ * accumulated gradient */
+int sgpu_mlp_loss_grad(sgpu_mlp *net, const float *x, const float *target, long n, float tscale,
+                       double *loss);
+int sgpu_mlp_zero_grad(sgpu_mlp *net);
+int sgpu_mlp_adam_step(sgpu_mlp *net, float lr, float beta1, float beta2, float eps);
 
 /* ------------------------------------------------------------------- kernel tuning */
 

@@ -31,7 +31,18 @@ EXPORTED = [
     "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
     "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
     "sgpu_CalculateNonlocalProjectors", "sgpu_autotune", "sgpu_set_stencil_variant",
+    "sgpu_ChebyshevFiltering_batched", "sgpu_set_grid_coeffs", "sgpu_density_descriptors",
+    "sgpu_mlp_create", "sgpu_mlp_destroy", "sgpu_mlp_nparam", "sgpu_mlp_get", "sgpu_mlp_set",
+    "sgpu_mlp_forward", "sgpu_mlp_loss_grad", "sgpu_mlp_zero_grad", "sgpu_mlp_adam_step",
 ]
+
+
+class FilterBlock(ctypes.Structure):
+    """sgpu_filter_block (include/sparc_gpu.h)."""
+    _fields_ = [("spin", ctypes.c_int), ("k", ctypes.c_double * 3), ("X", ctypes.c_void_p),
+                ("ldi", ctypes.c_int), ("Y", ctypes.c_void_p), ("ldo", ctypes.c_int),
+                ("ncol", ctypes.c_int), ("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("a0", ctypes.c_double)]
 
 
 class Psd(ctypes.Structure):
@@ -156,6 +167,19 @@ class Context:
         _check(lib().sgpu_set_nonlocal(self._h, len(arrs[0]) - 1, _ptr(arrs[0]), _ptr(arrs[1]),
                                        len(arrs[2]), _ptr(arrs[2]), _ptr(arrs[3]), _ptr(arrs[4]),
                                        _ptr(arrs[5])))
+
+    def set_grid_coeffs(self, cx, cy, cz, dV):
+        cx, cy, cz = (np.ascontiguousarray(c, dtype=np.float64) for c in (cx, cy, cz))
+        _check(lib().sgpu_set_grid_coeffs(self._h, _ptr(cx), _ptr(cy), _ptr(cz),
+                                          ctypes.c_double(dV)))
+
+    def density_descriptors(self, cell, atom_pos, desc, rcut=6.0, width=0.5):
+        """24 descriptors per grid point into desc (device float32 tensor, Nd x 24)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
+        _check(lib().sgpu_density_descriptors(self._h, _ptr(cell), int(pos.size // 3), _ptr(pos),
+                                              ctypes.c_double(rcut), ctypes.c_double(width),
+                                              _ptr(desc)))
 
     # ---- per-geometry set-up (pseudopotential tables from sparc_gb300.psp8.read_psp8)
     def set_psd(self, tables):
@@ -301,6 +325,20 @@ class Context:
                                                  ctypes.c_double(b), ctypes.c_double(a0),
                                                  int(precision)))
         return X, Y
+
+    def ChebyshevFiltering_batched(self, blocks, m, precision=SGPU_PREC_FP64):
+        """Filter several (k-point, spin) blocks in one call. blocks: list of dicts with spin,
+        k (3), X, Y (device torch tensors of shape (ncol, Nd), complex128 for FP64 or
+        complex64 for FP32) and the bounds a, b, a0."""
+        arr = (FilterBlock * len(blocks))()
+        for i, b in enumerate(blocks):
+            X, Y = b["X"], b["Y"]
+            ncol = int(X.shape[0]) if X.dim() == 2 else 1
+            arr[i] = FilterBlock(int(b.get("spin", 0)), (ctypes.c_double * 3)(*b["k"]),
+                                 X.data_ptr(), self.Nd, Y.data_ptr(), self.Nd, ncol,
+                                 float(b["a"]), float(b["b"]), float(b["a0"]))
+        _check(lib().sgpu_ChebyshevFiltering_batched(self._h, len(blocks), arr, int(m),
+                                                     int(precision)))
 
     # ---- Rayleigh-Ritz
     def Project_Hamiltonian(self, Y, HY, Hp, Mp, spin=0):

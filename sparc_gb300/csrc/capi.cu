@@ -192,6 +192,20 @@ int sgpu_create(sgpu_ctx **out, int device, int Nx, int Ny, int Nz, int FDn, con
     return SGPU_OK;
 }
 
+int sgpu_set_grid_coeffs(sgpu_ctx *ctx, const double *cx, const double *cy, const double *cz,
+                         double dV)
+{
+    SGPU_TRY(check_ctx(ctx));
+    if (!cx || !cy || !cz || !(dV > 0.0)) {
+        set_error("sgpu_set_grid_coeffs: null weights or dV <= 0");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    for (int p = 0; p <= ctx->FDn; p++) { ctx->cx[p] = cx[p]; ctx->cy[p] = cy[p]; ctx->cz[p] = cz[p]; }
+    ctx->dV = dV;
+    return SGPU_OK;
+}
+
 int sgpu_destroy(sgpu_ctx *ctx)
 {
     if (!ctx) return SGPU_OK;

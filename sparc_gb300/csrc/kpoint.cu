@@ -15,36 +15,22 @@
 // e^{i k.(face shift)}, so the tile loader needs no ghost copy.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "sgpu_internal.h"
+#include "zmath.cuh"
 
 namespace sgpu {
 namespace {
 
-template <typename CT> struct Real;
-template <> struct Real<double2> { using type = double; };
-template <> struct Real<float2> { using type = float; };
-
-template <typename CT>
-__device__ __forceinline__ CT cmul(CT a, CT b)
-{
-    return CT{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-template <typename CT>
-__device__ __forceinline__ CT cadd(CT a, CT b) { return CT{a.x + b.x, a.y + b.y}; }
-template <typename CT, typename R>
-__device__ __forceinline__ CT cscale(CT a, R s) { return CT{a.x * s, a.y * s}; }
-
-__device__ __forceinline__ int wrapz(int i, int n)
-{
-    i %= n;
-    return i < 0 ? i + n : i;
-}
-__device__ __forceinline__ int floordiv(int i, int n)
-{
-    return i >= 0 ? i / n : -((-i + n - 1) / n);
-}
+using zm::Real;
+using zm::cmul;
+using zm::cadd;
+using zm::cscale;
+using zm::wrapz;
+using zm::floordiv;
+using zm::phase;
 
 struct KParams {
     double kLx, kLy, kLz;  // k_d * L_d
@@ -64,26 +50,15 @@ struct StencilZParams {
     KParams k;
 };
 
-template <typename CT>
-__device__ __forceinline__ CT phase(double theta)
-{
-    double s, c;
-    sincos(theta, &s, &c);
-    using R = typename Real<CT>::type;
-    return CT{(R)c, (R)s};
-}
-
 // one point per thread, z-register queue, shared plane with x/y halo (as the real kernel);
 // every fetched value is multiplied by the Bloch factor of its unwrapped position
 template <typename CT, int R, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY) k_stencil_z(const StencilZParams<CT> p)
+__device__ __forceinline__ void stencil_z_body(const StencilZParams<CT> &p, int col, int slab)
 {
     using RT = typename Real<CT>::type;
     __shared__ CT s[BY + 2 * R][BX + 2 * R];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
-    const int col = blockIdx.z / p.nslab;
-    const int slab = blockIdx.z - col * p.nslab;
     const int zs = slab * p.zlen;
     const int ze = min(zs + p.zlen, p.Nz);
     if (zs >= ze) return;
@@ -156,21 +131,26 @@ __global__ void __launch_bounds__(BX *BY) k_stencil_z(const StencilZParams<CT> p
     }
 }
 
+template <typename CT, int R, int BX, int BY>
+__global__ void __launch_bounds__(BX *BY) k_stencil_z(const StencilZParams<CT> p)
+{
+    stencil_z_body<CT, R, BX, BY>(p, blockIdx.z / p.nslab, blockIdx.z % p.nslab);
+}
+
 // projection: block = (atom image g, group of 32 columns), threads stride over the image's
 // points; alpha[row * lda + n] += e^{i theta_g} dV Gamma_row sum_i Chi[i, j] x[gp_i, n]
+constexpr int kProjCols = 32;
 template <typename CT, int MAXJ>
-__global__ void __launch_bounds__(256)
-    k_nl_project_z(const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
-                   const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
-                   const int *__restrict__ grid_pos, const double *__restrict__ chi,
-                   const int *__restrict__ ip_displ, const double *__restrict__ gamma,
-                   const double2 *__restrict__ img_phase, int ncol, const CT *__restrict__ x,
-                   long ldx, CT *__restrict__ alpha, long lda, double dV)
+__device__ __forceinline__ void nl_project_z_body(
+    const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
+    const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
+    const int *__restrict__ grid_pos, const double *__restrict__ chi,
+    const int *__restrict__ ip_displ, const double *__restrict__ gamma,
+    const double2 *__restrict__ img_phase, int ncol, const CT *__restrict__ x, long ldx,
+    CT *__restrict__ alpha, long lda, double dV, int g, int n0)
 {
     using RT = typename Real<CT>::type;
-    constexpr int NC = 32, PG = 8;  // 32 columns x 8 point groups
-    const int g = blockIdx.x;
-    const int n0 = blockIdx.y * NC;
+    constexpr int NC = kProjCols, PG = 8;  // 32 columns x 8 point groups
     const int a = img_atom[g];
     const int np = ip_displ[a + 1] - ip_displ[a];
     const int ndc = img_ndc[g];
@@ -212,17 +192,30 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <typename CT, int MAXJ>
+__global__ void __launch_bounds__(256)
+    k_nl_project_z(const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
+                   const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
+                   const int *__restrict__ grid_pos, const double *__restrict__ chi,
+                   const int *__restrict__ ip_displ, const double *__restrict__ gamma,
+                   const double2 *__restrict__ img_phase, int ncol, const CT *__restrict__ x,
+                   long ldx, CT *__restrict__ alpha, long lda, double dV)
+{
+    nl_project_z_body<CT, MAXJ>(img_atom, img_ndc, img_off, img_chi_off, grid_pos, chi,
+                                ip_displ, gamma, img_phase, ncol, x, ldx, alpha, lda, dV,
+                                blockIdx.x, blockIdx.y * kProjCols);
+}
+
 // apply: one thread per covered point, all columns; Hx[p] += s1 e^{-i theta_g} Chi alpha
 template <typename CT, int NPMAX>
-__global__ void __launch_bounds__(256)
-    k_nl_apply_z(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
-                 const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
-                 const double *__restrict__ chi, const double2 *__restrict__ img_phase,
-                 int ncol, const CT *__restrict__ alpha, long lda, double scale,
-                 CT *__restrict__ out, long ldo)
+__device__ __forceinline__ void nl_apply_z_body(
+    int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+    const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+    const double *__restrict__ chi, const double2 *__restrict__ img_phase, int ncol,
+    const CT *__restrict__ alpha, long lda, double scale, CT *__restrict__ out, long ldo,
+    int cidx)
 {
     using RT = typename Real<CT>::type;
-    const int cidx = blockIdx.x * blockDim.x + threadIdx.x;
     if (cidx >= ncov) return;
     const long p = cov_pt[cidx];
     const int e0 = cov_ptr[cidx], e1 = cov_ptr[cidx + 1];
@@ -248,11 +241,126 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <typename CT, int NPMAX>
+__global__ void __launch_bounds__(256)
+    k_nl_apply_z(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+                 const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+                 const double *__restrict__ chi, const double2 *__restrict__ img_phase,
+                 int ncol, const CT *__restrict__ alpha, long lda, double scale,
+                 CT *__restrict__ out, long ldo)
+{
+    nl_apply_z_body<CT, NPMAX>(ncov, cov_pt, cov_ptr, ent_chi, ent_meta, chi, img_phase, ncol,
+                               alpha, lda, scale, out, ldo, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ------------------------------------------------------------ batched (k-point, spin) blocks
+//
+// All blocks of one filter call advance one degree per group of three launches (projection,
+// stencil + recurrence, apply), each launch covering every block: the work tables map a
+// launch's grid to (block, column) pairs, so blocks of uneven column counts share one launch.
+// Per-block data (buffers, Bloch vector, image phases, projection coefficients) and the
+// per-(block, degree) recurrence scalars live in device tables written before each call, so
+// the degree loop is captured once as a CUDA graph and replayed while the shapes repeat.
+
+template <typename CT>
+struct BBlock {
+    CT *buf[3];             // X, Y and the routing scratch block
+    long ld[3];
+    CT *alpha;              // ntot x ncol projection coefficients (lda = ncol)
+    const double2 *phase;   // e^{i theta_g} per image for this block's k
+    double kL[3];           // k_d * L_d
+    int ncol, spin;
+};
+
+struct BCoef {
+    double c0, s1, s2;      // centre weight (with the shift), output and recurrence scales
+};
+
+struct BConst {
+    double wx[kMaxFDn + 1], wy[kMaxFDn + 1], wz[kMaxFDn + 1];
+    int Nx, Ny, Nz, nslab, zlen, m;
+    long Nd;
+    const double *veff64;
+    const float *veff32;
+};
+
+template <typename CT, int R, int BX, int BY>
+__global__ void __launch_bounds__(BX *BY)
+    k_stencil_zb(const BBlock<CT> *__restrict__ blocks, const BCoef *__restrict__ coef,
+                 const int2 *__restrict__ work, const BConst cs, int deg, int in_sel,
+                 int out_sel, int z_sel)
+{
+    const int w = blockIdx.z / cs.nslab, slab = blockIdx.z % cs.nslab;
+    const int2 bc = work[w];
+    const BBlock<CT> &B = blocks[bc.x];
+    const BCoef cf = coef[(long)bc.x * cs.m + deg];
+    StencilZParams<CT> p;
+    p.x = B.buf[in_sel]; p.ldx = B.ld[in_sel];
+    p.out = B.buf[out_sel]; p.ldo = B.ld[out_sel];
+    p.z = z_sel >= 0 ? B.buf[z_sel] : nullptr; p.ldz = z_sel >= 0 ? B.ld[z_sel] : 0;
+    const bool f64 = sizeof(CT) == 16;
+    p.v = f64 ? cs.veff64 + (long)B.spin * cs.Nd : nullptr;
+    p.v32 = f64 ? nullptr : cs.veff32 + (long)B.spin * cs.Nd;
+    p.Nx = cs.Nx; p.Ny = cs.Ny; p.Nz = cs.Nz; p.nslab = cs.nslab; p.zlen = cs.zlen;
+#pragma unroll
+    for (int r = 0; r <= kMaxFDn; r++) { p.wx[r] = cs.wx[r]; p.wy[r] = cs.wy[r]; p.wz[r] = cs.wz[r]; }
+    p.c0 = cf.c0; p.bv = 1.0; p.s1 = cf.s1; p.s2 = cf.s2;
+    p.k.kLx = B.kL[0]; p.k.kLy = B.kL[1]; p.k.kLz = B.kL[2];
+    stencil_z_body<CT, R, BX, BY>(p, bc.y, slab);
+}
+
+// grid (image, column group); cg[y] = (block, first column)
+template <typename CT, int MAXJ>
+__global__ void __launch_bounds__(256)
+    k_nl_project_zb(const BBlock<CT> *__restrict__ blocks, const int2 *__restrict__ cg,
+                    int in_sel, const int *__restrict__ img_atom, const int *__restrict__ img_ndc,
+                    const long *__restrict__ img_off, const long *__restrict__ img_chi_off,
+                    const int *__restrict__ grid_pos, const double *__restrict__ chi,
+                    const int *__restrict__ ip_displ, const double *__restrict__ gamma,
+                    double dV)
+{
+    const int2 bc = cg[blockIdx.y];
+    const BBlock<CT> &B = blocks[bc.x];
+    nl_project_z_body<CT, MAXJ>(img_atom, img_ndc, img_off, img_chi_off, grid_pos, chi,
+                                ip_displ, gamma, B.phase, B.ncol, B.buf[in_sel], B.ld[in_sel],
+                                B.alpha, B.ncol, dV, blockIdx.x, bc.y);
+}
+
+// grid (covered-point chunk, block)
+template <typename CT, int NPMAX>
+__global__ void __launch_bounds__(256)
+    k_nl_apply_zb(const BBlock<CT> *__restrict__ blocks, const BCoef *__restrict__ coef,
+                  int m, int deg, int out_sel, int ncov, const int *__restrict__ cov_pt,
+                  const int *__restrict__ cov_ptr, const long *__restrict__ ent_chi,
+                  const int4 *__restrict__ ent_meta, const double *__restrict__ chi)
+{
+    const BBlock<CT> &B = blocks[blockIdx.y];
+    const double scale = coef[(long)blockIdx.y * m + deg].s1;
+    nl_apply_z_body<CT, NPMAX>(ncov, cov_pt, cov_ptr, ent_chi, ent_meta, chi, B.phase, B.ncol,
+                               B.alpha, B.ncol, scale, B.buf[out_sel], B.ld[out_sel],
+                               blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host side
 
+// device tables and the cached CUDA graph of the batched filter
+struct BatchState {
+    void *tables = nullptr;
+    size_t tables_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long> key;
+    ~BatchState()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (tables) cudaFree(tables);
+    }
+};
+
 struct KpointState {
+    BatchState batch;
+    long batch_launches = 0;         // kernels in the cached batched-filter graph
     double L[3] = {0, 0, 0};
     std::vector<double> img_coords;  // 3 * nimg
     double2 *img_phase = nullptr;    // device, nimg
@@ -450,6 +558,232 @@ int chebyshev_z(sgpu_ctx *ctx, int spin, const double *k, CT *X, long ldx, CT *Y
     return SGPU_OK;
 }
 
+// Batched filter: every block's degree j in one projection, one stencil and one apply launch;
+// the launches of all m degrees are captured once in a CUDA graph (replayed while the call's
+// shapes, buffers and workspaces repeat), and the per-call numbers go in through the tables.
+template <typename CT>
+static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
+                             cudaStream_t st)
+{
+    constexpr int R = 6, BX = 32, BY = 8;
+    KpointState *ks;
+    SGPU_TRY(kstate(ctx, &ks));
+    const Nonlocal &nl = ctx->nl;
+    const bool has_nl = ctx->has_nl && nl.ntot > 0;
+    if (has_nl && ks->nimg != nl.nimg) {
+        set_error("batched filter: image coordinates do not match the nonlocal set");
+        return SGPU_ERR_STATE;
+    }
+    if (has_nl && nl.max_np > 18) {
+        set_error("batched filter: more than 18 projectors per atom is not built");
+        return SGPU_ERR_ARG;
+    }
+    const long Nd = ctx->Nd;
+    const bool route = ((m - 1) % 2) == 1;
+    std::vector<long> coloff(nblk + 1, 0);
+    for (int b = 0; b < nblk; b++) coloff[b + 1] = coloff[b] + blk[b].ncol;
+    const long totcols = coloff[nblk];
+    if (totcols == 0) return SGPU_OK;
+    CT *W = nullptr, *alpha = nullptr;
+    if (route) SGPU_TRY(ws_get(ctx, WS_STAGE_C, sizeof(CT) * (size_t)Nd * totcols, (void **)&W));
+    if (has_nl)
+        SGPU_TRY(ws_get(ctx, WS_ALPHA, sizeof(CT) * (size_t)nl.ntot * totcols, (void **)&alpha));
+
+    // host copies of the tables: blocks | coef | work | column groups | phases
+    std::vector<BBlock<CT>> hb(nblk);
+    std::vector<BCoef> hc((size_t)nblk * m);
+    std::vector<int2> hw, hg;
+    const int nimg = has_nl ? nl.nimg : 0;
+    std::vector<double2> hp((size_t)nblk * std::max(nimg, 1));
+    int maxspin = 0;
+    for (int b = 0; b < nblk; b++) {
+        const sgpu_filter_block &f = blk[b];
+        maxspin = std::max(maxspin, f.spin);
+        BBlock<CT> &B = hb[b];
+        B.buf[0] = reinterpret_cast<CT *>(f.X); B.ld[0] = f.ldi;
+        B.buf[1] = reinterpret_cast<CT *>(f.Y); B.ld[1] = f.ldo;
+        B.buf[2] = route ? W + (size_t)Nd * coloff[b] : nullptr; B.ld[2] = Nd;
+        B.alpha = has_nl ? alpha + (size_t)nl.ntot * coloff[b] : nullptr;
+        B.phase = nullptr;  // set after the table is placed
+        for (int d = 0; d < 3; d++) B.kL[d] = f.k[d] * ks->L[d];
+        B.ncol = f.ncol;
+        B.spin = f.spin;
+        // recurrence scalars of ChebyshevFiltering_kpt (src/eigenSolverKpt.c:458-550)
+        const double e = 0.5 * (f.b - f.a), c = 0.5 * (f.b + f.a);
+        double sigma = e / (f.a0 - c);
+        const double sigma1 = sigma, gamma = 2.0 / sigma1;
+        double c0 = ctx->cx[0] * -0.5;
+        c0 += ctx->cy[0] * -0.5;
+        c0 += ctx->cz[0] * -0.5;
+        c0 += -c;
+        for (int j = 0; j < m; j++) {
+            BCoef &q = hc[(size_t)b * m + j];
+            q.c0 = c0;
+            if (j == 0) {
+                q.s1 = sigma1 / e;
+                q.s2 = 0.0;
+            } else {
+                const double sigma2 = 1.0 / (gamma - sigma);
+                q.s1 = 2.0 * sigma2 / e;
+                q.s2 = -sigma * sigma2;
+                sigma = sigma2;
+            }
+        }
+        for (int n = 0; n < f.ncol; n++) hw.push_back(make_int2(b, n));
+        for (int n0 = 0; n0 < f.ncol; n0 += kProjCols) hg.push_back(make_int2(b, n0));
+        for (int g = 0; g < nimg; g++) {
+            const double *cgc = &ks->img_coords[3 * g];
+            double th = 0.0;
+            for (int d = 0; d < 3; d++) th -= f.k[d] * (std::floor(cgc[d] / ks->L[d]) * ks->L[d]);
+            hp[(size_t)b * nimg + g] = make_double2(std::cos(th), std::sin(th));
+        }
+    }
+    if (maxspin >= ctx->nspin_veff) {
+        set_error("batched filter: a block's spin has no local potential");
+        return SGPU_ERR_STATE;
+    }
+    auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t ob = 0, oc = align(ob + sizeof(BBlock<CT>) * nblk),
+                 ow = align(oc + sizeof(BCoef) * hc.size()),
+                 og = align(ow + sizeof(int2) * hw.size()),
+                 op = align(og + sizeof(int2) * hg.size()), oend = align(op + sizeof(double2) * hp.size());
+    BatchState &bs = ks->batch;
+    if (bs.tables_bytes < oend) {
+        if (bs.exec) { cudaGraphExecDestroy(bs.exec); bs.exec = nullptr; }
+        SGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (bs.tables) cudaFree(bs.tables);
+        bs.tables = nullptr;
+        bs.tables_bytes = 0;
+        SGPU_CUDA_TRY(cudaMalloc(&bs.tables, oend));
+        bs.tables_bytes = oend;
+    }
+    char *tb = static_cast<char *>(bs.tables);
+    for (int b = 0; b < nblk; b++)
+        hb[b].phase = reinterpret_cast<const double2 *>(tb + op) + (size_t)b * nimg;
+    std::vector<char> pack(oend, 0);
+    std::memcpy(pack.data() + ob, hb.data(), sizeof(BBlock<CT>) * nblk);
+    std::memcpy(pack.data() + oc, hc.data(), sizeof(BCoef) * hc.size());
+    std::memcpy(pack.data() + ow, hw.data(), sizeof(int2) * hw.size());
+    std::memcpy(pack.data() + og, hg.data(), sizeof(int2) * hg.size());
+    std::memcpy(pack.data() + op, hp.data(), sizeof(double2) * hp.size());
+    SGPU_CUDA_TRY(cudaMemcpyAsync(tb, pack.data(), oend, cudaMemcpyHostToDevice, st));
+    // the host staging buffer must outlive the copy
+    SGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    const BBlock<CT> *dB = reinterpret_cast<const BBlock<CT> *>(tb + ob);
+    const BCoef *dC = reinterpret_cast<const BCoef *>(tb + oc);
+    const int2 *dW = reinterpret_cast<const int2 *>(tb + ow);
+    const int2 *dG = reinterpret_cast<const int2 *>(tb + og);
+
+    BConst cs;
+    for (int r = 0; r <= R; r++) {
+        cs.wx[r] = ctx->cx[r] * -0.5;
+        cs.wy[r] = ctx->cy[r] * -0.5;
+        cs.wz[r] = ctx->cz[r] * -0.5;
+    }
+    cs.Nx = ctx->Nx; cs.Ny = ctx->Ny; cs.Nz = ctx->Nz; cs.m = m; cs.Nd = Nd;
+    cs.veff64 = ctx->veff64;
+    cs.veff32 = ctx->veff32;
+    const int tilesx = (ctx->Nx + BX - 1) / BX, tilesy = (ctx->Ny + BY - 1) / BY;
+    int nslab = 1;
+    while ((long)tilesx * tilesy * totcols * nslab < 152L * 8 && ctx->Nz / (nslab * 2) >= 8)
+        nslab *= 2;
+    cs.nslab = nslab;
+    cs.zlen = (ctx->Nz + nslab - 1) / nslab;
+    const long maxw = 65535 / nslab;
+    const size_t abytes = has_nl ? sizeof(CT) * (size_t)nl.ntot * totcols : 0;
+
+    auto issue = [&]() -> int {
+        int cur = route ? 2 : 1, prev = 0;  // buffer ids: 0 X, 1 Y, 2 scratch
+        for (int j = 0; j < m; j++) {
+            int in, out, zsel;
+            if (j == 0) {
+                in = 0; out = cur; zsel = -1;
+            } else {
+                int dst = prev;
+                if (route && j == 1) dst = 1;
+                if (route && j == 2) dst = 0;
+                in = cur; out = dst; zsel = prev;
+                prev = cur;
+                cur = dst;
+            }
+            if (has_nl) {
+                SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, abytes, st));
+                ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
+                const dim3 pg(nl.nimg, (unsigned)hg.size());
+                if (nl.max_np <= 9)
+                    k_nl_project_zb<CT, 9><<<pg, 256, 0, st>>>(dB, dG, in, nl.img_atom,
+                        nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, nl.chi64,
+                        nl.ip_displ, nl.gamma64, ctx->dV);
+                else
+                    k_nl_project_zb<CT, 18><<<pg, 256, 0, st>>>(dB, dG, in, nl.img_atom,
+                        nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, nl.chi64,
+                        nl.ip_displ, nl.gamma64, ctx->dV);
+                ctx->launches++;
+            }
+            for (long w0 = 0; w0 < totcols; w0 += maxw) {
+                const long nw = std::min(maxw, totcols - w0);
+                ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
+                k_stencil_zb<CT, R, BX, BY><<<dim3(tilesx, tilesy, (unsigned)(nw * nslab)),
+                                              dim3(BX, BY), 0, st>>>(dB, dC, dW + w0, cs, j, in,
+                                                                     out, zsel);
+                ctx->launches++;
+            }
+            if (has_nl) {
+                ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+                const dim3 ag((nl.ncov + 255) / 256, nblk);
+                if (nl.max_np <= 9)
+                    k_nl_apply_zb<CT, 9><<<ag, 256, 0, st>>>(dB, dC, m, j, out, nl.ncov,
+                        nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.chi64);
+                else
+                    k_nl_apply_zb<CT, 18><<<ag, 256, 0, st>>>(dB, dC, m, j, out, nl.ncov,
+                        nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.chi64);
+                ctx->launches++;
+            }
+        }
+        if (route && m == 2) {  // the degree-1 iterate is still in the scratch block
+            for (int b = 0; b < nblk; b++)
+                SGPU_CUDA_TRY(cudaMemcpy2DAsync(blk[b].X, sizeof(CT) * blk[b].ldi,
+                                                W + (size_t)Nd * coloff[b], sizeof(CT) * Nd,
+                                                sizeof(CT) * Nd, blk[b].ncol,
+                                                cudaMemcpyDeviceToDevice, st));
+        }
+        SGPU_CUDA_TRY(cudaGetLastError());
+        return SGPU_OK;
+    };
+
+    if (ctx->prof_on) return issue();  // per-launch events need plain launches
+    std::vector<long> key = {(long)sizeof(CT), nblk, m, (long)(uintptr_t)tb, (long)(uintptr_t)W,
+                             (long)(uintptr_t)alpha, (long)hg.size(), nslab,
+                             (long)(uintptr_t)ctx->veff64, (long)(uintptr_t)ctx->veff32};
+    for (int b = 0; b < nblk; b++) {
+        key.push_back(blk[b].ncol);
+        key.push_back((long)(uintptr_t)blk[b].X);
+        key.push_back((long)(uintptr_t)blk[b].Y);
+    }
+    if (!bs.exec || key != bs.key) {
+        if (bs.exec) { cudaGraphExecDestroy(bs.exec); bs.exec = nullptr; }
+        const long launches0 = ctx->launches;
+        cudaGraph_t graph = nullptr;
+        SGPU_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = issue();
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (rc != SGPU_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        SGPU_CUDA_TRY(ec);
+        const cudaError_t ei = cudaGraphInstantiate(&bs.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        SGPU_CUDA_TRY(ei);
+        bs.key = key;
+        ks->batch_launches = ctx->launches - launches0;
+        ctx->launches = launches0;
+    }
+    SGPU_CUDA_TRY(cudaGraphLaunch(bs.exec, st));
+    ctx->launches += ks->batch_launches;
+    return SGPU_OK;
+}
+
 template int hamiltonian_z<double2>(sgpu_ctx *, int, const double *, int, double, const double2 *,
                                     long, double2 *, long, double, double, const double2 *, long,
                                     cudaStream_t);
@@ -635,6 +969,49 @@ int sgpu_ChebyshevFiltering_kpt(sgpu_ctx *ctx, int spin, const double *k, double
     SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
     SGPU_TRY(zstage_out(ctx, dX, lX, X, ldi, ncol));
     SGPU_TRY(zstage_out(ctx, dY, lY, Y, ldo, ncol));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    SGPU_CUDA_TRY(cudaEventElapsedTime(&ctx->last_filter_ms, ctx->ev0, ctx->ev1));
+    return SGPU_OK;
+}
+
+int sgpu_ChebyshevFiltering_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks,
+                                    int m, int precision)
+{
+    if (!ctx || nblk < 0 || (nblk > 0 && !blocks) || m < 1) {
+        set_error("ChebyshevFiltering_batched: need a context, nblk >= 0 blocks and m >= 1");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (precision != SGPU_PREC_FP64 && precision != SGPU_PREC_FP32) {
+        set_error("ChebyshevFiltering_batched: precision must be SGPU_PREC_FP64 (complex128) or "
+                  "SGPU_PREC_FP32 (complex64)");
+        return SGPU_ERR_ARG;
+    }
+    for (int b = 0; b < nblk; b++) {
+        const sgpu_filter_block &f = blocks[b];
+        if (f.ncol < 0 || f.ldi < ctx->Nd || f.ldo < ctx->Nd || f.spin < 0) {
+            set_error("ChebyshevFiltering_batched: block " + std::to_string(b) +
+                      ": need ncol >= 0, spin >= 0 and leading dimensions >= Nd");
+            return SGPU_ERR_ARG;
+        }
+        if (f.ncol > 0 && (!is_device_ptr(f.X) || !is_device_ptr(f.Y))) {
+            set_error("ChebyshevFiltering_batched: block " + std::to_string(b) +
+                      ": X and Y must be device memory");
+            return SGPU_ERR_ARG;
+        }
+        if (!(f.b > f.a) || !(f.a > f.a0)) {
+            set_error("ChebyshevFiltering_batched: block " + std::to_string(b) +
+                      ": need a0 < a < b");
+            return SGPU_ERR_ARG;
+        }
+    }
+    if (nblk == 0) return SGPU_OK;
+    SGPU_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (precision == SGPU_PREC_FP64)
+        SGPU_TRY(chebyshev_batched<double2>(ctx, nblk, blocks, m, ctx->stream));
+    else
+        SGPU_TRY(chebyshev_batched<float2>(ctx, nblk, blocks, m, ctx->stream));
+    SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
     SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     SGPU_CUDA_TRY(cudaEventElapsedTime(&ctx->last_filter_ms, ctx->ev0, ctx->ev1));
     return SGPU_OK;

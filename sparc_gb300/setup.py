@@ -46,26 +46,41 @@ class CellSystem:
                  FDn=6, device=0):
         """species: list of (symbol, positions (n, 3) Bohr); tables: {symbol: read_psp8
         dict}. Atoms are ordered type by type, as the reference orders them."""
-        self.L = np.asarray(L, dtype=np.float64)
         self.N = tuple(int(n) for n in N)
+        self.FDn = FDn
+        self.tables = [tables[s] for s, _ in species]
+        self.tol_scf = tol_scf
+        self.ref_cutoff = ref_cutoff
+        self.net_charge = net_charge
+        self.nlcc = any(float(t["fchrg"]) > 1e-12 for t in self.tables)
+        self._grid(L)
+        self.ctx = Context(*self.N, FDn, self.cx, self.cy, self.cz, self.dV, device=device)
+        self.ctx.set_psd(self.tables)
+        self.set_geometry(L, species)
+
+    def _grid(self, L):
+        self.L = np.asarray(L, dtype=np.float64)
         self.h = self.L / np.array(self.N)
         self.dV = float(np.prod(self.h))
-        self.FDn = FDn
-        self.cx, self.cy, self.cz = (fd_d2_coeffs(FDn, hh) for hh in self.h)
+        self.cx, self.cy, self.cz = (fd_d2_coeffs(self.FDn, hh) for hh in self.h)
+
+    def set_geometry(self, L, species):
+        """New cell lengths (same grid) and atom positions (same species and counts): the FD
+        weights, pseudocharge cut-offs, set-up fields and projectors are rebuilt on the
+        existing context."""
+        if np.any(np.asarray(L, dtype=np.float64) != getattr(self, "L", None)):
+            self._grid(L)
+            self.ctx.set_grid_coeffs(self.cx, self.cy, self.cz, self.dV)
         self.nAtomv = np.array([len(p) for _, p in species], dtype=np.int32)
         self.n_atom = int(self.nAtomv.sum())
         self.atom_pos = np.concatenate([ion_coordinates(p, self.L) for _, p in species], axis=0)
-        self.tables = [tables[s] for s, _ in species]
         self.Nelectron = float(sum(int(t["Znucl"]) * n for t, n in zip(self.tables,
-                                                                       self.nAtomv))) - net_charge
-        self.tol_scf = tol_scf
-        self.ctx = Context(*self.N, FDn, self.cx, self.cy, self.cz, self.dV, device=device)
-        self.ctx.set_psd(self.tables)
-        self.cutoff = self.ctx.Calculate_PseudochargeCutoff(self.L, 1e-3 * tol_scf)
+                                                                       self.nAtomv))) - self.net_charge
+        self.cutoff = self.ctx.Calculate_PseudochargeCutoff(self.L, 1e-3 * self.tol_scf)
         self.fields = self.ctx.Generate_PseudoChargeDensity(
-            self.L, self.nAtomv, self.atom_pos, ref_cutoff=ref_cutoff, net_charge=net_charge)
+            self.L, self.nAtomv, self.atom_pos, ref_cutoff=self.ref_cutoff,
+            net_charge=self.net_charge)
         self.ctx.CalculateNonlocalProjectors(self.L, self.nAtomv, self.atom_pos)
-        self.nlcc = any(float(t["fchrg"]) > 1e-12 for t in self.tables)
 
     def scf_params(self, Nstates, cheb_degree, smearing=1e-3, precision=SGPU_PREC_FP64,
                    fp64_switch_error=1e-4, graded_tail=0, tail_fp64_degrees=0, seed=1,
@@ -108,10 +123,11 @@ class CellSystem:
         p.verbose = verbose
         return p
 
-    def scf(self, params):
-        """Run the SCF from the superposition of atomic densities."""
+    def scf(self, params, rho_init=None):
+        """Run the SCF from the superposition of atomic densities (or from rho_init)."""
         f = self.fields
-        return self.ctx.scf(params, f["b"], f["rho_at"], f["rho_core"] if self.nlcc else None)
+        r0 = f["rho_at"] if rho_init is None else rho_init
+        return self.ctx.scf(params, f["b"], r0, f["rho_core"] if self.nlcc else None)
 
     def close(self):
         self.ctx.close()
