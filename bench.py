@@ -382,7 +382,8 @@ def main():
     # pick the FP32 stencil variant for this grid (all variants give identical results)
     variant, variant_ms = ctx.autotune(ncol=min(ncol, 64))
     kernel_name = ["k_stencil_f32x2<32x16>", "k_stencil_f32_b22<32x16>",
-                   "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>"][variant]
+                   "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
+                   "k_stencil_f32_b22<32x16, 3 blocks/SM>"][variant]
 
     gen = torch.Generator(device=dev)
     gen.manual_seed(1234 + rank)

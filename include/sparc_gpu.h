@@ -391,12 +391,12 @@ int sgpu_mlp_adam_step(sgpu_mlp *net, float lr, float beta1, float beta2, float 
 
 /* Time every FP32 stencil kernel variant (tile shape and register blocking) on ncol scratch
  * columns of this context's grid, keep the fastest for later calls, and return its index in
- * *variant and per-variant milliseconds in ms (4 values; may be NULL). All variants give
+ * *variant and per-variant milliseconds in ms (5 values; may be NULL). All variants give
  * identical results. sgpu_scf runs this once per context before its first FP32 filter.
  * No counterpart in the reference. */
 int sgpu_autotune(sgpu_ctx *ctx, int ncol, int *variant, double *ms);
 
-/* Fix the FP32 stencil variant (0..3) without timing. */
+/* Fix the FP32 stencil variant (0..4) without timing. */
 int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
 
 /* ------------------------------------------------------------------- measurement */

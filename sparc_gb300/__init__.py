@@ -430,7 +430,7 @@ class Context:
     def autotune(self, ncol=64):
         """Time the FP32 stencil variants; returns (chosen variant, per-variant ms)."""
         v = ctypes.c_int()
-        ms = np.zeros(4)
+        ms = np.zeros(5)
         _check(lib().sgpu_autotune(self._h, int(ncol), ctypes.byref(v), _ptr(ms)))
         return int(v.value), ms
 

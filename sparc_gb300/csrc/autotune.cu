@@ -8,7 +8,7 @@
 
 namespace sgpu {
 
-constexpr int kStencilVariants = 4;
+constexpr int kStencilVariants = 5;
 
 // Times one degree-step launch (stencil + potential + recurrence term) of each FP32 variant
 // over ncol columns; returns the fastest in *best and per-variant milliseconds in ms.
@@ -73,7 +73,7 @@ extern "C" {
 int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant)
 {
     if (!ctx || variant < 0 || variant >= kStencilVariants) {
-        set_error("sgpu_set_stencil_variant: variant must be 0..3");
+        set_error("sgpu_set_stencil_variant: variant must be 0..4");
         return SGPU_ERR_ARG;
     }
     ctx->stencil_variant = variant;

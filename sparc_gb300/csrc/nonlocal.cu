@@ -11,10 +11,12 @@
 //     once, then the block walks all column groups, gathering x[grid_pos, group] into shared
 //     memory chunk by chunk and accumulating alpha[j, n] in registers; one atomic add per
 //     (projector, column) and segment, with dV * Gamma folded in.
-//   * apply: owner-computes over a CSR of covered grid points: one thread per covered point
-//     loops over all column blocks, so each output element is written by exactly one thread
-//     (no atomics on the orbital block; overlapping spheres are summed in registers) and the
-//     thread's Chi values are re-read from L1, not HBM, for every column block after the first.
+//   * apply: owner-computes over a CSR of covered grid points, so each output element is
+//     written by exactly one thread (no atomics on the orbital block; overlapping spheres are
+//     summed in registers). The staged form gives each block a chunk of consecutive covered
+//     points and a block of columns, with the alpha rows of the chunk's atoms staged in shared
+//     memory; the unstaged form (one thread per point over all column blocks, alpha from L1)
+//     serves chunks whose atoms' rows would not fit.
 #include <algorithm>
 #include <numeric>
 
@@ -25,6 +27,8 @@ namespace {
 
 constexpr int kProjThreads = 256;
 constexpr int kSegPts = 512;  // points of one image handled by one projection block
+constexpr int kApplyChunk = 128;   // covered points per block of the staged apply
+constexpr size_t kApplyStageMax = 96 * 1024;  // staged alpha rows must fit this (bytes)
 
 template <typename T, int CB>
 struct VecOf;
@@ -188,6 +192,64 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Apply, staged: one block per (chunk of kApplyChunk consecutive covered points, block of CB
+// columns). The alpha rows of every atom that touches the chunk are staged once in shared
+// memory (rows listed in chunk_rows), and each thread accumulates its point's CB outputs from
+// there; the output block is read-modified-written once. Neighbouring covered points share
+// atoms, so one staged row serves many threads.
+template <typename T, int CB, int NPMAX>
+__global__ void __launch_bounds__(kApplyChunk)
+    k_nl_apply_staged(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+                      const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+                      const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
+                      const int *__restrict__ chunk_rows, const T *__restrict__ chi, int ncol,
+                      const T *__restrict__ alpha, long lda, T scale, T *__restrict__ out,
+                      long ldo)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *S = reinterpret_cast<T *>(smem_raw);  // [rows][CB]
+    const int c = blockIdx.x;
+    const int n0 = blockIdx.y * CB;
+    const int cidx = c * kApplyChunk + threadIdx.x;
+    const bool live = cidx < ncov;
+    const long p = live ? cov_pt[cidx] : 0;
+    // the thread's outputs are read first so their latency overlaps the staging
+    T ov[CB];
+#pragma unroll
+    for (int q = 0; q < CB; q++)
+        ov[q] = (live && n0 + q < ncol) ? out[(long)(n0 + q) * ldo + p] : T(0);
+    const int r0 = chunk_row_ptr[c], nr = chunk_row_ptr[c + 1] - r0;
+    for (int e = threadIdx.x; e < nr * CB; e += blockDim.x) {
+        const int r = e / CB, cc = e % CB;
+        S[e] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : T(0);
+    }
+    __syncthreads();
+    if (!live) return;
+    const int e0 = cov_ptr[cidx], e1 = cov_ptr[cidx + 1];
+    T acc[CB];
+#pragma unroll
+    for (int q = 0; q < CB; q++) acc[q] = T(0);
+    for (int e = e0; e < e1; e++) {
+        const int4 meta = ent_meta[e];  // (first projector row, projector count, ndc, image)
+        const int np = meta.y, ndc = meta.z;
+        const T *__restrict__ ch = chi + ent_chi[e];
+        const T *__restrict__ srow = S + (long)ent_slot[e] * CB;
+        T cvs[NPMAX];
+#pragma unroll
+        for (int j = 0; j < NPMAX; j++) cvs[j] = j < np ? __ldg(ch + (long)j * ndc) : T(0);
+#pragma unroll
+        for (int j = 0; j < NPMAX; j++) {
+            if (j >= np) break;
+            const T cv = cvs[j];
+#pragma unroll
+            for (int q = 0; q < CB; q++) acc[q] += cv * srow[j * CB + q];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < CB; q++)
+        if (n0 + q < ncol) out[(long)(n0 + q) * ldo + p] = ov[q] + scale * acc[q];
+}
+
 template <typename T>
 const T *chi_of(const Nonlocal &nl);
 template <>
@@ -261,6 +323,31 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
     if (!ctx->has_nl || nl.ncov == 0 || ncol <= 0) return SGPU_OK;
     constexpr int CB = apply_cb<T>();
     constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+    constexpr int SCB = sizeof(T) == 4 ? 32 : 16;  // columns per block of the staged form
+    const size_t stage = sizeof(T) * (size_t)nl.max_chunk_rows * SCB;
+    if (nl.nchunk > 0 && stage <= kApplyStageMax) {
+        const dim3 sg(nl.nchunk, (ncol + SCB - 1) / SCB);
+        ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+#define SGPU_STAGED(NPM)                                                                     \
+    {                                                                                        \
+        auto kern = k_nl_apply_staged<T, SCB, NPM>;                                          \
+        SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                           (int)std::max<size_t>(stage, 16)));               \
+        kern<<<sg, kApplyChunk, std::max<size_t>(stage, 16), st>>>(                          \
+            nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.ent_slot,            \
+            nl.chunk_row_ptr, nl.chunk_rows, chi_of<T>(nl), ncol, alpha, lda, (T)scale, out, \
+            ldo);                                                                            \
+    }
+        if (nl.max_np <= 9)
+            SGPU_STAGED(9)
+        else if (nl.max_np <= 18)
+            SGPU_STAGED(18)
+        else
+            SGPU_STAGED(32)
+#undef SGPU_STAGED
+        SGPU_CUDA_TRY(cudaGetLastError());
+        return SGPU_OK;
+    }
     const dim3 grid((nl.ncov + 255) / 256);
     ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
 #define SGPU_APPLY(NPM)                                                                      \
@@ -292,7 +379,7 @@ void nonlocal_free(Nonlocal &nl)
     void *ptrs[] = {nl.ip_displ, nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off,
                     nl.grid_pos, nl.chi64,    nl.chi32,   nl.gamma64, nl.gamma32,
                     nl.cov_pt,   nl.cov_ptr,  nl.ent_chi, nl.ent_meta, nl.seg_img,
-                    nl.seg_start};
+                    nl.seg_start, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     nl = Nonlocal();
@@ -372,6 +459,33 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     }
     nl.ncov = (int)covpts.size();
     nl.nent = npos;
+    // staged apply: per chunk of kApplyChunk covered points, the alpha rows of the atoms its
+    // entries use (each atom once) and, per entry, the staged row of its atom's first projector
+    std::vector<int> chunk_row_ptr(1, 0), chunk_rows, ent_slot(npos, 0);
+    nl.nchunk = (nl.ncov + kApplyChunk - 1) / kApplyChunk;
+    {
+        std::vector<int> atom_slot(natom, -1), touched;
+        for (int c = 0; c < nl.nchunk; c++) {
+            const int p0 = c * kApplyChunk, p1 = std::min(nl.ncov, p0 + kApplyChunk);
+            int rows = 0;
+            for (int e = covptr[p0]; e < covptr[p1]; e++) {
+                const int ip = ent_meta[e].x, np = ent_meta[e].y;
+                const int a = (int)(std::upper_bound(ip_displ, ip_displ + natom + 1, ip) -
+                                    ip_displ) - 1;
+                if (atom_slot[a] < 0) {
+                    atom_slot[a] = rows;
+                    touched.push_back(a);
+                    for (int j = 0; j < np; j++) chunk_rows.push_back(ip + j);
+                    rows += np;
+                }
+                ent_slot[e] = atom_slot[a];
+            }
+            for (int a : touched) atom_slot[a] = -1;
+            touched.clear();
+            chunk_row_ptr.push_back((int)chunk_rows.size());
+            nl.max_chunk_rows = std::max(nl.max_chunk_rows, rows);
+        }
+    }
     // projection work split: segments of at most kSegPts points per image
     std::vector<int> seg_img, seg_start;
     for (int g = 0; g < nimg; g++)
@@ -404,6 +518,9 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(ent_meta, ent_meta.data(), ent_meta.size());
     UP(seg_img, seg_img.data(), seg_img.size());
     UP(seg_start, seg_start.data(), seg_start.size());
+    UP(ent_slot, ent_slot.data(), ent_slot.size());
+    UP(chunk_row_ptr, chunk_row_ptr.data(), chunk_row_ptr.size());
+    UP(chunk_rows, chunk_rows.data(), chunk_rows.size());
 #undef UP
     if (rc != SGPU_OK) {
         nonlocal_free(nl);

@@ -72,6 +72,11 @@ struct Nonlocal {
     int nseg = 0;
     int *seg_img = nullptr;
     int *seg_start = nullptr;
+    // staged apply: chunks of consecutive covered points with the alpha rows they use
+    int nchunk = 0, max_chunk_rows = 0;
+    int *ent_slot = nullptr;       // nent: staged row of the entry's atom within its chunk
+    int *chunk_row_ptr = nullptr;  // nchunk + 1
+    int *chunk_rows = nullptr;     // alpha rows staged per chunk
 };
 
 struct Workspace {

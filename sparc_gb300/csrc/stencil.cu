@@ -74,9 +74,9 @@ __global__ void __launch_bounds__(BX *BY)
         hyr = gi + (long)wrapi(y0 + BY + ty, p.Ny) * p.Nx;
     }
 
-    T q[2 * R + 1];  // q[m] = x at plane k - R + m
+    T q[2 * R + 2];  // q[m] = x at plane k - R + m; q[2R+1], plane k+R+1, is in flight
 #pragma unroll
-    for (int m = 0; m < 2 * R; m++)
+    for (int m = 0; m <= 2 * R; m++)
         q[m] = __ldg(xc + own + (long)wrapi(zs - R + m, p.Nz) * NxNy);
 
     T h0 = T(0), h1 = T(0), h2 = T(0), h3 = T(0), vv = T(0), zz = T(0);
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(BX *BY)
 
     for (int k = zs; k < ze; k++) {
         const int b = k & 1;
-        q[2 * R] = __ldg(xc + own + (long)wrapi(k + R, p.Nz) * NxNy);
+        q[2 * R + 1] = __ldg(xc + own + (long)wrapi(k + R + 1, p.Nz) * NxNy);
         s[b][ty + R][tx + R] = q[R];
         if (hx) { s[b][ty + R][tx] = h0; s[b][ty + R][tx + BX + R] = h1; }
         if (hy) { s[b][ty][tx + R] = h2; s[b][ty + BY + R][tx + R] = h3; }
@@ -104,21 +104,23 @@ __global__ void __launch_bounds__(BX *BY)
         }
         __syncthreads();
         if (active) {
-            T res = p.c0 * q[R];
+            // three independent FMA chains (x, y, z): on GB300 the FP64 pipe bounds this
+            // kernel, and chained FMAs need 6 FP64 instructions per offset instead of 9
+            T rx = p.c0 * q[R], ry = T(0), rz = T(0);
 #pragma unroll
             for (int r = 1; r <= R; r++) {
-                T rx = (s[b][ty + R][tx + R - r] + s[b][ty + R][tx + R + r]) * p.wx[r];
-                T ry = (s[b][ty + R - r][tx + R] + s[b][ty + R + r][tx + R]) * p.wy[r];
-                T rz = (q[R - r] + q[R + r]) * p.wz[r];
-                res += rx + ry + rz;
+                rx = fma(s[b][ty + R][tx + R - r] + s[b][ty + R][tx + R + r], p.wx[r], rx);
+                ry = fma(s[b][ty + R - r][tx + R] + s[b][ty + R + r][tx + R], p.wy[r], ry);
+                rz = fma(q[R - r] + q[R + r], p.wz[r], rz);
             }
+            T res = rx + (ry + rz);
             if (p.v) res += p.bv * (vcur * q[R]);
             T o = p.s1 * res;
             if (zc) o += p.s2 * zcur;
             oc[own + (long)k * NxNy] = o;
         }
 #pragma unroll
-        for (int m = 0; m < 2 * R; m++) q[m] = q[m + 1];
+        for (int m = 0; m <= 2 * R; m++) q[m] = q[m + 1];
     }
 }
 
@@ -131,10 +133,10 @@ template <int R, int BXP, int BY, int MINB>
 __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
     k_stencil_f32x2(const StencilParams<float> p)
 {
-    constexpr int Q = 2 * R + 1;
+    constexpr int Q = 2 * R + 2;  // ring: planes k-R .. k+R in use, k+R+1 in flight
     constexpr int W = BXP + 2 * R;
     static_assert(R % 2 == 0 && BXP % 2 == 0, "paired layout needs even radius and tile");
-    static_assert(Q == 13, "the unrolled z-loop below is written for radius 6");
+    static_assert(Q == 14, "the unrolled z-loop below is written for radius 6");
     __shared__ __align__(16) float s[2][BY + 2 * R][W];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BXP, y0 = blockIdx.y * BY;
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
 
     float2 q[Q];
 #pragma unroll
-    for (int m = 0; m < 2 * R; m++) {
+    for (int m = 0; m <= 2 * R; m++) {
         const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
         q[m] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl));
     }
@@ -199,8 +201,8 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
         if (k < ze) {                                                                            \
             const int b = k & 1;                                                                 \
             {                                                                                    \
-                const int pl = wrapi(k + R, p.Nz) * NxNy;                                        \
-                q[((U) + 2 * R) % Q] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl)); \
+                const int pl = wrapi(k + R + 1, p.Nz) * NxNy;                                    \
+                q[((U) + 2 * R + 1) % Q] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl)); \
             }                                                                                    \
             const float2 cen = q[((U) + R) % Q];                                                 \
             *reinterpret_cast<float2 *>(&s[b][ty + R][R + 2 * tx]) = cen;                        \
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
     for (int kb = zs; kb < ze; kb += Q) {
         SGPU_F2_STEP(0) SGPU_F2_STEP(1) SGPU_F2_STEP(2) SGPU_F2_STEP(3) SGPU_F2_STEP(4)
         SGPU_F2_STEP(5) SGPU_F2_STEP(6) SGPU_F2_STEP(7) SGPU_F2_STEP(8) SGPU_F2_STEP(9)
-        SGPU_F2_STEP(10) SGPU_F2_STEP(11) SGPU_F2_STEP(12)
+        SGPU_F2_STEP(10) SGPU_F2_STEP(11) SGPU_F2_STEP(12) SGPU_F2_STEP(13)
     }
 #undef SGPU_F2_STEP
 }
@@ -315,9 +317,11 @@ template <int R, int BX, int BY, int MINB, bool VEC>
 __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     k_stencil_f32_b22(const StencilParams<float> p)
 {
-    constexpr int Q = 2 * R + 1;
+    // z-queue ring of Q = 2R+2 slots: planes k-R .. k+R are in use at plane k and plane
+    // k+R+1 is already in flight, so no plane's first use waits on its own load
+    constexpr int Q = 2 * R + 2;
     constexpr int W = BX + 2 * R;
-    static_assert(Q == 13 && R % 2 == 0, "the unrolled z-loop below is written for radius 6");
+    static_assert(Q == 14 && R % 2 == 0, "the unrolled z-loop below is written for radius 6");
     __shared__ __align__(16) float s[2][BY + 2 * R][W];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
@@ -391,7 +395,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
 
     float2 qa[Q], qb[Q];  // z-queues of rows j0 and j0+1: slot of plane k-R+m is (U+m) % Q
 #pragma unroll
-    for (int m = 0; m < 2 * R; m++) {
+    for (int m = 0; m <= 2 * R; m++) {
         const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
         qa[m] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);
         qb[m] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);
@@ -416,9 +420,9 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
         if (k < ze) {                                                                            \
             const int b = k & 1;                                                                 \
             {                                                                                    \
-                const int pl = wrapi(k + R, p.Nz) * NxNy;                                        \
-                qa[((U) + 2 * R) % Q] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);      \
-                qb[((U) + 2 * R) % Q] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);      \
+                const int pl = wrapi(k + R + 1, p.Nz) * NxNy;                                    \
+                qa[((U) + 2 * R + 1) % Q] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);  \
+                qb[((U) + 2 * R + 1) % Q] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);  \
             }                                                                                    \
             const float2 ca = qa[((U) + R) % Q], cb = qb[((U) + R) % Q];                         \
             *reinterpret_cast<float2 *>(&s[b][2 * ty + R][R + 2 * tx]) = ca;                     \
@@ -494,7 +498,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     for (int kb = zs; kb < ze; kb += Q) {
         SGPU_B22_STEP(0) SGPU_B22_STEP(1) SGPU_B22_STEP(2) SGPU_B22_STEP(3) SGPU_B22_STEP(4)
         SGPU_B22_STEP(5) SGPU_B22_STEP(6) SGPU_B22_STEP(7) SGPU_B22_STEP(8) SGPU_B22_STEP(9)
-        SGPU_B22_STEP(10) SGPU_B22_STEP(11) SGPU_B22_STEP(12)
+        SGPU_B22_STEP(10) SGPU_B22_STEP(11) SGPU_B22_STEP(12) SGPU_B22_STEP(13)
     }
 #undef SGPU_B22_STEP
     cp_async_wait_all();
@@ -538,11 +542,12 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     if (!z || s2 == 0.0) p.z = nullptr;
 
     const bool f32 = sizeof(T) == 4;
-    // FP32 variants (see stencil_variant_count): 0 paired 32x16, 1 2x2-blocked 32x16,
-    // 2 2x2-blocked 64x8, 3 paired 64x8
+    // FP32 variants (autotune.cu): 0 paired 32x16, 1 2x2-blocked 32x16, 2 2x2-blocked 64x8,
+    // 3 paired 64x8, 4 2x2-blocked 32x16 with 3 blocks per SM
     const int variant = f32 ? ctx->stencil_variant : 0;
-    const int tbx = f32 ? (variant >= 2 ? 64 : BXP) : BX;
-    const int tby = f32 ? (variant >= 2 ? 8 : BYP) : BY;
+    const bool wide = variant == 2 || variant == 3;
+    const int tbx = f32 ? (wide ? 64 : BXP) : BX;
+    const int tby = f32 ? (wide ? 8 : BYP) : BY;
     const int tilesx = (ctx->Nx + tbx - 1) / tbx;
     const int tilesy = (ctx->Ny + tby - 1) / tby;
     // split z into slabs until there are enough blocks to fill 152 SMs several times over
@@ -581,6 +586,12 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                 break;
             case 3:
                 k_stencil_f32x2<R, 64, 8, 3><<<grid, dim3(32, 8), 0, st>>>(q);
+                break;
+            case 4:  // 2x2 32x16 capped at 3 blocks per SM (no register spills)
+                if (vec)
+                    k_stencil_f32_b22<R, 32, 16, 3, true><<<grid, dim3(16, 8), 0, st>>>(q);
+                else
+                    k_stencil_f32_b22<R, 32, 16, 3, false><<<grid, dim3(16, 8), 0, st>>>(q);
                 break;
             default:
                 k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);

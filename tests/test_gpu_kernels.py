@@ -129,7 +129,7 @@ def test_fp32_stencil_variants_identical(gpu_available, shape):
     ctx = make_ctx(grid, nl, veff)
     x = rng.uniform(-1, 1, (3, Nd)).astype(np.float32)
     outs = []
-    for v in range(4):
+    for v in range(5):
         ctx.set_stencil_variant(v)
         X = x.copy(); Y = np.zeros_like(x)
         ctx.ChebyshevFiltering_f32(X, Y, 7, 0.5, 50.0, -1.0)
@@ -138,7 +138,7 @@ def test_fp32_stencil_variants_identical(gpu_available, shape):
         np.testing.assert_array_equal(Y, outs[0][1])
         np.testing.assert_array_equal(X, outs[0][0])
     best, ms = ctx.autotune(ncol=3)
-    assert 0 <= best < 4 and np.all(ms > 0)
+    assert 0 <= best < 5 and np.all(ms > 0)
 
 
 def test_device_pointers_match_host(gpu_available):
