@@ -89,9 +89,16 @@ __device__ __forceinline__ void stencil_z_body(const StencilZParams<CT> &p, int 
         f_yl = phase<CT>(floordiv(i, p.Nx) * p.k.kLx + floordiv(jl, p.Ny) * p.k.kLy);
         f_yr = phase<CT>(floordiv(i, p.Nx) * p.k.kLx + floordiv(jr, p.Ny) * p.k.kLy);
     }
+    // the z-shift factor of a plane is one of e^{-ikLz}, 1, e^{+ikLz} (the queue reaches at
+    // most one period beyond the cell), so the three products with f_own are formed once
+    const CT fz_m = cmul(f_own, phase<CT>(-p.k.kLz)), fz_p = cmul(f_own, phase<CT>(p.k.kLz));
     auto zload = [&](int kr) {  // own column at unwrapped plane kr
         const CT val = __ldg(xc + own + (long)wrapz(kr, p.Nz) * NxNy);
-        return cmul(cmul(val, f_own), phase<CT>(floordiv(kr, p.Nz) * p.k.kLz));
+        const int d = floordiv(kr, p.Nz);
+        const CT f = d == 0 ? f_own
+                   : d == -1 ? fz_m
+                   : d == 1 ? fz_p : cmul(f_own, phase<CT>(d * p.k.kLz));
+        return cmul(val, f);
     };
     CT q[2 * R + 1];
 #pragma unroll
@@ -241,6 +248,82 @@ __device__ __forceinline__ void nl_apply_z_body(
     }
 }
 
+// Staged apply (as k_nl_apply_staged for real blocks): block = (chunk of kApplyChunkZ covered
+// points, CB columns); the alpha rows of the chunk's atoms are staged in shared memory, and
+// each entry's contribution is (e^{-i theta_g} Chi_j) alpha_j, with the phase-scaled Chi value
+// formed once per projector.
+constexpr int kApplyChunkZ = kApplyChunkPts;    // the chunking of the nonlocal upload
+constexpr size_t kZStageMax = 96 * 1024;         // staged rows must fit this (bytes)
+template <typename CT, int CB, int NPMAX>
+__device__ __forceinline__ void nl_apply_z_staged_body(
+    int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+    const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+    const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
+    const int *__restrict__ chunk_rows, const double *__restrict__ chi,
+    const double2 *__restrict__ img_phase, int ncol, const CT *__restrict__ alpha, long lda,
+    double scale, CT *__restrict__ out, long ldo, int c, int n0, CT *S)
+{
+    using RT = typename Real<CT>::type;
+    const int cidx = c * kApplyChunkZ + threadIdx.x;
+    const bool live = cidx < ncov;
+    const long p = live ? cov_pt[cidx] : 0;
+    CT ov[CB];
+#pragma unroll
+    for (int q = 0; q < CB; q++)
+        ov[q] = (live && n0 + q < ncol) ? out[(long)(n0 + q) * ldo + p] : CT{0, 0};
+    const int r0 = chunk_row_ptr[c], nr = chunk_row_ptr[c + 1] - r0;
+    for (int e = threadIdx.x; e < nr * CB; e += blockDim.x) {
+        const int r = e / CB, cc = e % CB;
+        S[e] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : CT{0, 0};
+    }
+    __syncthreads();
+    if (!live) return;
+    const int e0 = cov_ptr[cidx], e1 = cov_ptr[cidx + 1];
+    CT acc[CB];
+#pragma unroll
+    for (int q = 0; q < CB; q++) acc[q] = CT{0, 0};
+    for (int e = e0; e < e1; e++) {
+        const int4 meta = ent_meta[e];
+        const int np = meta.y, ndc = meta.z;
+        const double *__restrict__ ch = chi + ent_chi[e];
+        const CT *srow = S + (long)ent_slot[e] * CB;
+        const double2 ph = img_phase[meta.w];  // e^{-i theta} = (cos, -sin)
+#pragma unroll
+        for (int j = 0; j < NPMAX; j++) {
+            if (j >= np) break;
+            const double cv = __ldg(ch + (long)j * ndc);
+            const CT t{(RT)(cv * ph.x), (RT)(-cv * ph.y)};
+#pragma unroll
+            for (int q = 0; q < CB; q++) acc[q] = cadd(acc[q], cmul(t, srow[j * CB + q]));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < CB; q++)
+        if (n0 + q < ncol)
+            out[(long)(n0 + q) * ldo + p] = cadd(ov[q], cscale(acc[q], (RT)scale));
+}
+
+template <typename CT>
+__host__ __device__ constexpr int zapply_cb() { return sizeof(CT) == 16 ? 4 : 8; }
+
+template <typename CT, int NPMAX>
+__global__ void __launch_bounds__(kApplyChunkZ)
+    k_nl_apply_z_staged(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+                        const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+                        const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
+                        const int *__restrict__ chunk_rows, const double *__restrict__ chi,
+                        const double2 *__restrict__ img_phase, int ncol,
+                        const CT *__restrict__ alpha, long lda, double scale,
+                        CT *__restrict__ out, long ldo)
+{
+    extern __shared__ __align__(16) unsigned char zsmem[];
+    constexpr int CB = zapply_cb<CT>();
+    nl_apply_z_staged_body<CT, CB, NPMAX>(ncov, cov_pt, cov_ptr, ent_chi, ent_meta, ent_slot,
+                                          chunk_row_ptr, chunk_rows, chi, img_phase, ncol,
+                                          alpha, lda, scale, out, ldo, blockIdx.x,
+                                          blockIdx.y * CB, reinterpret_cast<CT *>(zsmem));
+}
+
 template <typename CT, int NPMAX>
 __global__ void __launch_bounds__(256)
     k_nl_apply_z(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
@@ -324,6 +407,29 @@ __global__ void __launch_bounds__(256)
     nl_project_z_body<CT, MAXJ>(img_atom, img_ndc, img_off, img_chi_off, grid_pos, chi,
                                 ip_displ, gamma, B.phase, B.ncol, B.buf[in_sel], B.ld[in_sel],
                                 B.alpha, B.ncol, dV, blockIdx.x, bc.y);
+}
+
+// staged, grouped: grid (chunk, column block, block); blocks with fewer columns return early
+template <typename CT, int NPMAX>
+__global__ void __launch_bounds__(kApplyChunkZ)
+    k_nl_apply_zb_staged(const BBlock<CT> *__restrict__ blocks, const BCoef *__restrict__ coef,
+                         int m, int deg, int out_sel, int ncov, const int *__restrict__ cov_pt,
+                         const int *__restrict__ cov_ptr, const long *__restrict__ ent_chi,
+                         const int4 *__restrict__ ent_meta, const int *__restrict__ ent_slot,
+                         const int *__restrict__ chunk_row_ptr,
+                         const int *__restrict__ chunk_rows, const double *__restrict__ chi)
+{
+    extern __shared__ __align__(16) unsigned char zsmem[];
+    constexpr int CB = zapply_cb<CT>();
+    const BBlock<CT> &B = blocks[blockIdx.z];
+    const int n0 = blockIdx.y * CB;
+    if (n0 >= B.ncol) return;  // uniform per thread block
+    const double scale = coef[(long)blockIdx.z * m + deg].s1;
+    nl_apply_z_staged_body<CT, CB, NPMAX>(ncov, cov_pt, cov_ptr, ent_chi, ent_meta, ent_slot,
+                                          chunk_row_ptr, chunk_rows, chi, B.phase, B.ncol,
+                                          B.alpha, B.ncol, scale, B.buf[out_sel],
+                                          B.ld[out_sel], blockIdx.x, n0,
+                                          reinterpret_cast<CT *>(zsmem));
 }
 
 // grid (covered-point chunk, block)
@@ -490,13 +596,32 @@ static int nonlocal_z(sgpu_ctx *ctx, int ncol, const CT *x, long ldx, CT *out, l
     }
     {
         ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
-        const int blocks = (nl.ncov + 255) / 256;
-        if (nl.max_np <= 9)
-            k_nl_apply_z<CT, 9><<<blocks, 256, 0, st>>>(nl.ncov, nl.cov_pt, nl.cov_ptr,
-                nl.ent_chi, nl.ent_meta, nl.chi64, ks->img_phase, ncol, alpha, lda, scale, out, ldo);
-        else
-            k_nl_apply_z<CT, 18><<<blocks, 256, 0, st>>>(nl.ncov, nl.cov_pt, nl.cov_ptr,
-                nl.ent_chi, nl.ent_meta, nl.chi64, ks->img_phase, ncol, alpha, lda, scale, out, ldo);
+        constexpr int CB = zapply_cb<CT>();
+        const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * CB;
+        if (nl.nchunk > 0 && stage <= kZStageMax) {
+            const dim3 sg(nl.nchunk, (ncol + CB - 1) / CB);
+            auto launch = [&](auto kern) -> int {
+                SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)std::max<size_t>(stage, 16)));
+                kern<<<sg, kApplyChunkZ, std::max<size_t>(stage, 16), st>>>(
+                    nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.ent_slot,
+                    nl.chunk_row_ptr, nl.chunk_rows, nl.chi64, ks->img_phase, ncol, alpha, lda,
+                    scale, out, ldo);
+                return SGPU_OK;
+            };
+            if (nl.max_np <= 9)
+                SGPU_TRY(launch(k_nl_apply_z_staged<CT, 9>));
+            else
+                SGPU_TRY(launch(k_nl_apply_z_staged<CT, 18>));
+        } else {
+            const int blocks = (nl.ncov + 255) / 256;
+            if (nl.max_np <= 9)
+                k_nl_apply_z<CT, 9><<<blocks, 256, 0, st>>>(nl.ncov, nl.cov_pt, nl.cov_ptr,
+                    nl.ent_chi, nl.ent_meta, nl.chi64, ks->img_phase, ncol, alpha, lda, scale, out, ldo);
+            else
+                k_nl_apply_z<CT, 18><<<blocks, 256, 0, st>>>(nl.ncov, nl.cov_pt, nl.cov_ptr,
+                    nl.ent_chi, nl.ent_meta, nl.chi64, ks->img_phase, ncol, alpha, lda, scale, out, ldo);
+        }
     }
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
@@ -691,6 +816,18 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
     cs.zlen = (ctx->Nz + nslab - 1) / nslab;
     const long maxw = 65535 / nslab;
     const size_t abytes = has_nl ? sizeof(CT) * (size_t)nl.ntot * totcols : 0;
+    int maxcol = 0;
+    for (int b = 0; b < nblk; b++) maxcol = std::max(maxcol, blk[b].ncol);
+    if (has_nl) {  // shared-memory size of the staged apply, set before any capture
+        const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * zapply_cb<CT>();
+        if (nl.nchunk > 0 && stage <= kZStageMax) {
+            const int sm = (int)std::max<size_t>(stage, 16);
+            SGPU_CUDA_TRY(cudaFuncSetAttribute(k_nl_apply_zb_staged<CT, 9>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+            SGPU_CUDA_TRY(cudaFuncSetAttribute(k_nl_apply_zb_staged<CT, 18>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        }
+    }
 
     auto issue = [&]() -> int {
         int cur = route ? 2 : 1, prev = 0;  // buffer ids: 0 X, 1 Y, 2 scratch
@@ -730,13 +867,28 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
             }
             if (has_nl) {
                 ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
-                const dim3 ag((nl.ncov + 255) / 256, nblk);
-                if (nl.max_np <= 9)
-                    k_nl_apply_zb<CT, 9><<<ag, 256, 0, st>>>(dB, dC, m, j, out, nl.ncov,
-                        nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.chi64);
-                else
-                    k_nl_apply_zb<CT, 18><<<ag, 256, 0, st>>>(dB, dC, m, j, out, nl.ncov,
-                        nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.chi64);
+                constexpr int CB = zapply_cb<CT>();
+                const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * CB;
+                if (nl.nchunk > 0 && stage <= kZStageMax) {
+                    const dim3 sg(nl.nchunk, (unsigned)((maxcol + CB - 1) / CB), nblk);
+                    const size_t sm = std::max<size_t>(stage, 16);
+                    if (nl.max_np <= 9)
+                        k_nl_apply_zb_staged<CT, 9><<<sg, kApplyChunkZ, sm, st>>>(
+                            dB, dC, m, j, out, nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi,
+                            nl.ent_meta, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows, nl.chi64);
+                    else
+                        k_nl_apply_zb_staged<CT, 18><<<sg, kApplyChunkZ, sm, st>>>(
+                            dB, dC, m, j, out, nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi,
+                            nl.ent_meta, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows, nl.chi64);
+                } else {
+                    const dim3 ag((nl.ncov + 255) / 256, nblk);
+                    if (nl.max_np <= 9)
+                        k_nl_apply_zb<CT, 9><<<ag, 256, 0, st>>>(dB, dC, m, j, out, nl.ncov,
+                            nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.chi64);
+                    else
+                        k_nl_apply_zb<CT, 18><<<ag, 256, 0, st>>>(dB, dC, m, j, out, nl.ncov,
+                            nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.chi64);
+                }
                 ctx->launches++;
             }
         }

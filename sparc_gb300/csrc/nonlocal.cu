@@ -27,7 +27,7 @@ namespace {
 
 constexpr int kProjThreads = 256;
 constexpr int kSegPts = 512;  // points of one image handled by one projection block
-constexpr int kApplyChunk = 128;   // covered points per block of the staged apply
+constexpr int kApplyChunk = kApplyChunkPts;   // covered points per block of the staged apply
 constexpr size_t kApplyStageMax = 96 * 1024;  // staged alpha rows must fit this (bytes)
 
 template <typename T, int CB>

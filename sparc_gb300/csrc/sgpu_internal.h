@@ -15,6 +15,7 @@
 namespace sgpu {
 
 constexpr int kMaxFDn = 6;  // the library is specialised for FD order 12 (radius 6)
+constexpr int kApplyChunkPts = 128;  // covered points per chunk of the staged nonlocal apply
 
 // thread-local error text, returned by sgpu_last_error()
 void set_error(const std::string &msg);
