@@ -169,6 +169,16 @@ int sgpu_ChebyshevFiltering_kpt(sgpu_ctx *ctx, int spin, const double *k, double
 int sgpu_Project_Hamiltonian(sgpu_ctx *ctx, int spin, const double *Y, int ldi, double *HY,
                              int ldo, int ncol, double *Hp, double *Mp);
 
+/* The Cholesky-orthonormalising variant: Mp = Yᵀ Y, Mp = Rᵀ R, Y <- Y R^{-1} (Y is
+ * overwritten by the orthonormal block), HY = H Y, Hp = Yᵀ HY. Replaces
+ * DP_Project_Hamiltonian_std (src/eigenSolver.c:1088-1252). */
+int sgpu_Project_Hamiltonian_std(sgpu_ctx *ctx, int spin, double *Y, int ldi, double *HY,
+                                 int ldo, int ncol, double *Hp);
+
+/* Hp q = lambda q (upper triangle referenced); Hp becomes Q. The standard-eigenproblem branch
+ * of DP_Solve_Generalized_EigenProblem (LAPACKE_dsyevd, src/eigenSolver.c:1318-1321). */
+int sgpu_Solve_Standard_EigenProblem(sgpu_ctx *ctx, int Ns, double *Hp, double *lambda);
+
 /* Hp q = lambda Mp q for the Ns x Ns pencil (upper triangles referenced). On return Hp holds
  * the eigenvectors Q (column-major), lambda the eigenvalues in ascending order, and Mp its
  * Cholesky factor. Replaces DP_Solve_Generalized_EigenProblem (src/eigenSolver.c:1262),
@@ -325,7 +335,9 @@ typedef struct {
                                    (also left early when the FP32 error stops falling) */
     int graded_tail;            /* mixed mode after the switch: 0 = plain FP64 CheFSI; 1 = FP32
                                    filter whose last tail_fp64_degrees degrees run in FP64,
-                                   with the Rayleigh-Ritz step in FP64 */
+                                   with the Rayleigh-Ritz step in FP64; 2 = FP32 filter, Cholesky
+                                   orthonormalisation with an FP64 Gram matrix (two passes),
+                                   standard eigenproblem on FP32 products */
     int tail_fp64_degrees;      /* 0 .. cheb_degree-1 (graded_tail = 1) */
     unsigned long long seed;    /* initial orbitals and Lanczos start vector */
     int verbose;

@@ -34,6 +34,7 @@ EXPORTED = [
     "sgpu_ChebyshevFiltering_batched", "sgpu_set_grid_coeffs", "sgpu_density_descriptors",
     "sgpu_mlp_create", "sgpu_mlp_destroy", "sgpu_mlp_nparam", "sgpu_mlp_get", "sgpu_mlp_set",
     "sgpu_mlp_forward", "sgpu_mlp_loss_grad", "sgpu_mlp_zero_grad", "sgpu_mlp_adam_step",
+    "sgpu_Project_Hamiltonian_std", "sgpu_Solve_Standard_EigenProblem",
 ]
 
 
@@ -350,6 +351,18 @@ class Context:
     def Solve_Generalized_EigenProblem(self, Hp, Mp, lam):
         _check(lib().sgpu_Solve_Generalized_EigenProblem(self._h, int(Hp.shape[0]), _ptr(Hp),
                                                          _ptr(Mp), _ptr(lam)))
+        return Hp, lam
+
+    def Project_Hamiltonian_std(self, Y, HY, Hp, spin=0):
+        """Y is overwritten by its Cholesky-orthonormalised block."""
+        ncol, ld = self._ncol_ld(Y)
+        _check(lib().sgpu_Project_Hamiltonian_std(self._h, int(spin), _ptr(Y), ld, _ptr(HY),
+                                                  ld, ncol, _ptr(Hp)))
+        return Y, HY, Hp
+
+    def Solve_Standard_EigenProblem(self, Hp, lam):
+        _check(lib().sgpu_Solve_Standard_EigenProblem(self._h, int(Hp.shape[0]), _ptr(Hp),
+                                                      _ptr(lam)))
         return Hp, lam
 
     def Subspace_Rotation(self, Y, Q, X):

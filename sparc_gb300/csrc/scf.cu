@@ -286,6 +286,76 @@ int sgpu_Project_Hamiltonian(sgpu_ctx *ctx, int spin, const double *Y, int ldi, 
     return SGPU_OK;
 }
 
+int sgpu_Project_Hamiltonian_std(sgpu_ctx *ctx, int spin, double *Y, int ldi, double *HY,
+                                 int ldo, int ncol, double *Hp)
+{
+    SGPU_TRY(check(ctx));
+    if (ncol <= 0 || ldi < ctx->Nd || ldo < ctx->Nd || !Y || !HY || !Hp) {
+        set_error("Project_Hamiltonian_std: need ncol > 0, arrays and leading dimensions >= Nd");
+        return SGPU_ERR_ARG;
+    }
+    double *dY, *dHY, *dHp;
+    const bool hy = !is_device_ptr(Y), hh = !is_device_ptr(HY);
+    long ly = ldi, lh = ldo;
+    if (hy) {
+        SGPU_TRY(ws_get(ctx, WS_STAGE_A, sizeof(double) * (size_t)ctx->Nd * ncol, (void **)&dY));
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(dY, sizeof(double) * ctx->Nd, Y, sizeof(double) * ldi,
+                                        sizeof(double) * ctx->Nd, ncol, cudaMemcpyHostToDevice,
+                                        ctx->stream));
+        ly = ctx->Nd;
+    } else {
+        dY = Y;
+    }
+    if (hh) {
+        SGPU_TRY(ws_get(ctx, WS_STAGE_B, sizeof(double) * (size_t)ctx->Nd * ncol, (void **)&dHY));
+        lh = ctx->Nd;
+    } else {
+        dHY = HY;
+    }
+    const long n2 = (long)ncol * ncol;
+    SGPU_TRY(stage_vec(ctx, WS_SCF, Hp, n2, &dHp));
+    SGPU_TRY(cholqr_f64(ctx, ncol, dY, ly, ctx->stream));
+    SGPU_TRY(hamiltonian_dev<double>(ctx, spin, ncol, 0.0, dY, ly, dHY, lh, 1.0, 0.0, nullptr, 0,
+                                     ctx->stream));
+    {
+        SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, ctx->stream));
+        const double one = 1.0, zero = 0.0;
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, ctx->stream);
+        SGPU_CUBLAS_TRY(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol,
+                                    (int)ctx->Nd, &one, dY, (int)ly, dHY, (int)lh, &zero, dHp,
+                                    ncol));
+    }
+    if (hy)
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(Y, sizeof(double) * ldi, dY, sizeof(double) * ly,
+                                        sizeof(double) * ctx->Nd, ncol, cudaMemcpyDeviceToHost,
+                                        ctx->stream));
+    if (hh)
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(HY, sizeof(double) * ldo, dHY, sizeof(double) * lh,
+                                        sizeof(double) * ctx->Nd, ncol, cudaMemcpyDeviceToHost,
+                                        ctx->stream));
+    SGPU_TRY(unstage_vec(ctx, dHp, Hp, n2));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_Solve_Standard_EigenProblem(sgpu_ctx *ctx, int Ns, double *Hp, double *lambda)
+{
+    SGPU_TRY(check(ctx));
+    if (Ns <= 0 || !Hp || !lambda) {
+        set_error("Solve_Standard_EigenProblem: bad arguments");
+        return SGPU_ERR_ARG;
+    }
+    const long n2 = (long)Ns * Ns;
+    double *dH, *dl;
+    SGPU_TRY(stage_vec(ctx, WS_SCF, Hp, n2, &dH));
+    SGPU_TRY(stage_vec(ctx, WS_SCF2, is_device_ptr(lambda) ? lambda : nullptr, Ns, &dl));
+    SGPU_TRY(standard_eig(ctx, Ns, dH, dl, ctx->stream));
+    SGPU_TRY(unstage_vec(ctx, dH, Hp, n2));
+    SGPU_TRY(unstage_vec(ctx, dl, lambda, Ns));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
 int sgpu_Solve_Generalized_EigenProblem(sgpu_ctx *ctx, int Ns, double *Hp, double *Mp,
                                         double *lambda)
 {
@@ -494,9 +564,11 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         set_error("sgpu_scf: precision must be SGPU_PREC_FP64 or SGPU_PREC_FP32");
         return SGPU_ERR_ARG;
     }
-    if (prm->graded_tail &&
-        (prm->tail_fp64_degrees < 0 || prm->tail_fp64_degrees >= prm->cheb_degree)) {
-        set_error("sgpu_scf: tail_fp64_degrees must lie in [0, cheb_degree)");
+    if (prm->graded_tail < 0 || prm->graded_tail > 2 ||
+        (prm->graded_tail == 1 &&
+         (prm->tail_fp64_degrees < 0 || prm->tail_fp64_degrees >= prm->cheb_degree))) {
+        set_error("sgpu_scf: graded_tail must be 0, 1 or 2, and tail_fp64_degrees in "
+                  "[0, cheb_degree) for 1");
         return SGPU_ERR_ARG;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -596,6 +668,13 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 // HY into X (the reference reuses Xorb for HY), then project in FP32 products
                 SGPU_TRY(hamiltonian_dev<float>(ctx, 0, Ns, 0.0, Y32, N, X32, N, 1.0, 0.0, nullptr, 0, st));
                 SGPU_TRY(project_f32(ctx, Ns, Y32, N, X32, N, d_Hp, d_Mp, st));
+            } else if (graded && prm->graded_tail == 2) {
+                // FP32 filter, Cholesky QR with an FP64 Gram matrix, then the standard
+                // eigenproblem on FP32 products of the orthonormal block
+                SGPU_TRY(chebyshev_dev<float>(ctx, 0, X32, N, Y32, N, Ns, m, cutoff, eigmax, eigmin, st));
+                SGPU_TRY(cholqr2_f32(ctx, Ns, Y32, N, Y64, st));
+                SGPU_TRY(hamiltonian_dev<float>(ctx, 0, Ns, 0.0, Y32, N, X32, N, 1.0, 0.0, nullptr, 0, st));
+                SGPU_TRY(project_h_f32(ctx, Ns, Y32, N, X32, N, d_Hp, st));
             } else if (graded) {
                 SGPU_TRY(chebyshev_graded(ctx, 0, X32, Y32, X64, Y64, Ns, m,
                                           prm->tail_fp64_degrees, cutoff, eigmax, eigmin, st));
@@ -607,11 +686,15 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 SGPU_TRY(project_f64(ctx, Ns, Y64, N, X64, N, d_Hp, d_Mp, st));
             }
             SGPU_CUDA_TRY(cudaEventRecord(e1, st));
-            SGPU_TRY(generalized_eig(ctx, Ns, d_Hp, d_Mp, d_lam, st));
+            const bool cq = graded && prm->graded_tail == 2;  // orthonormal block: standard
+            if (cq)
+                SGPU_TRY(standard_eig(ctx, Ns, d_Hp, d_lam, st));
+            else
+                SGPU_TRY(generalized_eig(ctx, Ns, d_Hp, d_Mp, d_lam, st));
             float ms = 0.f;
             SGPU_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
             filter_ms += ms;
-            if (mixed) {
+            if (mixed || cq) {
                 SGPU_TRY(rotate_f32(ctx, Ns, Y32, N, d_Hp, X32, N, st));
             } else {
                 SGPU_TRY(rotate_f64(ctx, Ns, Y64, N, d_Hp, X64, N, st));
@@ -634,7 +717,7 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         std::vector<double> w(Ns);
         for (int n = 0; n < Ns; n++) w[n] = occfac * occ[n] / ctx->dV;
         SGPU_CUDA_TRY(cudaMemcpyAsync(d_w, w.data(), sizeof(double) * Ns, cudaMemcpyHostToDevice, st));
-        if (mixed)
+        if (mixed || (graded && prm->graded_tail == 2))
             SGPU_TRY(density_dev<float>(ctx, X32, N, Ns, d_w, d_rhoout, st));
         else
             SGPU_TRY(density_dev<double>(ctx, X64, N, Ns, d_w, d_rhoout, st));
