@@ -341,6 +341,9 @@ typedef struct {
     int tail_fp64_degrees;      /* 0 .. cheb_degree-1 (graded_tail = 1) */
     unsigned long long seed;    /* initial orbitals and Lanczos start vector */
     int verbose;
+    double *history;            /* optional host array of 3 * maxit_scf: per SCF iteration the
+                                   free energy, the SCF error and the seconds since the call
+                                   began (NULL: not recorded) */
 } sgpu_scf_params;
 
 typedef struct {
@@ -410,6 +413,11 @@ int sgpu_autotune(sgpu_ctx *ctx, int ncol, int *variant, double *ms);
 
 /* Fix the FP32 stencil variant (0..4) without timing. */
 int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
+
+/* Fix the form of the real nonlocal apply (0: one thread per covered point over all column
+ * blocks; 1: alpha rows staged in shared memory per chunk of covered points); sgpu_autotune
+ * times both. Same results either way. */
+int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
 
 /* ------------------------------------------------------------------- measurement */
 

@@ -35,6 +35,7 @@ EXPORTED = [
     "sgpu_mlp_create", "sgpu_mlp_destroy", "sgpu_mlp_nparam", "sgpu_mlp_get", "sgpu_mlp_set",
     "sgpu_mlp_forward", "sgpu_mlp_loss_grad", "sgpu_mlp_zero_grad", "sgpu_mlp_adam_step",
     "sgpu_Project_Hamiltonian_std", "sgpu_Solve_Standard_EigenProblem",
+    "sgpu_set_nonlocal_apply_variant",
 ]
 
 
@@ -75,7 +76,7 @@ class ScfParams(ctypes.Structure):
                 ("Esc", ctypes.c_double), ("precision", ctypes.c_int),
                 ("fp64_switch_error", ctypes.c_double), ("graded_tail", ctypes.c_int),
                 ("tail_fp64_degrees", ctypes.c_int), ("seed", ctypes.c_ulonglong),
-                ("verbose", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("history", ctypes.c_void_p)]
 
 
 class ScfResult(ctypes.Structure):
@@ -436,9 +437,18 @@ class Context:
         b = np.ascontiguousarray(b, dtype=np.float64)
         r0 = np.ascontiguousarray(rho_init, dtype=np.float64)
         rc_ = None if rho_core is None else np.ascontiguousarray(rho_core, dtype=np.float64)
-        _check(lib().sgpu_scf(self._h, ctypes.byref(params), _ptr(b), _ptr(r0), _ptr(rc_),
-                              _ptr(rho), _ptr(lam), _ptr(occ), ctypes.byref(res)))
-        return res.as_dict(), rho, lam, occ
+        hist = np.full(3 * max(1, params.maxit_scf), np.nan)
+        params.history = hist.ctypes.data
+        try:
+            _check(lib().sgpu_scf(self._h, ctypes.byref(params), _ptr(b), _ptr(r0), _ptr(rc_),
+                                  _ptr(rho), _ptr(lam), _ptr(occ), ctypes.byref(res)))
+        finally:
+            params.history = None
+        out = res.as_dict()
+        h = hist.reshape(-1, 3)[:out["scf_iters"]]
+        out["history"] = {"Etot": h[:, 0].tolist(), "scf_error": h[:, 1].tolist(),
+                          "time_s": h[:, 2].tolist()}
+        return out, rho, lam, occ
 
     def autotune(self, ncol=64):
         """Time the FP32 stencil variants; returns (chosen variant, per-variant ms)."""
@@ -449,6 +459,9 @@ class Context:
 
     def set_stencil_variant(self, variant):
         _check(lib().sgpu_set_stencil_variant(self._h, int(variant)))
+
+    def set_nonlocal_apply_variant(self, variant):
+        _check(lib().sgpu_set_nonlocal_apply_variant(self._h, int(variant)))
 
     def profile_enable(self, on=True):
         _check(lib().sgpu_profile_enable(self._h, int(bool(on))))

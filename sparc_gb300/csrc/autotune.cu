@@ -1,7 +1,9 @@
-// Autotuner for the FP32 stencil kernel: times each tile / register-blocking variant of the
-// fused stencil + Chebyshev update on scratch blocks of the context's grid and keeps the
-// fastest. All variants compute the same IEEE operation sequence per point, so the choice
-// changes speed only, never results.
+// Autotuner for the FP32 filter kernels: times each tile / register-blocking variant of the
+// fused stencil + Chebyshev update, and each form of the nonlocal apply (per point over all
+// column blocks, or alpha rows staged per chunk of covered points), on scratch blocks of the
+// context's grid and projector set, and keeps the fastest of each. The stencil variants
+// compute the same IEEE operation sequence per point, and so do the two apply forms, so the
+// choice changes speed only, never results.
 #include <vector>
 
 #include "sgpu_internal.h"
@@ -56,8 +58,41 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
         if (ms) ms[v] = tmin;
         if (tmin < best_ms) { best_ms = tmin; *best = v; }
     }
-    ctx->prof_on = prof;
     ctx->stencil_variant = rc == SGPU_OK ? *best : saved;
+    // nonlocal apply: per-point form vs the form with alpha rows staged per chunk
+    if (rc == SGPU_OK && ctx->has_nl && ctx->nl.ntot > 0 && ctx->nl.ncov > 0) {
+        const long lda = nonlocal_alpha_ld(ncol, 4);
+        float *alpha = nullptr;
+        if (cudaMallocAsync(&alpha, sizeof(float) * (size_t)ctx->nl.ntot * lda, st) != cudaSuccess ||
+            cudaMemsetAsync(alpha, 0, sizeof(float) * (size_t)ctx->nl.ntot * lda, st) != cudaSuccess) {
+            rc = SGPU_ERR_CUDA;
+        } else {
+            const int saved_a = ctx->nl_apply_variant;
+            float tbest = 1e30f;
+            int abest = saved_a;
+            for (int v = 0; v < 2 && rc == SGPU_OK; v++) {
+                ctx->nl_apply_variant = v;
+                float t = 0.f, tmin = 1e30f;
+                for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
+                    if (cudaEventRecord(ctx->ev0, st) != cudaSuccess) { rc = SGPU_ERR_CUDA; break; }
+                    if ((rc = launch_nonlocal_apply<float>(ctx, ncol, alpha, lda, 1.0, Y, Nd,
+                                                           st)) != SGPU_OK)
+                        break;
+                    if (cudaEventRecord(ctx->ev1, st) != cudaSuccess ||
+                        cudaEventSynchronize(ctx->ev1) != cudaSuccess ||
+                        cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) != cudaSuccess) {
+                        rc = SGPU_ERR_CUDA;
+                        break;
+                    }
+                    if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
+                }
+                if (rc == SGPU_OK && tmin < tbest) { tbest = tmin; abest = v; }
+            }
+            ctx->nl_apply_variant = rc == SGPU_OK ? abest : saved_a;
+            cudaFreeAsync(alpha, st);
+        }
+    }
+    ctx->prof_on = prof;
     cudaFreeAsync(buf, st);
     if (cudaStreamSynchronize(st) != cudaSuccess && rc == SGPU_OK) rc = SGPU_ERR_CUDA;
     if (rc == SGPU_ERR_CUDA) set_error("autotune: CUDA error while timing stencil variants");
@@ -78,6 +113,16 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant)
     }
     ctx->stencil_variant = variant;
     ctx->stencil_tuned = true;
+    return SGPU_OK;
+}
+
+int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant)
+{
+    if (!ctx || variant < 0 || variant > 1) {
+        set_error("sgpu_set_nonlocal_apply_variant: variant must be 0 or 1");
+        return SGPU_ERR_ARG;
+    }
+    ctx->nl_apply_variant = variant;
     return SGPU_OK;
 }
 

@@ -325,7 +325,7 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
     constexpr int VW = sizeof(T) == 4 ? 4 : 2;
     constexpr int SCB = sizeof(T) == 4 ? 32 : 16;  // columns per block of the staged form
     const size_t stage = sizeof(T) * (size_t)nl.max_chunk_rows * SCB;
-    if (nl.nchunk > 0 && stage <= kApplyStageMax) {
+    if (ctx->nl_apply_variant == 1 && nl.nchunk > 0 && stage <= kApplyStageMax) {
         const dim3 sg(nl.nchunk, (ncol + SCB - 1) / SCB);
         ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
 #define SGPU_STAGED(NPM)                                                                     \

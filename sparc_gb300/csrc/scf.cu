@@ -757,6 +757,12 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         }
         // ---- SCF error, mixing, new potential
         SGPU_TRY(scf_error_dev(ctx, d_rhoout, xk, &error, st));
+        if (prm->history && scf < prm->maxit_scf) {
+            prm->history[3 * scf] = Etot;
+            prm->history[3 * scf + 1] = error;
+            prm->history[3 * scf + 2] =
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
         SGPU_TRY(mixing_step(ctx, scf, d_rhoout, st));
         SGPU_CUDA_TRY(cudaMemcpyAsync(d_rho, d_rhoout, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         SGPU_TRY(poisson_dev(ctx, d_rho, d_b, d_phi, prm->tol_poisson, prm->maxit_poisson, &pits, st));

@@ -137,6 +137,7 @@ struct sgpu_ctx {
     sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
     int stencil_variant = 0;   // FP32 stencil kernel variant (autotune.cu)
     bool stencil_tuned = false;
+    int nl_apply_variant = 0;  // real nonlocal apply: 0 per point over all columns, 1 staged
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on

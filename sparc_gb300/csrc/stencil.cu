@@ -133,10 +133,10 @@ template <int R, int BXP, int BY, int MINB>
 __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
     k_stencil_f32x2(const StencilParams<float> p)
 {
-    constexpr int Q = 2 * R + 2;  // ring: planes k-R .. k+R in use, k+R+1 in flight
+    constexpr int Q = 2 * R + 1;
     constexpr int W = BXP + 2 * R;
     static_assert(R % 2 == 0 && BXP % 2 == 0, "paired layout needs even radius and tile");
-    static_assert(Q == 14, "the unrolled z-loop below is written for radius 6");
+    static_assert(Q == 13, "the unrolled z-loop below is written for radius 6");
     __shared__ __align__(16) float s[2][BY + 2 * R][W];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BXP, y0 = blockIdx.y * BY;
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
 
     float2 q[Q];
 #pragma unroll
-    for (int m = 0; m <= 2 * R; m++) {
+    for (int m = 0; m < 2 * R; m++) {
         const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
         q[m] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl));
     }
@@ -201,8 +201,8 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
         if (k < ze) {                                                                            \
             const int b = k & 1;                                                                 \
             {                                                                                    \
-                const int pl = wrapi(k + R + 1, p.Nz) * NxNy;                                    \
-                q[((U) + 2 * R + 1) % Q] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl)); \
+                const int pl = wrapi(k + R, p.Nz) * NxNy;                                        \
+                q[((U) + 2 * R) % Q] = make_float2(__ldg(xc + own0 + pl), __ldg(xc + own1 + pl)); \
             }                                                                                    \
             const float2 cen = q[((U) + R) % Q];                                                 \
             *reinterpret_cast<float2 *>(&s[b][ty + R][R + 2 * tx]) = cen;                        \
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(BXP / 2 * BY, MINB)
     for (int kb = zs; kb < ze; kb += Q) {
         SGPU_F2_STEP(0) SGPU_F2_STEP(1) SGPU_F2_STEP(2) SGPU_F2_STEP(3) SGPU_F2_STEP(4)
         SGPU_F2_STEP(5) SGPU_F2_STEP(6) SGPU_F2_STEP(7) SGPU_F2_STEP(8) SGPU_F2_STEP(9)
-        SGPU_F2_STEP(10) SGPU_F2_STEP(11) SGPU_F2_STEP(12) SGPU_F2_STEP(13)
+        SGPU_F2_STEP(10) SGPU_F2_STEP(11) SGPU_F2_STEP(12)
     }
 #undef SGPU_F2_STEP
 }
@@ -317,11 +317,11 @@ template <int R, int BX, int BY, int MINB, bool VEC>
 __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     k_stencil_f32_b22(const StencilParams<float> p)
 {
-    // z-queue ring of Q = 2R+2 slots: planes k-R .. k+R are in use at plane k and plane
-    // k+R+1 is already in flight, so no plane's first use waits on its own load
-    constexpr int Q = 2 * R + 2;
+    // z-queue of Q = 2R+1 slots (planes k-R .. k+R). A 2R+2 ring that keeps plane k+R+1 in
+    // flight was measured slower: its extra registers cost a resident block per SM.
+    constexpr int Q = 2 * R + 1;
     constexpr int W = BX + 2 * R;
-    static_assert(Q == 14 && R % 2 == 0, "the unrolled z-loop below is written for radius 6");
+    static_assert(Q == 13 && R % 2 == 0, "the unrolled z-loop below is written for radius 6");
     __shared__ __align__(16) float s[2][BY + 2 * R][W];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
@@ -395,7 +395,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
 
     float2 qa[Q], qb[Q];  // z-queues of rows j0 and j0+1: slot of plane k-R+m is (U+m) % Q
 #pragma unroll
-    for (int m = 0; m <= 2 * R; m++) {
+    for (int m = 0; m < 2 * R; m++) {
         const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
         qa[m] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);
         qb[m] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);
@@ -420,9 +420,9 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
         if (k < ze) {                                                                            \
             const int b = k & 1;                                                                 \
             {                                                                                    \
-                const int pl = wrapi(k + R + 1, p.Nz) * NxNy;                                    \
-                qa[((U) + 2 * R + 1) % Q] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);  \
-                qb[((U) + 2 * R + 1) % Q] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);  \
+                const int pl = wrapi(k + R, p.Nz) * NxNy;                                        \
+                qa[((U) + 2 * R) % Q] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);      \
+                qb[((U) + 2 * R) % Q] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);      \
             }                                                                                    \
             const float2 ca = qa[((U) + R) % Q], cb = qb[((U) + R) % Q];                         \
             *reinterpret_cast<float2 *>(&s[b][2 * ty + R][R + 2 * tx]) = ca;                     \
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     for (int kb = zs; kb < ze; kb += Q) {
         SGPU_B22_STEP(0) SGPU_B22_STEP(1) SGPU_B22_STEP(2) SGPU_B22_STEP(3) SGPU_B22_STEP(4)
         SGPU_B22_STEP(5) SGPU_B22_STEP(6) SGPU_B22_STEP(7) SGPU_B22_STEP(8) SGPU_B22_STEP(9)
-        SGPU_B22_STEP(10) SGPU_B22_STEP(11) SGPU_B22_STEP(12) SGPU_B22_STEP(13)
+        SGPU_B22_STEP(10) SGPU_B22_STEP(11) SGPU_B22_STEP(12)
     }
 #undef SGPU_B22_STEP
     cp_async_wait_all();

@@ -212,9 +212,22 @@ def train(torch, net, descs, targs, dev, epochs=8, batch=65536, lr=2e-3, seed=0,
     return hist
 
 
+def energy_reached(history, e_conv, n_atom, tol=1e-5):
+    """(iterations, seconds) until the free energy per atom is within tol of e_conv and stays
+    there for the rest of the SCF (None if never)."""
+    e = np.asarray(history["Etot"]) / n_atom
+    ok = np.abs(e - e_conv) < tol
+    for i in range(len(e)):
+        if ok[i:].all():
+            return i + 1, float(history["time_s"][i])
+    return None, None
+
+
 def evaluate(torch, cs, net, indices, dev, precision=32, log=None, snap=si64_snapshot,
-             scf_kw=None):
-    """SCF iterations and time from rho_at and from the learned start, per snapshot."""
+             scf_kw=None, energy_tol=1e-5):
+    """Per snapshot and start (rho_at, learned): SCF iterations and time to TOL_SCF, and
+    iterations and time until the energy is within energy_tol Ha/atom of the converged one
+    (the converged energy of the rho_at start)."""
     out = []
     for idx in indices:
         L, pos, sigma, strain = snap(idx)
@@ -228,12 +241,35 @@ def evaluate(torch, cs, net, indices, dev, precision=32, log=None, snap=si64_sna
                                     rho_init=rho0)
             rec[tag] = dict(scf_iters=res["scf_iters"], time_s=res["time_s"] + t_pred,
                             converged=bool(res["converged"]),
-                            Etot_per_atom=res["Etot"] / cs.n_atom,
+                            Etot_per_atom=res["Etot"] / cs.n_atom, history=res["history"],
+                            predict_s=t_pred,
                             start_error=float(np.linalg.norm(rho0 - rho) / np.linalg.norm(rho)))
+        e_conv = rec["rho_at"]["Etot_per_atom"]
+        for tag in ("rho_at", "learned"):
+            it, ts = energy_reached(rec[tag]["history"], e_conv, cs.n_atom, energy_tol)
+            rec[tag]["iters_to_energy_tol"] = it
+            rec[tag]["time_to_energy_tol_s"] = None if ts is None else ts + rec[tag]["predict_s"]
+            del rec[tag]["history"]
         out.append(rec)
         if log:
             log(f"held-out {idx}: {rec['rho_at']['scf_iters']} -> {rec['learned']['scf_iters']} "
                 f"iterations")
+    return out
+
+
+def summarize(ev, mode):
+    """Means over the held-out snapshots of one evaluation mode."""
+    def col(tag, key):
+        return np.array([np.nan if r[tag][key] is None else r[tag][key] for r in ev], dtype=float)
+    dE = np.abs(col("rho_at", "Etot_per_atom") - col("learned", "Etot_per_atom"))
+    out = dict(scf_mode=mode, snapshots=len(ev))
+    for tag in ("rho_at", "learned"):
+        out[tag] = dict(mean_scf_iters=float(np.nanmean(col(tag, "scf_iters"))),
+                        mean_time_s=float(np.nanmean(col(tag, "time_s"))),
+                        mean_iters_to_1e-5=float(np.nanmean(col(tag, "iters_to_energy_tol"))),
+                        mean_time_to_1e-5_s=float(np.nanmean(col(tag, "time_to_energy_tol_s"))),
+                        mean_start_error=float(np.nanmean(col(tag, "start_error"))))
+    out["max_dE_per_atom_between_starts"] = float(np.nanmax(dE))
     return out
 
 
@@ -244,7 +280,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--out", default=None)
     ap.add_argument("--save", default=None)
-    ap.add_argument("--precision", type=int, default=32)
+    ap.add_argument("--load", default=None, help="evaluate a saved network instead of training")
+    ap.add_argument("--precision", type=int, default=32, help="SCF mode of the data generation")
+    ap.add_argument("--eval-modes", default="32,64", help="SCF modes of the evaluation")
+    ap.add_argument("--eval-count", type=int, default=None,
+                    help="held-out snapshots per evaluation mode (default: all)")
     args = ap.parse_args()
     import torch
     from .psp8 import load_tables
@@ -255,40 +295,38 @@ def main():
     L0, pos0, _, _ = si64_snapshot(0)
     cs = CellSystem((L0, L0, L0), (52, 52, 52), [("Si", pos0)], tab)
     ntrain = args.snapshots - args.test
-    t0 = time.perf_counter()
-    descs, targs, info = generate(torch, cs, list(range(ntrain)), dev, args.precision,
-                                  log=lambda s: print(s, flush=True))
-    t_gen = time.perf_counter() - t0
-    net = DensityMLP()
-    t0 = time.perf_counter()
-    hist = train(torch, net, descs, targs, dev, epochs=args.epochs,
-                 log=lambda s: print(s, flush=True))
-    t_train = time.perf_counter() - t0
-    del descs, targs
-    ev = evaluate(torch, cs, net, list(range(ntrain, args.snapshots)), dev, args.precision,
-                  log=lambda s: print(s, flush=True))
-    it_at = np.array([r["rho_at"]["scf_iters"] for r in ev])
-    it_ml = np.array([r["learned"]["scf_iters"] for r in ev])
-    t_at = np.array([r["rho_at"]["time_s"] for r in ev])
-    t_ml = np.array([r["learned"]["time_s"] for r in ev])
-    dE = np.array([abs(r["rho_at"]["Etot_per_atom"] - r["learned"]["Etot_per_atom"]) for r in ev])
     summary = dict(
         system="Si64 (2x2x2 diamond cells, a=20.52 Bohr +-3% strain, sigma 0.1-0.4 Bohr), "
                "52^3 grid, 160 states, LDA_PW, degree 20, TOL_SCF 1e-6",
-        train_snapshots=ntrain, test_snapshots=args.test, train_points=ntrain * 52 ** 3,
-        generation_s=round(t_gen, 1), training_s=round(t_train, 1), loss_history=hist,
-        mean_iters_rho_at=float(it_at.mean()), mean_iters_learned=float(it_ml.mean()),
-        mean_time_rho_at_s=float(t_at.mean()), mean_time_learned_s=float(t_ml.mean()),
-        mean_start_error_rho_at=float(np.mean([r["rho_at"]["start_error"] for r in ev])),
-        mean_start_error_learned=float(np.mean([r["learned"]["start_error"] for r in ev])),
-        max_dE_per_atom_between_starts=float(dE.max()), per_snapshot=ev,
-        scf_mode="mixed (FP32 then graded)" if args.precision == 32 else "FP64")
-    print(json.dumps({k: v for k, v in summary.items() if k != "per_snapshot"}), flush=True)
+        train_snapshots=ntrain, test_snapshots=args.test, train_points=ntrain * 52 ** 3)
+    if args.load:
+        net = DensityMLP.load(args.load)
+    else:
+        t0 = time.perf_counter()
+        descs, targs, info = generate(torch, cs, list(range(ntrain)), dev, args.precision,
+                                      log=lambda s: print(s, flush=True))
+        t_gen = time.perf_counter() - t0
+        net = DensityMLP()
+        t0 = time.perf_counter()
+        hist = train(torch, net, descs, targs, dev, epochs=args.epochs,
+                     log=lambda s: print(s, flush=True))
+        summary.update(generation_s=round(t_gen, 1), training_s=round(time.perf_counter() - t0, 1),
+                       loss_history=hist)
+        del descs, targs
+    held = list(range(ntrain, args.snapshots))[:args.eval_count]
+    evals = {}
+    for mode in (int(m) for m in args.eval_modes.split(",")):
+        ev = evaluate(torch, cs, net, held, dev, mode, log=lambda s: print(s, flush=True))
+        name = "mixed" if mode == 32 else "fp64"
+        summary[f"eval_{name}"] = summarize(ev, "mixed (FP32, then FP32 filter + FP64 "
+                                                "Rayleigh-Ritz)" if mode == 32 else "FP64")
+        evals[name] = ev
+    print(json.dumps(summary), flush=True)
     if args.out:
         with open(args.out, "w") as f:
-            json.dump(summary, f, indent=1)
+            json.dump(dict(summary, per_snapshot=evals), f, indent=1)
     if args.save:
-        net.save(args.save, meta={k: v for k, v in summary.items() if k != "per_snapshot"})
+        net.save(args.save, meta=summary)
 
 
 if __name__ == "__main__":

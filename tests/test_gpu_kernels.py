@@ -141,6 +141,27 @@ def test_fp32_stencil_variants_identical(gpu_available, shape):
     assert 0 <= best < 5 and np.all(ms > 0)
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_nonlocal_apply_forms_identical(gpu_available, dtype):
+    """The staged and the per-point nonlocal apply give bit-identical results."""
+    grid, nl, veff, rng = _random_case((30, 26, 22), seed=21, natom=7)
+    Nd = 30 * 26 * 22
+    ctx = make_ctx(grid, nl, veff)
+    x = rng.uniform(-1, 1, (37, Nd)).astype(dtype)  # not a multiple of any column block
+    outs = []
+    for v in (0, 1):
+        ctx.set_nonlocal_apply_variant(v)
+        if dtype == np.float64:
+            h = np.zeros_like(x)
+            ctx.Hamiltonian_vectors_mult(0.1, x, h)
+            outs.append(h)
+        else:
+            X = x.copy(); Y = np.zeros_like(x)
+            ctx.ChebyshevFiltering_f32(X, Y, 3, 0.5, 50.0, -1.0)
+            outs.append(Y)
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
 def test_device_pointers_match_host(gpu_available):
     import torch
     grid, nl, veff, rng = _random_case((24, 20, 16), seed=9)
