@@ -266,8 +266,8 @@ def summarize(ev, mode):
     for tag in ("rho_at", "learned"):
         out[tag] = dict(mean_scf_iters=float(np.nanmean(col(tag, "scf_iters"))),
                         mean_time_s=float(np.nanmean(col(tag, "time_s"))),
-                        mean_iters_to_1e-5=float(np.nanmean(col(tag, "iters_to_energy_tol"))),
-                        mean_time_to_1e-5_s=float(np.nanmean(col(tag, "time_to_energy_tol_s"))),
+                        mean_iters_to_energy_tol=float(np.nanmean(col(tag, "iters_to_energy_tol"))),
+                        mean_time_to_energy_tol_s=float(np.nanmean(col(tag, "time_to_energy_tol_s"))),
                         mean_start_error=float(np.nanmean(col(tag, "start_error"))))
     out["max_dE_per_atom_between_starts"] = float(np.nanmax(dE))
     return out

@@ -37,3 +37,14 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(sparc_gb300, "_lib", None)
     with pytest.raises(sparc_gb300.SgpuError):
         sparc_gb300.lib()
+
+
+def test_host_modules_import():
+    """Every host-side module of the package and the bench import on a machine without a GPU."""
+    import importlib
+    for mod in ("sparc_gb300.setup", "sparc_gb300.psp8", "sparc_gb300.learned_density",
+                "sparc_gb300.synthetic"):
+        importlib.import_module(mod)
+    import py_compile
+    for fn in ("bench.py", "__graft_entry__.py"):
+        py_compile.compile(os.path.join(ROOT, fn), doraise=True)
