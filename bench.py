@@ -383,7 +383,9 @@ def main():
     variant, variant_ms = ctx.autotune(ncol=min(ncol, 64))
     kernel_name = ["k_stencil_f32x2<32x16>", "k_stencil_f32_b22<32x16>",
                    "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
-                   "k_stencil_f32_b22<32x16, 3 blocks/SM>"][variant]
+                   "k_stencil_f32_b22<32x16, 3 blocks/SM>",
+                   "k_stencil_f32_ring<32x16, 1 plane ahead>",
+                   "k_stencil_f32_ring<32x16, 2 planes ahead>"][variant]
 
     gen = torch.Generator(device=dev)
     gen.manual_seed(1234 + rank)

@@ -335,9 +335,7 @@ typedef struct {
                                    (also left early when the FP32 error stops falling) */
     int graded_tail;            /* mixed mode after the switch: 0 = plain FP64 CheFSI; 1 = FP32
                                    filter whose last tail_fp64_degrees degrees run in FP64,
-                                   with the Rayleigh-Ritz step in FP64; 2 = FP32 filter, Cholesky
-                                   orthonormalisation with an FP64 Gram matrix (two passes),
-                                   standard eigenproblem on FP32 products */
+                                   with the Rayleigh-Ritz step in FP64 */
     int tail_fp64_degrees;      /* 0 .. cheb_degree-1 (graded_tail = 1) */
     unsigned long long seed;    /* initial orbitals and Lanczos start vector */
     int verbose;
@@ -404,19 +402,23 @@ int sgpu_mlp_adam_step(sgpu_mlp *net, float lr, float beta1, float beta2, float 
 
 /* ------------------------------------------------------------------- kernel tuning */
 
+/* Number of FP32 stencil kernel variants (tile shape, register blocking, plane ring). */
+#define SGPU_STENCIL_VARIANTS 7
+
 /* Time every FP32 stencil kernel variant (tile shape and register blocking) on ncol scratch
  * columns of this context's grid, keep the fastest for later calls, and return its index in
- * *variant and per-variant milliseconds in ms (5 values; may be NULL). All variants give
- * identical results. sgpu_scf runs this once per context before its first FP32 filter.
- * No counterpart in the reference. */
+ * *variant and per-variant milliseconds in ms (SGPU_STENCIL_VARIANTS values; may be NULL).
+ * All variants give identical results. sgpu_scf runs this once per context before its first
+ * FP32 filter. No counterpart in the reference. */
 int sgpu_autotune(sgpu_ctx *ctx, int ncol, int *variant, double *ms);
 
-/* Fix the FP32 stencil variant (0..4) without timing. */
+/* Fix the FP32 stencil variant (0 .. SGPU_STENCIL_VARIANTS-1) without timing. */
 int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
 
 /* Fix the form of the real nonlocal apply (0: one thread per covered point over all column
- * blocks; 1: alpha rows staged in shared memory per chunk of covered points); sgpu_autotune
- * times both. Same results either way. */
+ * blocks; 1: alpha rows staged in shared memory per chunk of covered points; 2: as 0 with the
+ * point's Chi values loaded once before the column loop); sgpu_autotune times all three.
+ * Same results whichever is used. */
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
 
 /* ------------------------------------------------------------------- measurement */

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "libsparc_gpu.so")
 SGPU_OK = 0
 SGPU_PREC_FP64 = 64
 SGPU_PREC_FP32 = 32
+STENCIL_VARIANTS = 7  # SGPU_STENCIL_VARIANTS
 
 # every entry point declared in include/sparc_gpu.h
 EXPORTED = [
@@ -453,7 +454,7 @@ class Context:
     def autotune(self, ncol=64):
         """Time the FP32 stencil variants; returns (chosen variant, per-variant ms)."""
         v = ctypes.c_int()
-        ms = np.zeros(5)
+        ms = np.zeros(STENCIL_VARIANTS)
         _check(lib().sgpu_autotune(self._h, int(ncol), ctypes.byref(v), _ptr(ms)))
         return int(v.value), ms
 

@@ -1,6 +1,7 @@
 // Autotuner for the FP32 filter kernels: times each tile / register-blocking variant of the
 // fused stencil + Chebyshev update, and each form of the nonlocal apply (per point over all
-// column blocks, or alpha rows staged per chunk of covered points), on scratch blocks of the
+// column blocks, alpha rows staged per chunk of covered points, or per point with its Chi
+// values hoisted out of the column loop), on scratch blocks of the
 // context's grid and projector set, and keeps the fastest of each. The stencil variants
 // compute the same IEEE operation sequence per point, and so do the two apply forms, so the
 // choice changes speed only, never results.
@@ -10,7 +11,7 @@
 
 namespace sgpu {
 
-constexpr int kStencilVariants = 5;
+constexpr int kStencilVariants = SGPU_STENCIL_VARIANTS;
 
 // Times one degree-step launch (stencil + potential + recurrence term) of each FP32 variant
 // over ncol columns; returns the fastest in *best and per-variant milliseconds in ms.
@@ -59,7 +60,7 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
         if (tmin < best_ms) { best_ms = tmin; *best = v; }
     }
     ctx->stencil_variant = rc == SGPU_OK ? *best : saved;
-    // nonlocal apply: per-point form vs the form with alpha rows staged per chunk
+    // nonlocal apply: per-point form, alpha rows staged per chunk, Chi hoisted per point
     if (rc == SGPU_OK && ctx->has_nl && ctx->nl.ntot > 0 && ctx->nl.ncov > 0) {
         const long lda = nonlocal_alpha_ld(ncol, 4);
         float *alpha = nullptr;
@@ -70,7 +71,7 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
             const int saved_a = ctx->nl_apply_variant;
             float tbest = 1e30f;
             int abest = saved_a;
-            for (int v = 0; v < 2 && rc == SGPU_OK; v++) {
+            for (int v = 0; v < 3 && rc == SGPU_OK; v++) {
                 ctx->nl_apply_variant = v;
                 float t = 0.f, tmin = 1e30f;
                 for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
@@ -108,7 +109,7 @@ extern "C" {
 int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant)
 {
     if (!ctx || variant < 0 || variant >= kStencilVariants) {
-        set_error("sgpu_set_stencil_variant: variant must be 0..4");
+        set_error("sgpu_set_stencil_variant: variant must be 0..6");
         return SGPU_ERR_ARG;
     }
     ctx->stencil_variant = variant;
@@ -118,8 +119,8 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant)
 
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant)
 {
-    if (!ctx || variant < 0 || variant > 1) {
-        set_error("sgpu_set_nonlocal_apply_variant: variant must be 0 or 1");
+    if (!ctx || variant < 0 || variant > 2) {
+        set_error("sgpu_set_nonlocal_apply_variant: variant must be 0, 1 or 2");
         return SGPU_ERR_ARG;
     }
     ctx->nl_apply_variant = variant;

@@ -192,6 +192,93 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Apply with the Chi values hoisted: as k_nl_apply, but the Chi values and metadata of the
+// point's first NE entries are loaded once into registers before the column loop, so each
+// column block only reads the output block and alpha rows (L1); entries beyond the first NE
+// (a few percent of points) are read per column block. Same summation order as k_nl_apply.
+template <typename T, int CB, int VW, int NPMAX, int NE>
+__global__ void __launch_bounds__(256)
+    k_nl_apply_hoist(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+                     const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+                     const T *__restrict__ chi, int ncol, const T *__restrict__ alpha, long lda,
+                     T scale, T *__restrict__ out, long ldo)
+{
+    using V = typename VecOf<T, VW>::type;
+    const int cidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cidx >= ncov) return;
+    const long p = cov_pt[cidx];
+    const int e0 = cov_ptr[cidx], e1 = cov_ptr[cidx + 1];
+    T cr[NE][NPMAX];
+    int ipr[NE], npr[NE];
+#pragma unroll
+    for (int ee = 0; ee < NE; ee++) {
+        npr[ee] = 0;
+        ipr[ee] = 0;
+        if (e0 + ee < e1) {
+            const int4 meta = ent_meta[e0 + ee];
+            ipr[ee] = meta.x;
+            npr[ee] = meta.y;
+        }
+    }
+#pragma unroll
+    for (int ee = 0; ee < NE; ee++) {
+        const T *__restrict__ ch = chi + (e0 + ee < e1 ? ent_chi[e0 + ee] : 0);
+        const int ndc = e0 + ee < e1 ? ent_meta[e0 + ee].z : 0;
+#pragma unroll
+        for (int j = 0; j < NPMAX; j++) cr[ee][j] = j < npr[ee] ? __ldg(ch + (long)j * ndc) : T(0);
+    }
+    for (int n0 = 0; n0 < ncol; n0 += CB) {
+        T acc[CB], ov[CB];
+#pragma unroll
+        for (int c = 0; c < CB; c++) {
+            acc[c] = T(0);
+            ov[c] = n0 + c < ncol ? out[(long)(n0 + c) * ldo + p] : T(0);
+        }
+#pragma unroll
+        for (int ee = 0; ee < NE; ee++) {
+#pragma unroll
+            for (int j = 0; j < NPMAX; j++) {
+                if (j >= npr[ee]) break;
+                const T cv = cr[ee][j];
+                const V *__restrict__ al =
+                    reinterpret_cast<const V *>(alpha + (long)(ipr[ee] + j) * lda + n0);
+#pragma unroll
+                for (int c = 0; c < CB / VW; c++) {
+                    const V av = __ldg(al + c);
+                    const T *ae = reinterpret_cast<const T *>(&av);
+#pragma unroll
+                    for (int w = 0; w < VW; w++) acc[c * VW + w] += cv * ae[w];
+                }
+            }
+        }
+        for (int e = e0 + NE; e < e1; e++) {
+            const int4 meta = ent_meta[e];
+            const int ip = meta.x, np = meta.y, ndc = meta.z;
+            const T *__restrict__ ch = chi + ent_chi[e];
+            T cvs[NPMAX];
+#pragma unroll
+            for (int j = 0; j < NPMAX; j++) cvs[j] = j < np ? __ldg(ch + (long)j * ndc) : T(0);
+#pragma unroll
+            for (int j = 0; j < NPMAX; j++) {
+                if (j >= np) break;
+                const T cv = cvs[j];
+                const V *__restrict__ al =
+                    reinterpret_cast<const V *>(alpha + (long)(ip + j) * lda + n0);
+#pragma unroll
+                for (int c = 0; c < CB / VW; c++) {
+                    const V av = __ldg(al + c);
+                    const T *ae = reinterpret_cast<const T *>(&av);
+#pragma unroll
+                    for (int w = 0; w < VW; w++) acc[c * VW + w] += cv * ae[w];
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CB; c++)
+            if (n0 + c < ncol) out[(long)(n0 + c) * ldo + p] = ov[c] + scale * acc[c];
+    }
+}
+
 // Apply, staged: one block per (chunk of kApplyChunk consecutive covered points, block of CB
 // columns). The alpha rows of every atom that touches the chunk are staged once in shared
 // memory (rows listed in chunk_rows), and each thread accumulates its point's CB outputs from
@@ -350,6 +437,21 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
     }
     const dim3 grid((nl.ncov + 255) / 256);
     ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+    if (ctx->nl_apply_variant == 2) {
+#define SGPU_HOIST(NPM, NE)                                                                  \
+    k_nl_apply_hoist<T, CB, VW, NPM, NE><<<grid, 256, 0, st>>>(                              \
+        nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, chi_of<T>(nl), ncol, alpha, \
+        lda, (T)scale, out, ldo)
+        if (nl.max_np <= 9)
+            SGPU_HOIST(9, 2);
+        else if (nl.max_np <= 18)
+            SGPU_HOIST(18, 1);
+        else
+            SGPU_HOIST(32, 1);
+#undef SGPU_HOIST
+        SGPU_CUDA_TRY(cudaGetLastError());
+        return SGPU_OK;
+    }
 #define SGPU_APPLY(NPM)                                                                      \
     k_nl_apply<T, CB, VW, NPM><<<grid, 256, 0, st>>>(nl.ncov, nl.cov_pt, nl.cov_ptr,         \
                                                      nl.ent_chi, nl.ent_meta, chi_of<T>(nl), \

@@ -564,10 +564,10 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         set_error("sgpu_scf: precision must be SGPU_PREC_FP64 or SGPU_PREC_FP32");
         return SGPU_ERR_ARG;
     }
-    if (prm->graded_tail < 0 || prm->graded_tail > 2 ||
+    if (prm->graded_tail < 0 || prm->graded_tail > 1 ||
         (prm->graded_tail == 1 &&
          (prm->tail_fp64_degrees < 0 || prm->tail_fp64_degrees >= prm->cheb_degree))) {
-        set_error("sgpu_scf: graded_tail must be 0, 1 or 2, and tail_fp64_degrees in "
+        set_error("sgpu_scf: graded_tail must be 0 or 1, and tail_fp64_degrees in "
                   "[0, cheb_degree) for 1");
         return SGPU_ERR_ARG;
     }
@@ -668,13 +668,6 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 // HY into X (the reference reuses Xorb for HY), then project in FP32 products
                 SGPU_TRY(hamiltonian_dev<float>(ctx, 0, Ns, 0.0, Y32, N, X32, N, 1.0, 0.0, nullptr, 0, st));
                 SGPU_TRY(project_f32(ctx, Ns, Y32, N, X32, N, d_Hp, d_Mp, st));
-            } else if (graded && prm->graded_tail == 2) {
-                // FP32 filter, Cholesky QR with an FP64 Gram matrix, then the standard
-                // eigenproblem on FP32 products of the orthonormal block
-                SGPU_TRY(chebyshev_dev<float>(ctx, 0, X32, N, Y32, N, Ns, m, cutoff, eigmax, eigmin, st));
-                SGPU_TRY(cholqr2_f32(ctx, Ns, Y32, N, Y64, st));
-                SGPU_TRY(hamiltonian_dev<float>(ctx, 0, Ns, 0.0, Y32, N, X32, N, 1.0, 0.0, nullptr, 0, st));
-                SGPU_TRY(project_h_f32(ctx, Ns, Y32, N, X32, N, d_Hp, st));
             } else if (graded) {
                 SGPU_TRY(chebyshev_graded(ctx, 0, X32, Y32, X64, Y64, Ns, m,
                                           prm->tail_fp64_degrees, cutoff, eigmax, eigmin, st));
@@ -686,15 +679,11 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 SGPU_TRY(project_f64(ctx, Ns, Y64, N, X64, N, d_Hp, d_Mp, st));
             }
             SGPU_CUDA_TRY(cudaEventRecord(e1, st));
-            const bool cq = graded && prm->graded_tail == 2;  // orthonormal block: standard
-            if (cq)
-                SGPU_TRY(standard_eig(ctx, Ns, d_Hp, d_lam, st));
-            else
-                SGPU_TRY(generalized_eig(ctx, Ns, d_Hp, d_Mp, d_lam, st));
+            SGPU_TRY(generalized_eig(ctx, Ns, d_Hp, d_Mp, d_lam, st));
             float ms = 0.f;
             SGPU_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
             filter_ms += ms;
-            if (mixed || cq) {
+            if (mixed) {
                 SGPU_TRY(rotate_f32(ctx, Ns, Y32, N, d_Hp, X32, N, st));
             } else {
                 SGPU_TRY(rotate_f64(ctx, Ns, Y64, N, d_Hp, X64, N, st));
@@ -717,7 +706,7 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         std::vector<double> w(Ns);
         for (int n = 0; n < Ns; n++) w[n] = occfac * occ[n] / ctx->dV;
         SGPU_CUDA_TRY(cudaMemcpyAsync(d_w, w.data(), sizeof(double) * Ns, cudaMemcpyHostToDevice, st));
-        if (mixed || (graded && prm->graded_tail == 2))
+        if (mixed)
             SGPU_TRY(density_dev<float>(ctx, X32, N, Ns, d_w, d_rhoout, st));
         else
             SGPU_TRY(density_dev<double>(ctx, X64, N, Ns, d_w, d_rhoout, st));

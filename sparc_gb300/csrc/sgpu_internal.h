@@ -219,9 +219,6 @@ int generalized_eig(sgpu_ctx *ctx, int n, double *Hp, double *Mp, double *lambda
 int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *Q, double *X,
                long ldx, cudaStream_t st);
 int cholqr_f64(sgpu_ctx *ctx, int ncol, double *Y, long ldy, cudaStream_t st);
-int cholqr2_f32(sgpu_ctx *ctx, int ncol, float *Y, long ldy, double *wide, cudaStream_t st);
-int project_h_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
-                  double *Hp, cudaStream_t st);
 int standard_eig(sgpu_ctx *ctx, int n, double *Hp, double *lambda_dev, cudaStream_t st);
 int rotate_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const double *Q, float *X,
                long ldx, cudaStream_t st);

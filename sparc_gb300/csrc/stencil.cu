@@ -304,6 +304,12 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 template <bool VEC>
 __device__ __forceinline__ float2 ld_pair(const float *__restrict__ base, int o0, int o1)
 {
@@ -311,6 +317,81 @@ __device__ __forceinline__ float2 ld_pair(const float *__restrict__ base, int o0
         return __ldg(reinterpret_cast<const float2 *>(base + o0));
     else
         return make_float2(__ldg(base + o0), __ldg(base + o1));
+}
+
+// Arithmetic of one 2x2 block at plane k (queue slot (U+R) % Q holds plane k): x-neighbours
+// from the shared-memory rows srow0 and srow0 + W (each starting R points left of the
+// block's first column), y-neighbours from the column yv (rows j0-R .. j0+1+R), z-neighbours
+// from the register queues qa (row j0) and qb (row j0+1). Per point this is the operation
+// sequence of k_stencil_f32x2: three FMA chains (x, y, z) over the symmetric pair sums, the
+// potential term, the s1 scale and the recurrence term.
+template <int R, int Q, int U>
+__device__ __forceinline__ void b22_block(const StencilParams<float> &p,
+                                          const float *__restrict__ srow0, int W,
+                                          const float2 (&yv)[2 * R + 2], const float2 (&qa)[Q],
+                                          const float2 (&qb)[Q], const float2 (&vc)[2],
+                                          const float2 (&zc)[2], bool hasv, bool hasz,
+                                          float2 (&o)[2])
+{
+#pragma unroll
+    for (int rr = 0; rr < 2; rr++) {
+        const float2 cen = rr ? qb[(U + R) % Q] : qa[(U + R) % Q];
+        const float *srow = srow0 + rr * W;
+        float2 L[R + 1];
+#pragma unroll
+        for (int m = 0; m <= R; m++) L[m] = *reinterpret_cast<const float2 *>(srow + 2 * m);
+        float ax0 = p.c0 * cen.x, ax1 = p.c0 * cen.y;
+        float ay0 = 0.f, ay1 = 0.f, az0 = 0.f, az1 = 0.f;
+#pragma unroll
+        for (int r = 1; r <= R; r++) {
+            float2 lo, hi;
+            if (r % 2 == 0) {
+                lo = L[(R - r) / 2];
+                hi = L[(R + r) / 2];
+            } else {
+                lo = make_float2(L[(R - r) / 2].y, L[(R - r + 1) / 2].x);
+                hi = make_float2(L[(R + r) / 2].y, L[(R + r + 1) / 2].x);
+            }
+            const float2 xs = __fadd2_rn(lo, hi);
+            const float2 ys = __fadd2_rn(yv[R + rr - r], yv[R + rr + r]);
+            const float2 zsum = rr ? __fadd2_rn(qb[(U + R - r) % Q], qb[(U + R + r) % Q])
+                                   : __fadd2_rn(qa[(U + R - r) % Q], qa[(U + R + r) % Q]);
+            ax0 = fmaf(xs.x, p.wx[r], ax0); ax1 = fmaf(xs.y, p.wx[r], ax1);
+            ay0 = fmaf(ys.x, p.wy[r], ay0); ay1 = fmaf(ys.y, p.wy[r], ay1);
+            az0 = fmaf(zsum.x, p.wz[r], az0); az1 = fmaf(zsum.y, p.wz[r], az1);
+        }
+        float o0 = ax0 + (ay0 + az0), o1 = ax1 + (ay1 + az1);
+        if (hasv) {
+            o0 = fmaf(p.bv, vc[rr].x * cen.x, o0);
+            o1 = fmaf(p.bv, vc[rr].y * cen.y, o1);
+        }
+        o0 *= p.s1;
+        o1 *= p.s1;
+        if (hasz) {
+            o0 = fmaf(p.s2, zc[rr].x, o0);
+            o1 = fmaf(p.s2, zc[rr].y, o1);
+        }
+        o[rr] = make_float2(o0, o1);
+    }
+}
+
+// Stores one 2x2 block (rows beyond Ny and points beyond Nx are skipped).
+template <bool VEC>
+__device__ __forceinline__ void b22_store(float *__restrict__ oc, int kpl, int row0, int row1,
+                                          int gx0, int gx1, bool r0ok, bool r1ok, bool in0,
+                                          bool in1, const float2 (&o)[2])
+{
+#pragma unroll
+    for (int rr = 0; rr < 2; rr++) {
+        const bool rok = rr ? r1ok : r0ok;
+        const int orow = (rr ? row1 : row0) + kpl;
+        if (VEC && rok && in1) {
+            *reinterpret_cast<float2 *>(oc + orow + gx0) = o[rr];
+        } else if (rok) {
+            if (in0) oc[orow + gx0] = o[rr].x;
+            if (in1) oc[orow + gx1] = o[rr].y;
+        }
+    }
 }
 
 template <int R, int BX, int BY, int MINB, bool VEC>
@@ -445,53 +526,11 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             float2 yv[2 * R + 2];                                                                \
             _Pragma("unroll") for (int t = 0; t < 2 * R + 2; t++)                                \
                 yv[t] = *reinterpret_cast<const float2 *>(&s[b][2 * ty + t][R + 2 * tx]);        \
-            _Pragma("unroll") for (int rr = 0; rr < 2; rr++) {                                   \
-                const float2 cen = rr ? cb : ca;                                                 \
-                const float *srow = &s[b][2 * ty + R + rr][2 * tx];                              \
-                float2 L[R + 1];                                                                 \
-                _Pragma("unroll") for (int m = 0; m <= R; m++)                                   \
-                    L[m] = *reinterpret_cast<const float2 *>(srow + 2 * m);                      \
-                float ax0 = p.c0 * cen.x, ax1 = p.c0 * cen.y;                                    \
-                float ay0 = 0.f, ay1 = 0.f, az0 = 0.f, az1 = 0.f;                                \
-                _Pragma("unroll") for (int r = 1; r <= R; r++) {                                 \
-                    float2 lo, hi;                                                               \
-                    if (r % 2 == 0) {                                                            \
-                        lo = L[(R - r) / 2];                                                     \
-                        hi = L[(R + r) / 2];                                                     \
-                    } else {                                                                     \
-                        lo = make_float2(L[(R - r) / 2].y, L[(R - r + 1) / 2].x);                \
-                        hi = make_float2(L[(R + r) / 2].y, L[(R + r + 1) / 2].x);                \
-                    }                                                                            \
-                    const float2 xs = __fadd2_rn(lo, hi);                                        \
-                    const float2 ys = __fadd2_rn(yv[R + rr - r], yv[R + rr + r]);                \
-                    const float2 zsum = rr ? __fadd2_rn(qb[((U) + R - r) % Q], qb[((U) + R + r) % Q]) \
-                                           : __fadd2_rn(qa[((U) + R - r) % Q], qa[((U) + R + r) % Q]); \
-                    ax0 = fmaf(xs.x, p.wx[r], ax0); ax1 = fmaf(xs.y, p.wx[r], ax1);              \
-                    ay0 = fmaf(ys.x, p.wy[r], ay0); ay1 = fmaf(ys.y, p.wy[r], ay1);              \
-                    az0 = fmaf(zsum.x, p.wz[r], az0); az1 = fmaf(zsum.y, p.wz[r], az1);          \
-                }                                                                                \
-                float o0 = ax0 + (ay0 + az0), o1 = ax1 + (ay1 + az1);                            \
-                if (p.v) {                                                                       \
-                    const float2 vcur = rr ? vcb : vca;                                          \
-                    o0 = fmaf(p.bv, vcur.x * cen.x, o0);                                         \
-                    o1 = fmaf(p.bv, vcur.y * cen.y, o1);                                         \
-                }                                                                                \
-                o0 *= p.s1;                                                                      \
-                o1 *= p.s1;                                                                      \
-                if (zc) {                                                                        \
-                    const float2 zcur = rr ? zcb : zca;                                          \
-                    o0 = fmaf(p.s2, zcur.x, o0);                                                 \
-                    o1 = fmaf(p.s2, zcur.y, o1);                                                 \
-                }                                                                                \
-                const bool rok = rr ? r1ok : r0ok;                                               \
-                const int orow = (rr ? row1 : row0) + k * NxNy;                                  \
-                if (VEC && rok && in1) {                                                         \
-                    *reinterpret_cast<float2 *>(oc + orow + gx0) = make_float2(o0, o1);          \
-                } else if (rok) {                                                                \
-                    if (in0) oc[orow + gx0] = o0;                                                \
-                    if (in1) oc[orow + gx1] = o1;                                                \
-                }                                                                                \
-            }                                                                                    \
+            const float2 vcs[2] = {vca, vcb}, zcs[2] = {zca, zcb};                               \
+            float2 o[2];                                                                         \
+            b22_block<R, Q, (U)>(p, &s[b][2 * ty + R][2 * tx], W, yv, qa, qb, vcs, zcs,          \
+                                 p.v != nullptr, zc != nullptr, o);                              \
+            b22_store<VEC>(oc, k * NxNy, row0, row1, gx0, gx1, r0ok, r1ok, in0, in1, o);         \
         }                                                                                        \
     }
 
@@ -502,6 +541,180 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     }
 #undef SGPU_B22_STEP
     cp_async_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP32 kernel with 2x2 register blocking fed from a shared-memory plane ring. Every plane
+// (centre tile plus its x/y halo) reaches shared memory by cp.async R+D planes before the
+// block computes it, and the potential / recurrence-term planes D planes before; the register
+// z-queue is topped up from the ring (plane k+R, in shared memory since step k-D) instead of
+// from global memory, so no step waits on a global load issued in the same step. One barrier
+// per plane: after it the slot of plane k-1 is free and receives plane k+R+D. Same arithmetic
+// (b22_block) as k_stencil_f32_b22, so the results are identical.
+template <int R, int BX, int BY, int D, bool VEC>
+struct RingShape {
+    static constexpr int W = BX + 2 * R, H = BY + 2 * R;
+    static constexpr int SLOT = H * W;     // one plane with its halo (the corners stay unused)
+    static constexpr int NR = R + D + 1;   // ring slots: planes k .. k+R+D
+    static constexpr int NV = D + 1;       // potential / recurrence-term slots: planes k .. k+D
+    static constexpr int NT = BX / 2 * (BY / 2);
+    static constexpr int EW = VEC ? 2 : 1;  // floats per copy
+    static constexpr int CROW = W / EW, HROW = BX / EW;
+    static constexpr int NCOPY = BY * CROW + 2 * R * HROW;  // copies per plane
+    static constexpr int NU = (NCOPY + NT - 1) / NT;        // copies per thread and plane
+    static constexpr size_t smem_bytes = sizeof(float) * ((size_t)NR * SLOT + (size_t)NV * 2 * BX * BY);
+};
+
+template <int R, int BX, int BY, int MINB, bool VEC, int D>
+__global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
+    k_stencil_f32_ring(const StencilParams<float> p)
+{
+    using S = RingShape<R, BX, BY, D, VEC>;
+    constexpr int Q = 2 * R + 1;
+    constexpr int W = S::W;
+    static_assert(Q == 13 && R % 2 == 0 && D >= 1, "the unrolled z-loop is written for radius 6");
+    extern __shared__ __align__(16) float ring[];
+    float *const vzs = ring + S::NR * S::SLOT;  // [NV][2][BY][BX]: potential, recurrence term
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * (BX / 2) + tx;
+    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+    const int col = blockIdx.z / p.nslab;
+    const int slab = blockIdx.z - col * p.nslab;
+    const int zs = slab * p.zlen;
+    const int ze = min(zs + p.zlen, p.Nz);
+    if (zs >= ze) return;
+
+    const int i0 = x0 + 2 * tx, j0 = y0 + 2 * ty;
+    const bool in0 = i0 < p.Nx, in1 = i0 + 1 < p.Nx;
+    const bool r0ok = j0 < p.Ny, r1ok = j0 + 1 < p.Ny;
+    const int gx0 = wrapi(i0, p.Nx), gx1 = wrapi(i0 + 1, p.Nx);
+    const int row0 = wrapi(j0, p.Ny) * p.Nx, row1 = wrapi(j0 + 1, p.Ny) * p.Nx;
+    const int NxNy = p.Nx * p.Ny;
+    const float *__restrict__ xc = p.x + (long)col * p.ldx;
+    const float *__restrict__ zc = p.z ? p.z + (long)col * p.ldz : nullptr;
+    float *__restrict__ oc = p.out + (long)col * p.ldo;
+
+    // this thread's copies of a plane: in-plane source offset and ring-slot destination
+    int gofs[S::NU], sofs[S::NU];
+#pragma unroll
+    for (int u = 0; u < S::NU; u++) {
+        const int e = tid + u * S::NT;
+        gofs[u] = 0;
+        sofs[u] = -1;
+        if (e < S::NCOPY) {
+            int r, c;
+            if (e < BY * S::CROW) {
+                r = R + e / S::CROW;
+                c = (e % S::CROW) * S::EW;
+            } else {
+                const int e2 = e - BY * S::CROW, hr = e2 / S::HROW;
+                r = hr < R ? hr : hr + BY;
+                c = R + (e2 % S::HROW) * S::EW;
+            }
+            gofs[u] = wrapi(y0 - R + r, p.Ny) * p.Nx + wrapi(x0 - R + c, p.Nx);
+            sofs[u] = r * W + c;
+        }
+    }
+    // group of step k: plane k+R+D into the ring, and the potential / recurrence term of
+    // plane k+D; a group is committed (possibly empty) for every step
+    auto issue = [&](int k) {
+        if (k + D < ze) {
+            const int kp = k + R + D;
+            const float *pl = xc + wrapi(kp, p.Nz) * NxNy;
+            float *dst = ring + (kp % S::NR) * S::SLOT;
+#pragma unroll
+            for (int u = 0; u < S::NU; u++) {
+                if (sofs[u] >= 0) {
+                    if constexpr (VEC) cp_async8(dst + sofs[u], pl + gofs[u]);
+                    else cp_async4(dst + sofs[u], pl + gofs[u]);
+                }
+            }
+            const int kv = k + D;
+            if (kv >= zs) {
+                const int pk = kv * NxNy;
+                float *vd = vzs + (kv % S::NV) * 2 * BX * BY + 2 * ty * BX + 2 * tx;
+                const float *srcs[2] = {p.v, zc};
+#pragma unroll
+                for (int a = 0; a < 2; a++) {
+                    if (!srcs[a]) continue;
+                    float *d = vd + a * BX * BY;
+                    if constexpr (VEC) {
+                        cp_async8(d, srcs[a] + pk + gx0 + row0);
+                        cp_async8(d + BX, srcs[a] + pk + gx0 + row1);
+                    } else {
+                        cp_async4(d, srcs[a] + pk + gx0 + row0);
+                        cp_async4(d + 1, srcs[a] + pk + gx1 + row0);
+                        cp_async4(d + BX, srcs[a] + pk + gx0 + row1);
+                        cp_async4(d + BX + 1, srcs[a] + pk + gx1 + row1);
+                    }
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    // prologue: the register queue holds planes zs-R .. zs+R-1; the ring receives planes
+    // zs .. zs+R+D-1 (the groups of steps zs-R-D .. zs-1)
+    float2 qa[Q], qb[Q];
+#pragma unroll
+    for (int m = 0; m < 2 * R; m++) {
+        const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
+        qa[m] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);
+        qb[m] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);
+    }
+    for (int j = 0; j < R + D; j++) issue(zs - R - D + j);
+
+#define SGPU_RING_STEP(U)                                                                        \
+    {                                                                                            \
+        const int k = kb + (U);                                                                  \
+        if (k < ze) {                                                                            \
+            cp_async_wait_group<D - 1>();                                                        \
+            __syncthreads();                                                                     \
+            issue(k);                                                                            \
+            const float *sl = ring + (k % S::NR) * S::SLOT;                                      \
+            const float *sq = ring + ((k + R) % S::NR) * S::SLOT + (2 * ty + R) * W + R + 2 * tx; \
+            qa[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq);                       \
+            qb[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq + W);                   \
+            const float *vz = vzs + (k % S::NV) * 2 * BX * BY + 2 * ty * BX + 2 * tx;            \
+            float2 vcs[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};                      \
+            float2 zcs[2] = {vcs[0], vcs[1]};                                                    \
+            if (p.v) {                                                                           \
+                vcs[0] = *reinterpret_cast<const float2 *>(vz);                                  \
+                vcs[1] = *reinterpret_cast<const float2 *>(vz + BX);                             \
+            }                                                                                    \
+            if (zc) {                                                                            \
+                zcs[0] = *reinterpret_cast<const float2 *>(vz + BX * BY);                        \
+                zcs[1] = *reinterpret_cast<const float2 *>(vz + BX * BY + BX);                   \
+            }                                                                                    \
+            float2 yv[2 * R + 2];                                                                \
+            _Pragma("unroll") for (int t = 0; t < 2 * R + 2; t++)                                \
+                yv[t] = *reinterpret_cast<const float2 *>(sl + (2 * ty + t) * W + R + 2 * tx);   \
+            float2 o[2];                                                                         \
+            b22_block<R, Q, (U)>(p, sl + (2 * ty + R) * W + 2 * tx, W, yv, qa, qb, vcs, zcs,     \
+                                 p.v != nullptr, zc != nullptr, o);                              \
+            b22_store<VEC>(oc, k * NxNy, row0, row1, gx0, gx1, r0ok, r1ok, in0, in1, o);         \
+        }                                                                                        \
+    }
+
+    for (int kb = zs; kb < ze; kb += Q) {
+        SGPU_RING_STEP(0) SGPU_RING_STEP(1) SGPU_RING_STEP(2) SGPU_RING_STEP(3)
+        SGPU_RING_STEP(4) SGPU_RING_STEP(5) SGPU_RING_STEP(6) SGPU_RING_STEP(7)
+        SGPU_RING_STEP(8) SGPU_RING_STEP(9) SGPU_RING_STEP(10) SGPU_RING_STEP(11)
+        SGPU_RING_STEP(12)
+    }
+#undef SGPU_RING_STEP
+    cp_async_wait_all();
+}
+
+template <int R, int BX, int BY, int MINB, bool VEC, int D>
+int launch_ring(const StencilParams<float> &q, dim3 grid, cudaStream_t st)
+{
+    constexpr size_t smem = RingShape<R, BX, BY, D, VEC>::smem_bytes;
+    auto kern = k_stencil_f32_ring<R, BX, BY, MINB, VEC, D>;
+    SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    kern<<<grid, dim3(BX / 2, BY / 2), smem, st>>>(q);
+    return SGPU_OK;
 }
 
 }  // namespace
@@ -543,7 +756,8 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
 
     const bool f32 = sizeof(T) == 4;
     // FP32 variants (autotune.cu): 0 paired 32x16, 1 2x2-blocked 32x16, 2 2x2-blocked 64x8,
-    // 3 paired 64x8, 4 2x2-blocked 32x16 with 3 blocks per SM
+    // 3 paired 64x8, 4 2x2-blocked 32x16 with 3 blocks per SM, 5 and 6 2x2-blocked 32x16 fed
+    // from the shared-memory plane ring one and two planes ahead
     const int variant = f32 ? ctx->stencil_variant : 0;
     const bool wide = variant == 2 || variant == 3;
     const int tbx = f32 ? (wide ? 64 : BXP) : BX;
@@ -592,6 +806,18 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                     k_stencil_f32_b22<R, 32, 16, 3, true><<<grid, dim3(16, 8), 0, st>>>(q);
                 else
                     k_stencil_f32_b22<R, 32, 16, 3, false><<<grid, dim3(16, 8), 0, st>>>(q);
+                break;
+            case 5:  // 2x2 32x16 from the plane ring, planes one step ahead
+                if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, true, 1>(q, grid, st)));
+                else
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, false, 1>(q, grid, st)));
+                break;
+            case 6:  // 2x2 32x16 from the plane ring, planes two steps ahead
+                if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 16, 3, true, 2>(q, grid, st)));
+                else
+                    SGPU_TRY((launch_ring<R, 32, 16, 3, false, 2>(q, grid, st)));
                 break;
             default:
                 k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);

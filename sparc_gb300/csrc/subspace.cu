@@ -198,78 +198,6 @@ int cholqr_f64(sgpu_ctx *ctx, int ncol, double *Y, long ldy, cudaStream_t st)
     return SGPU_OK;
 }
 
-// Cholesky QR of an FP32 block in two passes: the first with the Gram matrix formed in FP64
-// (the block widened into `wide`, DSYRK), so its conditioning does not limit the result; the
-// second with BF16x9 products on the tensor cores, which restores orthonormality to FP32
-// level once the first pass has brought the condition number near one. The triangular solves
-// run in FP32 with the FP64 Cholesky factors narrowed.
-int cholqr2_f32(sgpu_ctx *ctx, int ncol, float *Y, long ldy, double *wide, cudaStream_t st)
-{
-    SGPU_TRY(ensure_handles(ctx));
-    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
-    cusolverDnSetStream(ctx->cusolver, st);
-    double *M = nullptr;
-    SGPU_TRY(ws_get(ctx, WS_EIG, sizeof(double) * (size_t)ncol * ncol +
-                                     sizeof(float) * 2 * (size_t)ncol * ncol,
-                    (void **)&M));
-    float *R32 = reinterpret_cast<float *>(M + (size_t)ncol * ncol);
-    float *M32 = R32 + (size_t)ncol * ncol;
-    const long n2 = (long)ncol * ncol;
-    const float onef = 1.f, zerof = 0.f;
-    const double one = 1.0, zero = 0.0;
-    for (int pass = 0; pass < 2; pass++) {
-        if (pass == 0) {
-            SGPU_TRY(convert_cols<float, double>(Y, ldy, wide, ctx->Nd, ctx->Nd, ncol, st));
-            ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
-            SGPU_CUBLAS_TRY(cublasDsyrk(ctx->cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, ncol,
-                                        (int)ctx->Nd, &one, wide, (int)ctx->Nd, &zero, M, ncol));
-        } else {
-            ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
-            SGPU_CUBLAS_TRY(cublasGemmEx(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol,
-                                         (int)ctx->Nd, &onef, Y, CUDA_R_32F, (int)ldy, Y,
-                                         CUDA_R_32F, (int)ldy, &zerof, M32, CUDA_R_32F, ncol,
-                                         CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
-                                         CUBLAS_GEMM_DEFAULT));
-            k_f32_to_f64<<<std::max<long>(1, std::min<long>((n2 + 255) / 256, 4096)), 256, 0,
-                           st>>>(M32, M, n2);
-            ctx->launches++;
-        }
-        SGPU_TRY(potrf_upper(ctx, ncol, M, st));
-        SGPU_TRY(convert_cols<double, float>(M, ncol, R32, ncol, ncol, ncol, st));
-        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
-        SGPU_CUBLAS_TRY(cublasStrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER,
-                                    CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, (int)ctx->Nd, ncol, &onef,
-                                    R32, ncol, Y, (int)ldy));
-    }
-    return SGPU_OK;
-}
-
-// Hp = Yᵀ HY for an orthonormal FP32 block (BF16x9 products), widened to FP64
-int project_h_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
-                  double *Hp, cudaStream_t st)
-{
-    SGPU_TRY(ensure_handles(ctx));
-    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
-    float *tmp = nullptr;
-    SGPU_TRY(ws_get(ctx, WS_MISC, sizeof(float) * (size_t)ncol * ncol, (void **)&tmp));
-    const float one = 1.f, zero = 0.f;
-    {
-        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
-        SGPU_CUBLAS_TRY(cublasGemmEx(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol,
-                                     (int)ctx->Nd, &one, Y, CUDA_R_32F, (int)ldy, HY, CUDA_R_32F,
-                                     (int)ldh, &zero, tmp, CUDA_R_32F, ncol,
-                                     CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT));
-    }
-    const long n2 = (long)ncol * ncol;
-    // widened as computed: the eigensolver reads the upper triangle only, as the reference's
-    // dsyevd does
-    k_f32_to_f64<<<std::max<long>(1, std::min<long>((n2 + 255) / 256, 4096)), 256, 0, st>>>(
-        tmp, Hp, n2);
-    ctx->launches++;
-    SGPU_CUDA_TRY(cudaGetLastError());
-    return SGPU_OK;
-}
-
 // Hp q = lambda q (upper triangle; dsyevd, the STANDARD_EIGEN branch of
 // DP_Solve_Generalized_EigenProblem, src/eigenSolver.c:1318-1321); Hp becomes Q.
 int standard_eig(sgpu_ctx *ctx, int n, double *Hp, double *lambda_dev, cudaStream_t st)

@@ -153,12 +153,16 @@ def initial_density(torch, cs, net, dev):
     return rho
 
 
-def scf_settings(cs, precision, Nstates=160, cheb_degree=20):
+def scf_settings(cs, precision, Nstates=160, cheb_degree=20, rho_trigger=4):
+    """SCF parameters of the data generation and the evaluation; rho_trigger is the number of
+    filter passes of the first SCF iteration (the reference's rhoTrigger, default 4)."""
     kw = dict(Nstates=Nstates, cheb_degree=cheb_degree)
     if precision == 32:
         kw.update(precision=SGPU_PREC_FP32, fp64_switch_error=1e-4, graded_tail=1,
                   tail_fp64_degrees=0)
-    return cs.scf_params(**kw)
+    p = cs.scf_params(**kw)
+    p.rho_trigger = int(rho_trigger)
+    return p
 
 
 def generate(torch, cs, indices, dev, precision=32, log=None, snap=si64_snapshot, scf_kw=None):
@@ -246,10 +250,13 @@ def evaluate(torch, cs, net, indices, dev, precision=32, log=None, snap=si64_sna
                             start_error=float(np.linalg.norm(rho0 - rho) / np.linalg.norm(rho)))
         e_conv = rec["rho_at"]["Etot_per_atom"]
         for tag in ("rho_at", "learned"):
-            it, ts = energy_reached(rec[tag]["history"], e_conv, cs.n_atom, energy_tol)
+            h = rec[tag].pop("history")
+            it, ts = energy_reached(h, e_conv, cs.n_atom, energy_tol)
             rec[tag]["iters_to_energy_tol"] = it
             rec[tag]["time_to_energy_tol_s"] = None if ts is None else ts + rec[tag]["predict_s"]
-            del rec[tag]["history"]
+            # per iteration: energy error per atom against e_conv, and the SCF error
+            rec[tag]["dE_per_atom"] = [float(f"{e / cs.n_atom - e_conv:.3e}") for e in h["Etot"]]
+            rec[tag]["scf_error"] = [float(f"{v:.3e}") for v in h["scf_error"]]
         out.append(rec)
         if log:
             log(f"held-out {idx}: {rec['rho_at']['scf_iters']} -> {rec['learned']['scf_iters']} "
@@ -285,6 +292,8 @@ def main():
     ap.add_argument("--eval-modes", default="32,64", help="SCF modes of the evaluation")
     ap.add_argument("--eval-count", type=int, default=None,
                     help="held-out snapshots per evaluation mode (default: all)")
+    ap.add_argument("--rho-triggers", default="4",
+                    help="filter passes of the first SCF iteration to evaluate (comma list)")
     args = ap.parse_args()
     import torch
     from .psp8 import load_tables
@@ -315,12 +324,16 @@ def main():
         del descs, targs
     held = list(range(ntrain, args.snapshots))[:args.eval_count]
     evals = {}
+    triggers = [int(t) for t in args.rho_triggers.split(",")]
     for mode in (int(m) for m in args.eval_modes.split(",")):
-        ev = evaluate(torch, cs, net, held, dev, mode, log=lambda s: print(s, flush=True))
-        name = "mixed" if mode == 32 else "fp64"
-        summary[f"eval_{name}"] = summarize(ev, "mixed (FP32, then FP32 filter + FP64 "
-                                                "Rayleigh-Ritz)" if mode == 32 else "FP64")
-        evals[name] = ev
+        for rt in triggers:
+            ev = evaluate(torch, cs, net, held, dev, mode, log=lambda s: print(s, flush=True),
+                          scf_kw=dict(rho_trigger=rt))
+            name = ("mixed" if mode == 32 else "fp64") + ("" if triggers == [4] else f"_rt{rt}")
+            desc = ("mixed (FP32, then FP32 filter + FP64 Rayleigh-Ritz)" if mode == 32
+                    else "FP64") + f", {rt} filter passes in the first SCF iteration"
+            summary[f"eval_{name}"] = summarize(ev, desc)
+            evals[name] = ev
     print(json.dumps(summary), flush=True)
     if args.out:
         with open(args.out, "w") as f:

@@ -48,3 +48,10 @@ def test_host_modules_import():
     import py_compile
     for fn in ("bench.py", "__graft_entry__.py"):
         py_compile.compile(os.path.join(ROOT, fn), doraise=True)
+
+
+def test_python_mirror_constants_match_header():
+    import sparc_gb300
+    txt = open(os.path.join(ROOT, "include", "sparc_gpu.h")).read()
+    n = int(re.search(r"#define SGPU_STENCIL_VARIANTS (\d+)", txt).group(1))
+    assert sparc_gb300.STENCIL_VARIANTS == n

@@ -129,7 +129,7 @@ def test_fp32_stencil_variants_identical(gpu_available, shape):
     ctx = make_ctx(grid, nl, veff)
     x = rng.uniform(-1, 1, (3, Nd)).astype(np.float32)
     outs = []
-    for v in range(5):
+    for v in range(sg.STENCIL_VARIANTS):
         ctx.set_stencil_variant(v)
         X = x.copy(); Y = np.zeros_like(x)
         ctx.ChebyshevFiltering_f32(X, Y, 7, 0.5, 50.0, -1.0)
@@ -138,18 +138,18 @@ def test_fp32_stencil_variants_identical(gpu_available, shape):
         np.testing.assert_array_equal(Y, outs[0][1])
         np.testing.assert_array_equal(X, outs[0][0])
     best, ms = ctx.autotune(ncol=3)
-    assert 0 <= best < 5 and np.all(ms > 0)
+    assert 0 <= best < sg.STENCIL_VARIANTS and np.all(ms > 0)
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_nonlocal_apply_forms_identical(gpu_available, dtype):
-    """The staged and the per-point nonlocal apply give bit-identical results."""
+    """The per-point, staged and hoisted nonlocal apply forms give bit-identical results."""
     grid, nl, veff, rng = _random_case((30, 26, 22), seed=21, natom=7)
     Nd = 30 * 26 * 22
     ctx = make_ctx(grid, nl, veff)
     x = rng.uniform(-1, 1, (37, Nd)).astype(dtype)  # not a multiple of any column block
     outs = []
-    for v in (0, 1):
+    for v in (0, 1, 2):
         ctx.set_nonlocal_apply_variant(v)
         if dtype == np.float64:
             h = np.zeros_like(x)
@@ -160,6 +160,7 @@ def test_nonlocal_apply_forms_identical(gpu_available, dtype):
             ctx.ChebyshevFiltering_f32(X, Y, 3, 0.5, 50.0, -1.0)
             outs.append(Y)
     np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
 
 
 def test_device_pointers_match_host(gpu_available):

@@ -159,19 +159,14 @@ def test_std_projection_and_standard_eig_vs_lapack(gpu_available):
     assert np.abs(lam - lg).max() < 1e-8 * np.abs(lg).max()
 
 
-def test_scf_cholesky_tail_matches_reference_program(gpu_available):
-    """Mixed mode with the Cholesky-QR tail (graded_tail = 2) converges to the reference
-    program's energy and eigenvalues."""
+def test_scf_rejects_unknown_tail_mode(gpu_available):
+    """graded_tail takes 0 (plain FP64 tail) or 1 (graded filter + FP64 Rayleigh-Ritz)."""
     d, grid, nl, ref = load_scf()
     ctx = make_ctx(grid, nl)
     prm = scf_params(sg, d, ref, precision=32, switch=1e-4)
     prm.graded_tail = 2
-    res, rho, lam, occ = ctx.scf(prm, d["b"], d["rho0"], d["rho_core"])
-    n_atom = int(d["n_atom"])
-    assert res["converged"] == 1
-    assert abs(res["Etot"] / n_atom - ref["Etot_per_atom"]) < 1e-5
-    occupied = np.array(ref["occ"]) > 1e-3
-    assert np.abs(lam[occupied] - np.array(ref["lambda"])[occupied]).max() < 1e-5
+    with pytest.raises(sg.SgpuError):
+        ctx.scf(prm, d["b"], d["rho0"], d["rho_core"])
 
 
 def test_lanczos_bounds(gpu_available):
