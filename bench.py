@@ -181,13 +181,18 @@ def scf_block(sg, device=0, repeats=2):
     return out
 
 
-def scf_c4_block(sg, device=0):
+def scf_c4_block(sg, torch=None, device=0):
     """SCF time-to-solution on the 216-atom Si cell (3x3x3 diamond cells, a = 30.78 Bohr,
     77^3 grid, 520 states, degree 24, LDA, TOL_SCF 1e-6), set up on the device from the Si
-    psp8 tables (sparc_gb300.setup): plain FP64 CheFSI against the mixed-precision mode (FP32
-    filter and BF16x9 products while the SCF error falls, then the FP32 filter with an FP64
-    Rayleigh-Ritz step). Energies and eigenvalues against the reference program's run of the
-    same input where that run is committed (tests/golden/Si216_c4_scf_ref.json)."""
+    psp8 tables (sparc_gb300.setup): plain FP64 CheFSI (the reference's settings, 4 filter
+    passes in the first SCF iteration) against the mixed-precision mode (FP32 filter and
+    BF16x9 products while the SCF error falls, then the FP32 filter with an FP64 Rayleigh-Ritz
+    step), from the atomic superposition and from the learned initial density
+    (sparc_gb300/data/si64_density_mlp.npz, trained on Si64 snapshots; 8 first-iteration
+    passes, which a good start density turns into an almost converged first iteration; the
+    mixed run from rho_at with 8 passes is the ablation). Per run: the time to TOL_SCF, and the
+    time until the free energy is within 1e-5 Ha/atom of the reference program's converged
+    energy (tests/golden/Si216_c4_scf_ref.json; of the FP64 GPU run without it) and stays."""
     golden = os.path.join(ROOT, "tests", "golden")
     sys.path.insert(0, golden)
     import systems
@@ -211,17 +216,42 @@ def scf_c4_block(sg, device=0):
         out["reference"] = {"Etot_per_atom": ref["Etot_per_atom"], "scf_iters": ref["scf_iters"],
                             "walltime_s": ref.get("walltime_s"),
                             "where": ref.get("where", "reference program, x86 build host")}
-    runs = {"fp64": dict(precision=64),
-            "mixed": dict(precision=32, fp64_switch_error=1e-4, graded_tail=1,
-                          tail_fp64_degrees=0)}
+    from sparc_gb300.learned_density import DensityMLP, energy_reached, initial_density
+    mixed = dict(precision=32, fp64_switch_error=1e-4, graded_tail=1, tail_fp64_degrees=0)
+    runs = {"fp64": (dict(precision=64), 4, False),
+            "mixed": (mixed, 4, False),
+            "mixed_rt8": (mixed, 8, False),
+            "mixed_learned": (mixed, 8, True)}
+    net = None
+    npz = os.path.join(ROOT, "sparc_gb300", "data", "si64_density_mlp.npz")
+    if torch is not None and os.path.exists(npz):
+        net = DensityMLP.load(npz, device=device)
+    else:
+        runs.pop("mixed_learned")
     e64 = None
-    for name, kw in runs.items():
+    for name, (kw, rt, learned) in runs.items():
         prm = cs.scf_params(Nstates=520, cheb_degree=24, **kw)
-        res, rho, lam, occ = cs.scf(prm)
+        prm.rho_trigger = rt
+        t_pred = 0.0
+        rho0 = None
+        if learned:
+            dev = torch.device("cuda", device)
+            torch.cuda.synchronize(dev)
+            tp = time.perf_counter()
+            rho0 = initial_density(torch, cs, net, dev)
+            t_pred = time.perf_counter() - tp
+        res, rho, lam, occ = cs.scf(prm, rho_init=rho0)
         e = res["Etot"] / cs.n_atom
-        rec = {"time_s": round(res["time_s"], 3), "scf_iters": res["scf_iters"],
+        e_target = ref["Etot_per_atom"] if ref else (e64 if e64 is not None else e)
+        it, ts = energy_reached(res["history"], e_target, cs.n_atom, 1e-5)
+        rec = {"time_s": round(res["time_s"] + t_pred, 3), "scf_iters": res["scf_iters"],
                "converged": bool(res["converged"]), "Etot_per_atom": e,
-               "fp64_switch_iter": res["fp64_switch_iter"]}
+               "fp64_switch_iter": res["fp64_switch_iter"], "first_iteration_passes": rt,
+               "start": "learned" if learned else "rho_at",
+               "iters_to_1e-5_Ha_per_atom": it,
+               "time_to_1e-5_Ha_per_atom_s": None if ts is None else round(ts + t_pred, 3)}
+        if learned:
+            rec["predict_s"] = round(t_pred, 3)
         if name == "fp64":
             e64, lam64 = e, lam
         else:
@@ -235,6 +265,11 @@ def scf_c4_block(sg, device=0):
             rec["max_occ_eig_err_vs_ref"] = float(np.abs(lam[occd] - lr[occd]).max())
         out[name] = rec
     out["speedup_mixed_vs_fp64"] = round(out["fp64"]["time_s"] / out["mixed"]["time_s"], 3)
+    t64 = out["fp64"]["time_to_1e-5_Ha_per_atom_s"]
+    for name in ("mixed", "mixed_rt8", "mixed_learned"):
+        tn = out.get(name, {}).get("time_to_1e-5_Ha_per_atom_s")
+        if t64 and tn:
+            out[f"speedup_to_1e-5_{name}_vs_fp64"] = round(t64 / tn, 3)
     cs.close()
     return out
 
@@ -381,6 +416,7 @@ def main():
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     # pick the FP32 stencil variant for this grid (all variants give identical results)
     variant, variant_ms = ctx.autotune(ncol=min(ncol, 64))
+    forms = ctx.variants()
     kernel_name = ["k_stencil_f32x2<32x16>", "k_stencil_f32_b22<32x16>",
                    "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
                    "k_stencil_f32_b22<32x16, 3 blocks/SM>",
@@ -503,7 +539,7 @@ def main():
     if rank == 0 and not args.no_scf:
         scf = scf_block(sg, device=local)
         if not args.no_c4:
-            scf_c4 = scf_c4_block(sg, device=local)
+            scf_c4 = scf_c4_block(sg, torch, device=local)
     c3 = None
     if rank == 0 and not args.no_c3:
         c3 = batched_c3_block(sg, torch, dev, device=local)
@@ -518,7 +554,14 @@ def main():
                        "l2": "inputs larger than L2 (1.8 GB FP32 block), no flush",
                        "step": "X reset copy + degree-20 filter over 512 vectors",
                        "stencil_variant": {"chosen": kernel_name,
-                                           "autotune_ms": [round(float(v), 4) for v in variant_ms]}},
+                                           "autotune_ms": [round(float(v), 4) for v in variant_ms]},
+                       "nonlocal_forms": {
+                           "apply": ["per point", "staged per chunk", "per point, Chi hoisted"][
+                               forms["nl_apply"]],
+                           "project": ["per image segment", "per range of covered points"][
+                               forms["nl_project"]],
+                           "autotune_ms": {k: [round(float(v), 4) for v in vs]
+                                           for k, vs in ctx.tuning().items()}}},
             "roofline": {"bound": "hbm", "kernel": kernel_name,
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_src,

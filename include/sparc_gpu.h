@@ -421,6 +421,21 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
  * Same results whichever is used. */
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
 
+/* Fix the form of the FP32 nonlocal projection (0: one block per segment of one image's
+ * points; 1: one block per range of consecutive covered points, each x element read once);
+ * sgpu_autotune times both. The two sum in different orders (and both add per-block
+ * partial sums atomically), so results agree to FP32 rounding. */
+int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
+
+/* The kernel forms in use (set by sgpu_autotune or the sgpu_set_*_variant calls); any
+ * pointer may be NULL. */
+int sgpu_get_variants(sgpu_ctx *ctx, int *stencil, int *nl_apply, int *nl_project);
+
+/* Milliseconds per launch that the last sgpu_autotune measured for the three nonlocal apply
+ * forms (apply_ms[3]) and the two FP32 projection forms (project_ms[2]); zeros before any
+ * tuning or without projectors. Either pointer may be NULL. */
+int sgpu_get_tuning(sgpu_ctx *ctx, double *apply_ms, double *project_ms);
+
 /* ------------------------------------------------------------------- measurement */
 
 /* kernel kinds reported by sgpu_profile_read */

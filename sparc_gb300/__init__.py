@@ -36,7 +36,8 @@ EXPORTED = [
     "sgpu_mlp_create", "sgpu_mlp_destroy", "sgpu_mlp_nparam", "sgpu_mlp_get", "sgpu_mlp_set",
     "sgpu_mlp_forward", "sgpu_mlp_loss_grad", "sgpu_mlp_zero_grad", "sgpu_mlp_adam_step",
     "sgpu_Project_Hamiltonian_std", "sgpu_Solve_Standard_EigenProblem",
-    "sgpu_set_nonlocal_apply_variant",
+    "sgpu_set_nonlocal_apply_variant", "sgpu_set_nonlocal_project_variant", "sgpu_get_variants",
+    "sgpu_get_tuning",
 ]
 
 
@@ -463,6 +464,21 @@ class Context:
 
     def set_nonlocal_apply_variant(self, variant):
         _check(lib().sgpu_set_nonlocal_apply_variant(self._h, int(variant)))
+
+    def set_nonlocal_project_variant(self, variant):
+        _check(lib().sgpu_set_nonlocal_project_variant(self._h, int(variant)))
+
+    def variants(self):
+        """The kernel forms in use: dict(stencil, nl_apply, nl_project)."""
+        s, a, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().sgpu_get_variants(self._h, ctypes.byref(s), ctypes.byref(a), ctypes.byref(p)))
+        return dict(stencil=s.value, nl_apply=a.value, nl_project=p.value)
+
+    def tuning(self):
+        """Per-form milliseconds of the last autotune: dict(nl_apply=[3], nl_project=[2])."""
+        a, p = np.zeros(3), np.zeros(2)
+        _check(lib().sgpu_get_tuning(self._h, _ptr(a), _ptr(p)))
+        return dict(nl_apply=a.tolist(), nl_project=p.tolist())
 
     def profile_enable(self, on=True):
         _check(lib().sgpu_profile_enable(self._h, int(bool(on))))

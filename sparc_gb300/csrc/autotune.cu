@@ -1,7 +1,8 @@
 // Autotuner for the FP32 filter kernels: times each tile / register-blocking variant of the
 // fused stencil + Chebyshev update, and each form of the nonlocal apply (per point over all
 // column blocks, alpha rows staged per chunk of covered points, or per point with its Chi
-// values hoisted out of the column loop), on scratch blocks of the
+// values hoisted out of the column loop), and each form of the FP32 projection (per image
+// segment, or per range of consecutive covered points), on scratch blocks of the
 // context's grid and projector set, and keeps the fastest of each. The stencil variants
 // compute the same IEEE operation sequence per point, and so do the two apply forms, so the
 // choice changes speed only, never results.
@@ -87,9 +88,34 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
                     }
                     if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
                 }
+                if (rc == SGPU_OK) ctx->tune_apply_ms[v] = tmin;
                 if (rc == SGPU_OK && tmin < tbest) { tbest = tmin; abest = v; }
             }
             ctx->nl_apply_variant = rc == SGPU_OK ? abest : saved_a;
+            // FP32 projection: per image segment vs per range of covered points
+            const int saved_p = ctx->nl_project_variant;
+            float pbest = 1e30f;
+            int pv = saved_p;
+            for (int v = 0; v < 2 && rc == SGPU_OK; v++) {
+                ctx->nl_project_variant = v;
+                float t = 0.f, tmin = 1e30f;
+                for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
+                    if (cudaEventRecord(ctx->ev0, st) != cudaSuccess) { rc = SGPU_ERR_CUDA; break; }
+                    if ((rc = launch_nonlocal_project<float>(ctx, ncol, X, Nd, alpha, lda, st)) !=
+                        SGPU_OK)
+                        break;
+                    if (cudaEventRecord(ctx->ev1, st) != cudaSuccess ||
+                        cudaEventSynchronize(ctx->ev1) != cudaSuccess ||
+                        cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) != cudaSuccess) {
+                        rc = SGPU_ERR_CUDA;
+                        break;
+                    }
+                    if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
+                }
+                if (rc == SGPU_OK) ctx->tune_project_ms[v] = tmin;
+                if (rc == SGPU_OK && tmin < pbest) { pbest = tmin; pv = v; }
+            }
+            ctx->nl_project_variant = rc == SGPU_OK ? pv : saved_p;
             cudaFreeAsync(alpha, st);
         }
     }
@@ -124,6 +150,39 @@ int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant)
         return SGPU_ERR_ARG;
     }
     ctx->nl_apply_variant = variant;
+    return SGPU_OK;
+}
+
+int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant)
+{
+    if (!ctx || variant < 0 || variant > 1) {
+        set_error("sgpu_set_nonlocal_project_variant: variant must be 0 or 1");
+        return SGPU_ERR_ARG;
+    }
+    ctx->nl_project_variant = variant;
+    return SGPU_OK;
+}
+
+int sgpu_get_tuning(sgpu_ctx *ctx, double *apply_ms, double *project_ms)
+{
+    if (!ctx) {
+        set_error("sgpu_get_tuning: null context");
+        return SGPU_ERR_ARG;
+    }
+    for (int v = 0; v < 3 && apply_ms; v++) apply_ms[v] = ctx->tune_apply_ms[v];
+    for (int v = 0; v < 2 && project_ms; v++) project_ms[v] = ctx->tune_project_ms[v];
+    return SGPU_OK;
+}
+
+int sgpu_get_variants(sgpu_ctx *ctx, int *stencil, int *nl_apply, int *nl_project)
+{
+    if (!ctx) {
+        set_error("sgpu_get_variants: null context");
+        return SGPU_ERR_ARG;
+    }
+    if (stencil) *stencil = ctx->stencil_variant;
+    if (nl_apply) *nl_apply = ctx->nl_apply_variant;
+    if (nl_project) *nl_project = ctx->nl_project_variant;
     return SGPU_OK;
 }
 

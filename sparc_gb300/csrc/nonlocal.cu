@@ -141,6 +141,97 @@ __global__ void __launch_bounds__(kProjThreads)
     }
 }
 
+// Range projection (FP32): block = one range of at most kRangePts consecutive covered points
+// (grid order). The range's entries, regrouped by image into work items, have their Chi rows
+// (range_jp values each) and point indices staged in shared memory once. For each group of
+// NC = 64 columns the block gathers x[range points, group] into shared memory (every covered
+// x element is read once per launch, in grid order, whatever the number of spheres over it),
+// then each warp takes work items in turn: lane l accumulates alpha[0..MAXJ-1] of columns
+// 2l, 2l+1 over the item's entries and adds them atomically, with dV * Gamma folded in.
+template <int MAXJ>
+__global__ void __launch_bounds__(256)
+    k_nl_project_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
+                       const int *__restrict__ rng_item0, const int *__restrict__ item_e0,
+                       const int2 *__restrict__ item_row, const int *__restrict__ pe_lp,
+                       const float *__restrict__ pe_chi, const int *__restrict__ cov_pt,
+                       const float *__restrict__ gamma, int ncol, const float *__restrict__ x,
+                       long ldx, float *__restrict__ alpha, long lda, float dV)
+{
+    constexpr int NC = 64, XLD = NC + 2;             // columns per group, padded x row
+    constexpr int MAXJP = (MAXJ + 3) / 4 * 4;        // staged Chi values per entry
+    constexpr int GB = 16;                           // gathers in flight per thread
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *xs = reinterpret_cast<float *>(smem_raw);  // [kRangePts][XLD]
+    float *cs = xs + kRangePts * XLD;                 // [entries][MAXJP]
+    const int r = blockIdx.x;
+    const int p0 = rng_pt0[r], npt = rng_pt0[r + 1] - p0;
+    const int eb = rng_ent0[r], ne = rng_ent0[r + 1] - eb;
+    const int ib = rng_item0[r], ni = rng_item0[r + 1] - ib;
+    int *lps = reinterpret_cast<int *>(cs + (size_t)ne * MAXJP);  // [entries]
+    int *gps = lps + ne;                                          // [kRangePts]
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+    for (int i = t; i < npt; i += 256) gps[i] = cov_pt[p0 + i];
+    for (int i = t; i < ne; i += 256) lps[i] = pe_lp[eb + i];
+    {
+        const float4 *src = reinterpret_cast<const float4 *>(pe_chi + (long)eb * MAXJP);
+        float4 *dst = reinterpret_cast<float4 *>(cs);
+        for (int i = t; i < ne * (MAXJP / 4); i += 256) dst[i] = __ldg(src + i);
+    }
+    for (int n0 = 0; n0 < ncol; n0 += NC) {
+        __syncthreads();  // staging done / previous group consumed
+        for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
+            float v[GB];
+#pragma unroll
+            for (int u = 0; u < GB; u++) {
+                const int idx = base + t + u * 256;
+                const int lp = idx % kRangePts, c = idx / kRangePts;
+                v[u] = (lp < npt && n0 + c < ncol) ? __ldg(x + (long)(n0 + c) * ldx + gps[lp])
+                                                   : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < GB; u++) {
+                const int idx = base + t + u * 256;
+                xs[(idx % kRangePts) * XLD + idx / kRangePts] = v[u];
+            }
+        }
+        __syncthreads();
+        for (int it = warp; it < ni; it += 8) {
+            const int2 row = item_row[ib + it];  // (first projector row, projector count)
+            const int e0 = item_e0[ib + it] - eb, e1 = item_e0[ib + it + 1] - eb;
+            float acc0[MAXJ], acc1[MAXJ];
+#pragma unroll
+            for (int j = 0; j < MAXJ; j++) acc0[j] = acc1[j] = 0.f;
+            for (int e = e0; e < e1; e++) {
+                const float2 xv = *reinterpret_cast<const float2 *>(xs + lps[e] * XLD + 2 * lane);
+                const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
+#pragma unroll
+                for (int q = 0; q < MAXJP / 4; q++) {
+                    const float4 c4 = cv[q];
+                    const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                    for (int w = 0; w < 4; w++) {
+                        if (q * 4 + w < MAXJ) {
+                            acc0[q * 4 + w] += ce[w] * xv.x;
+                            acc1[q * 4 + w] += ce[w] * xv.y;
+                        }
+                    }
+                }
+            }
+            const int c0 = n0 + 2 * lane;
+#pragma unroll
+            for (int j = 0; j < MAXJ; j++) {
+                if (j < row.y) {
+                    const float s = dV * gamma[row.x + j];
+                    float *dst = alpha + (long)(row.x + j) * lda + c0;
+                    if (c0 < ncol) atomicAdd(dst, s * acc0[j]);
+                    if (c0 + 1 < ncol) atomicAdd(dst + 1, s * acc1[j]);
+                }
+            }
+        }
+    }
+}
+
 // Apply: one thread per covered grid point, looping over column blocks of CB; alpha rows are
 // read as vectors (VW elements per load, broadcast across the warp when neighbouring points
 // share an atom).
@@ -382,12 +473,41 @@ static int project_launch(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alph
     return SGPU_OK;
 }
 
+template <int MAXJ>
+static int project_range_launch(sgpu_ctx *ctx, int ncol, const float *x, long ldx, float *alpha,
+                                long lda, cudaStream_t st)
+{
+    const Nonlocal &nl = ctx->nl;
+    const size_t smem = sizeof(float) * ((size_t)kRangePts * 66 + (size_t)nl.max_range_ent * nl.range_jp) +
+                        sizeof(int) * ((size_t)nl.max_range_ent + kRangePts);
+    auto kern = k_nl_project_range<MAXJ>;
+    SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
+    kern<<<nl.nrange, 256, smem, st>>>(nl.rng_pt0, nl.rng_ent0, nl.rng_item0, nl.item_e0,
+                                       nl.item_row, nl.pe_lp, nl.pe_chi32, nl.cov_pt, nl.gamma32,
+                                       ncol, x, ldx, alpha, lda, (float)ctx->dV);
+    return SGPU_OK;
+}
+
 template <typename T>
 int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
                             cudaStream_t st)
 {
     const Nonlocal &nl = ctx->nl;
     if (!ctx->has_nl || nl.nimg == 0 || ncol <= 0) return SGPU_OK;
+    if constexpr (sizeof(T) == 4) {
+        if (ctx->nl_project_variant == 1 && nl.nrange > 0) {
+            if (nl.range_jp == 12)
+                SGPU_TRY(project_range_launch<9>(ctx, ncol, x, ldx, alpha, lda, st));
+            else if (nl.range_jp == 20)
+                SGPU_TRY(project_range_launch<18>(ctx, ncol, x, ldx, alpha, lda, st));
+            else
+                SGPU_TRY(project_range_launch<32>(ctx, ncol, x, ldx, alpha, lda, st));
+            SGPU_CUDA_TRY(cudaGetLastError());
+            return SGPU_OK;
+        }
+    }
     if (nl.max_np <= 9)
         SGPU_TRY(project_launch<T, 9>(ctx, ncol, x, ldx, alpha, lda, st));
     else if (nl.max_np <= 18)
@@ -481,7 +601,9 @@ void nonlocal_free(Nonlocal &nl)
     void *ptrs[] = {nl.ip_displ, nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off,
                     nl.grid_pos, nl.chi64,    nl.chi32,   nl.gamma64, nl.gamma32,
                     nl.cov_pt,   nl.cov_ptr,  nl.ent_chi, nl.ent_meta, nl.seg_img,
-                    nl.seg_start, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows};
+                    nl.seg_start, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows,
+                    nl.rng_pt0,  nl.rng_ent0, nl.rng_item0, nl.item_e0, nl.item_row,
+                    nl.pe_lp,    nl.pe_chi32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     nl = Nonlocal();
@@ -588,6 +710,69 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
             nl.max_chunk_rows = std::max(nl.max_chunk_rows, rows);
         }
     }
+    // range projection: ranges of at most kRangePts consecutive covered points and
+    // kRangeMaxEnt entries; within a range the entries are regrouped by image (then by point)
+    // into work items of at most kRangeItemEnt entries, with their Chi rows in FP32
+    std::vector<int> rng_pt0(1, 0), rng_ent0(1, 0), rng_item0(1, 0), item_e0(1, 0), pe_lp;
+    std::vector<int2> item_row;
+    std::vector<float> pe_chi;
+    {
+        const int mj = nl.max_np <= 9 ? 9 : nl.max_np <= 18 ? 18 : 32;
+        nl.range_jp = (mj + 3) / 4 * 4;
+        pe_chi.reserve((size_t)npos * nl.range_jp);
+        pe_lp.reserve(npos);
+        std::vector<std::pair<long, int>> order;  // (image * Nd-span key, entry)
+        int p = 0;
+        while (p < nl.ncov) {
+            const int q0 = p;
+            int ents = 0;
+            while (p < nl.ncov && p - q0 < kRangePts &&
+                   ents + (covptr[p + 1] - covptr[p]) <= kRangeMaxEnt) {
+                ents += covptr[p + 1] - covptr[p];
+                p++;
+            }
+            if (p == q0) {
+                set_error("set_nonlocal: more than " + std::to_string(kRangeMaxEnt) +
+                          " projector spheres overlap at one grid point");
+                return SGPU_ERR_ARG;
+            }
+            order.clear();
+            for (int e = covptr[q0]; e < covptr[p]; e++) order.push_back({(long)ent_meta[e].w, e});
+            // entries are already in point order; a stable sort by image keeps it per image
+            std::stable_sort(order.begin(), order.end(),
+                             [](const std::pair<long, int> &a, const std::pair<long, int> &b) {
+                                 return a.first < b.first;
+                             });
+            size_t k = 0;
+            while (k < order.size()) {
+                const int g = (int)order[k].first;
+                size_t k1 = k;
+                while (k1 < order.size() && order[k1].first == g &&
+                       (int)(k1 - k) < kRangeItemEnt)
+                    k1++;
+                const int4 meta = ent_meta[order[k].second];
+                item_row.push_back(make_int2(meta.x, meta.y));
+                for (size_t u = k; u < k1; u++) {
+                    const int e = order[u].second;
+                    // the local point: entries of point c lie in [covptr[c], covptr[c+1])
+                    const int c = (int)(std::upper_bound(covptr.begin() + q0, covptr.begin() + p + 1,
+                                                         e) - covptr.begin()) - 1;
+                    pe_lp.push_back(c - q0);
+                    const int4 m = ent_meta[e];
+                    for (int j = 0; j < nl.range_jp; j++)
+                        pe_chi.push_back(j < m.y ? (float)chi[ent_chi[e] + (long)j * m.z] : 0.f);
+                }
+                item_e0.push_back((int)pe_lp.size());
+                k = k1;
+            }
+            rng_pt0.push_back(p);
+            rng_ent0.push_back((int)pe_lp.size());
+            rng_item0.push_back((int)item_row.size());
+            nl.max_range_ent = std::max(nl.max_range_ent, ents);
+        }
+        nl.nrange = (int)rng_pt0.size() - 1;
+        nl.nitem = (int)item_row.size();
+    }
     // projection work split: segments of at most kSegPts points per image
     std::vector<int> seg_img, seg_start;
     for (int g = 0; g < nimg; g++)
@@ -623,6 +808,13 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(ent_slot, ent_slot.data(), ent_slot.size());
     UP(chunk_row_ptr, chunk_row_ptr.data(), chunk_row_ptr.size());
     UP(chunk_rows, chunk_rows.data(), chunk_rows.size());
+    UP(rng_pt0, rng_pt0.data(), rng_pt0.size());
+    UP(rng_ent0, rng_ent0.data(), rng_ent0.size());
+    UP(rng_item0, rng_item0.data(), rng_item0.size());
+    UP(item_e0, item_e0.data(), item_e0.size());
+    UP(item_row, item_row.data(), item_row.size());
+    UP(pe_lp, pe_lp.data(), pe_lp.size());
+    UP(pe_chi32, pe_chi.data(), pe_chi.size());
 #undef UP
     if (rc != SGPU_OK) {
         nonlocal_free(nl);

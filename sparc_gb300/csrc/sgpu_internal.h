@@ -16,6 +16,9 @@ namespace sgpu {
 
 constexpr int kMaxFDn = 6;  // the library is specialised for FD order 12 (radius 6)
 constexpr int kApplyChunkPts = 128;  // covered points per chunk of the staged nonlocal apply
+constexpr int kRangePts = 256;       // covered points per range of the range projection
+constexpr int kRangeMaxEnt = 640;    // entries per range at most (bounds its staged Chi)
+constexpr int kRangeItemEnt = 96;    // entries per work item of the range projection at most
 
 // thread-local error text, returned by sgpu_last_error()
 void set_error(const std::string &msg);
@@ -78,6 +81,16 @@ struct Nonlocal {
     int *ent_slot = nullptr;       // nent: staged row of the entry's atom within its chunk
     int *chunk_row_ptr = nullptr;  // nchunk + 1
     int *chunk_rows = nullptr;     // alpha rows staged per chunk
+    // range projection (FP32): ranges of consecutive covered points, each with its entries
+    // regrouped by image into work items of at most kRangeItemEnt entries
+    int nrange = 0, nitem = 0, max_range_ent = 0, range_jp = 0;
+    int *rng_pt0 = nullptr;     // nrange + 1: first covered point of each range
+    int *rng_ent0 = nullptr;    // nrange + 1: first entry (range order) of each range
+    int *rng_item0 = nullptr;   // nrange + 1: first work item of each range
+    int *item_e0 = nullptr;     // nitem + 1: first entry (range order) of each item
+    int2 *item_row = nullptr;   // nitem: (first projector row, projector count)
+    int *pe_lp = nullptr;       // entries in range order: point index within the range
+    float *pe_chi32 = nullptr;  // entries in range order: Chi values, range_jp per entry
 };
 
 struct Workspace {
@@ -137,7 +150,10 @@ struct sgpu_ctx {
     sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
     int stencil_variant = 0;   // FP32 stencil kernel variant (autotune.cu)
     bool stencil_tuned = false;
-    int nl_apply_variant = 0;  // real nonlocal apply: 0 per point over all columns, 1 staged
+    int nl_apply_variant = 0;  // real nonlocal apply: 0 per point over all columns, 1 staged,
+                               // 2 per point with the Chi values hoisted
+    int nl_project_variant = 0;  // FP32 projection: 0 per image segment, 1 per point range
+    double tune_apply_ms[3] = {0, 0, 0}, tune_project_ms[2] = {0, 0};  // last autotune timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on

@@ -163,6 +163,34 @@ def test_nonlocal_apply_forms_identical(gpu_available, dtype):
     np.testing.assert_array_equal(outs[0], outs[2])
 
 
+@pytest.mark.parametrize("natom,rc,lmax", [(7, 1.6, 2), (40, 3.0, 2), (12, 2.0, 3)])
+def test_fp32_projection_forms_agree(gpu_available, natom, rc, lmax):
+    """The per-segment and the per-range FP32 projection agree to FP32 rounding, and both
+    match the oracle: sparse spheres, heavy overlap (ranges cut by their entry count, work
+    items cut by size) and 16 projectors per atom."""
+    shape = (30, 26, 22)
+    rng = np.random.default_rng(31 + natom)
+    h = (0.41, 0.37, 0.45)
+    grid = dict(Nx=shape[0], Ny=shape[1], Nz=shape[2], FDn=6, cx=fd_d2_coeffs(6, h[0]),
+                cy=fd_d2_coeffs(6, h[1]), cz=fd_d2_coeffs(6, h[2]), dV=h[0] * h[1] * h[2])
+    Nd = shape[0] * shape[1] * shape[2]
+    veff = rng.normal(0.0, 1.0, Nd)
+    nl = synthetic_nonlocal(rng, shape, 0.4, natom=natom, rc=rc, lmax=lmax)
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    x = rng.uniform(-1, 1, (70, Nd))  # two column groups of 64, the second partial
+    outs = []
+    for v in (0, 1):
+        ctx.set_nonlocal_project_variant(v)
+        X = x.astype(np.float32); Y = np.zeros_like(X)
+        ctx.ChebyshevFiltering_f32(X, Y, 3, 0.5, 50.0, -1.0)
+        outs.append(Y.astype(np.float64))
+    _, Yo = o.chebyshev(veff, 3, 0.5, 50.0, -1.0, x)
+    for Y in outs:
+        assert rel_err(Y, Yo) < TOL32_FILTER
+    assert rel_err(outs[1], outs[0]) < 1e-5
+
+
 def test_device_pointers_match_host(gpu_available):
     import torch
     grid, nl, veff, rng = _random_case((24, 20, 16), seed=9)
