@@ -556,8 +556,8 @@ def main():
                        "stencil_variant": {"chosen": kernel_name,
                                            "autotune_ms": [round(float(v), 4) for v in variant_ms]},
                        "nonlocal_forms": {
-                           "apply": ["per point", "staged per chunk", "per point, Chi hoisted"][
-                               forms["nl_apply"]],
+                           "apply": ["per point", "staged per chunk", "per point, Chi hoisted",
+                                     "dense per chunk"][forms["nl_apply"]],
                            "project": ["per image segment", "per range of covered points"][
                                forms["nl_project"]],
                            "autotune_ms": {k: [round(float(v), 4) for v in vs]

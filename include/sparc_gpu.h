@@ -417,8 +417,9 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
 
 /* Fix the form of the real nonlocal apply (0: one thread per covered point over all column
  * blocks; 1: alpha rows staged in shared memory per chunk of covered points; 2: as 0 with the
- * point's Chi values loaded once before the column loop); sgpu_autotune times all three.
- * Same results whichever is used. */
+ * point's Chi values loaded once before the column loop; 3: FP32 only, a dense product per
+ * chunk of covered points over the alpha rows of the chunk's atoms); sgpu_autotune times all
+ * four. Forms 0-2 give identical results; form 3 sums in another order (FP32 rounding). */
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
 
 /* Fix the form of the FP32 nonlocal projection (0: one block per segment of one image's
@@ -431,8 +432,8 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
  * pointer may be NULL. */
 int sgpu_get_variants(sgpu_ctx *ctx, int *stencil, int *nl_apply, int *nl_project);
 
-/* Milliseconds per launch that the last sgpu_autotune measured for the three nonlocal apply
- * forms (apply_ms[3]) and the two FP32 projection forms (project_ms[2]); zeros before any
+/* Milliseconds per launch that the last sgpu_autotune measured for the four nonlocal apply
+ * forms (apply_ms[4]) and the two FP32 projection forms (project_ms[2]); zeros before any
  * tuning or without projectors. Either pointer may be NULL. */
 int sgpu_get_tuning(sgpu_ctx *ctx, double *apply_ms, double *project_ms);
 

@@ -29,6 +29,7 @@ constexpr int kProjThreads = 256;
 constexpr int kSegPts = 512;  // points of one image handled by one projection block
 constexpr int kApplyChunk = kApplyChunkPts;   // covered points per block of the staged apply
 constexpr size_t kApplyStageMax = 96 * 1024;  // staged alpha rows must fit this (bytes)
+constexpr size_t kApplyDenseMax = 150 * 1024; // dense-chunk apply: staged rows and Chi (bytes)
 
 template <typename T, int CB>
 struct VecOf;
@@ -147,7 +148,8 @@ __global__ void __launch_bounds__(kProjThreads)
 // NC = 64 columns the block gathers x[range points, group] into shared memory (every covered
 // x element is read once per launch, in grid order, whatever the number of spheres over it),
 // then each warp takes work items in turn: lane l accumulates alpha[0..MAXJ-1] of columns
-// 2l, 2l+1 over the item's entries and adds them atomically, with dV * Gamma folded in.
+// 2l, 2l+1 over the item's entries and adds them atomically (one 8-byte atomic per pair),
+// with dV * Gamma folded in. lda must be even.
 template <int MAXJ>
 __global__ void __launch_bounds__(256)
     k_nl_project_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
@@ -178,7 +180,11 @@ __global__ void __launch_bounds__(256)
         float4 *dst = reinterpret_cast<float4 *>(cs);
         for (int i = t; i < ne * (MAXJP / 4); i += 256) dst[i] = __ldg(src + i);
     }
-    for (int n0 = 0; n0 < ncol; n0 += NC) {
+    // column groups in an order rotated by the range index, so that neighbouring ranges (which
+    // share atoms) add into different alpha columns at any one time
+    const int ngroup = (ncol + NC - 1) / NC;
+    for (int gi = 0; gi < ngroup; gi++) {
+        const int n0 = ((gi + r) % ngroup) * NC;
         __syncthreads();  // staging done / previous group consumed
         for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
             float v[GB];
@@ -224,8 +230,11 @@ __global__ void __launch_bounds__(256)
                 if (j < row.y) {
                     const float s = dV * gamma[row.x + j];
                     float *dst = alpha + (long)(row.x + j) * lda + c0;
-                    if (c0 < ncol) atomicAdd(dst, s * acc0[j]);
-                    if (c0 + 1 < ncol) atomicAdd(dst + 1, s * acc1[j]);
+                    if (c0 + 1 < ncol)  // lda and c0 are even: an 8-byte aligned pair
+                        atomicAdd(reinterpret_cast<float2 *>(dst),
+                                  make_float2(s * acc0[j], s * acc1[j]));
+                    else if (c0 < ncol)
+                        atomicAdd(dst, s * acc0[j]);
                 }
             }
         }
@@ -368,6 +377,76 @@ __global__ void __launch_bounds__(256)
         for (int c = 0; c < CB; c++)
             if (n0 + c < ncol) out[(long)(n0 + c) * ldo + p] = ov[c] + scale * acc[c];
     }
+}
+
+// Apply as a dense product per chunk (FP32): block = (chunk of kApplyChunk consecutive
+// covered points, 64 columns), 256 threads = 128 points x 2 column halves. The alpha rows of
+// the chunk's atoms (nr rows, listed in chunk_rows) and a dense Chi matrix C[nr][points]
+// (zero where an atom's sphere misses a point; images of one atom over one point summed) are
+// staged in shared memory, then thread (point, half) accumulates its 32 outputs over the nr
+// rows: one C value and eight 16-byte alpha loads (the same for the whole warp) per 32 FMAs;
+// then its 32 output values are read together and written back. Summation runs over staged
+// rows, so results agree with the per-point forms to FP32 rounding.
+__global__ void __launch_bounds__(256, 2)
+    k_nl_apply_dense(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
+                     const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
+                     const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
+                     const int *__restrict__ chunk_rows, const float *__restrict__ chi, int ncol,
+                     const float *__restrict__ alpha, long lda, float scale,
+                     float *__restrict__ out, long ldo)
+{
+    constexpr int NC = 64, HC = 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int c = blockIdx.x;
+    const int n0 = blockIdx.y * NC;
+    const int r0 = chunk_row_ptr[c], nr = chunk_row_ptr[c + 1] - r0;
+    float *As = reinterpret_cast<float *>(smem_raw);  // [nr][NC]
+    float *Cs = As + (size_t)nr * NC;                 // [nr][kApplyChunk]
+    const int t = threadIdx.x;
+    const int pt = t % kApplyChunk, half = t / kApplyChunk;
+    const int cidx = c * kApplyChunk + pt;
+    const bool live = cidx < ncov;
+    const long p = live ? cov_pt[cidx] : 0;
+    const int cb = n0 + half * HC;
+    for (int i = t; i < nr * kApplyChunk; i += 256) Cs[i] = 0.f;
+    for (int i = t; i < nr * NC; i += 256) {
+        const int r = i / NC, cc = i % NC;
+        As[i] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : 0.f;
+    }
+    __syncthreads();
+    if (half == 0 && live) {  // one thread per point writes its column of C
+        for (int e = cov_ptr[cidx]; e < cov_ptr[cidx + 1]; e++) {
+            const int4 meta = ent_meta[e];
+            const float *__restrict__ ch = chi + ent_chi[e];
+            float *col = Cs + (size_t)ent_slot[e] * kApplyChunk + pt;
+            for (int j = 0; j < meta.y; j++) col[(size_t)j * kApplyChunk] += __ldg(ch + (long)j * meta.z);
+        }
+    }
+    __syncthreads();
+    float acc[HC];
+#pragma unroll
+    for (int q = 0; q < HC; q++) acc[q] = 0.f;
+    const float4 *Ah = reinterpret_cast<const float4 *>(As + half * HC);
+#pragma unroll 2
+    for (int k = 0; k < nr; k++) {
+        const float cv = Cs[(size_t)k * kApplyChunk + pt];
+        const float4 *a4 = Ah + (size_t)k * (NC / 4);
+#pragma unroll
+        for (int q = 0; q < HC / 4; q++) {
+            const float4 a = a4[q];
+            acc[4 * q] += cv * a.x;
+            acc[4 * q + 1] += cv * a.y;
+            acc[4 * q + 2] += cv * a.z;
+            acc[4 * q + 3] += cv * a.w;
+        }
+    }
+    if (!live) return;
+    float ov[HC];  // all loads of the output block in flight together
+#pragma unroll
+    for (int q = 0; q < HC; q++) ov[q] = cb + q < ncol ? out[(long)(cb + q) * ldo + p] : 0.f;
+#pragma unroll
+    for (int q = 0; q < HC; q++)
+        if (cb + q < ncol) out[(long)(cb + q) * ldo + p] = ov[q] + scale * acc[q];
 }
 
 // Apply, staged: one block per (chunk of kApplyChunk consecutive covered points, block of CB
@@ -554,6 +633,22 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
 #undef SGPU_STAGED
         SGPU_CUDA_TRY(cudaGetLastError());
         return SGPU_OK;
+    }
+    if constexpr (sizeof(T) == 4) {
+        const size_t dsm = sizeof(float) * (size_t)nl.max_chunk_rows * (64 + kApplyChunk);
+        if (ctx->nl_apply_variant == 3 && nl.nchunk > 0 && dsm <= kApplyDenseMax) {
+            SGPU_CUDA_TRY(cudaFuncSetAttribute(k_nl_apply_dense,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)std::max<size_t>(dsm, 16)));
+            const dim3 dg(nl.nchunk, (ncol + 63) / 64);
+            ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+            k_nl_apply_dense<<<dg, 256, std::max<size_t>(dsm, 16), st>>>(
+                nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.ent_slot,
+                nl.chunk_row_ptr, nl.chunk_rows, nl.chi32, ncol, alpha, lda, (float)scale, out,
+                ldo);
+            SGPU_CUDA_TRY(cudaGetLastError());
+            return SGPU_OK;
+        }
     }
     const dim3 grid((nl.ncov + 255) / 256);
     ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
