@@ -57,6 +57,12 @@ def parse():
     ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution blocks")
     ap.add_argument("--no-c4", action="store_true", help="skip the 216-atom SCF block")
     ap.add_argument("--no-c3", action="store_true", help="skip the batched k-point/spin block")
+    ap.add_argument("--stencil-variant", type=int, default=None,
+                    help="use this FP32 stencil variant instead of the tuned one (profiling)")
+    ap.add_argument("--nl-apply", type=int, default=None,
+                    help="use this nonlocal apply form instead of the tuned one (profiling)")
+    ap.add_argument("--nl-project", type=int, default=None,
+                    help="use this FP32 projection form instead of the tuned one (profiling)")
     return ap.parse_args()
 
 
@@ -416,6 +422,13 @@ def main():
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     # pick the FP32 stencil variant for this grid (all variants give identical results)
     variant, variant_ms = ctx.autotune(ncol=min(ncol, 64))
+    if args.stencil_variant is not None:
+        variant = args.stencil_variant
+        ctx.set_stencil_variant(variant)
+    if args.nl_apply is not None:
+        ctx.set_nonlocal_apply_variant(args.nl_apply)
+    if args.nl_project is not None:
+        ctx.set_nonlocal_project_variant(args.nl_project)
     forms = ctx.variants()
     kernel_name = ["k_stencil_f32x2<32x16>", "k_stencil_f32_b22<32x16>",
                    "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
