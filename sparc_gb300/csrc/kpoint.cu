@@ -249,11 +249,14 @@ __device__ __forceinline__ void nl_apply_z_body(
 }
 
 // Staged apply (as k_nl_apply_staged for real blocks): block = (chunk of kApplyChunkZ covered
-// points, CB columns); the alpha rows of the chunk's atoms are staged in shared memory, and
+// points, CB columns); the alpha rows of the chunk's atoms are staged in shared memory (each
+// row padded by 16 bytes, so distinct rows read by one warp start four banks apart), and
 // each entry's contribution is (e^{-i theta_g} Chi_j) alpha_j, with the phase-scaled Chi value
 // formed once per projector.
 constexpr int kApplyChunkZ = kApplyChunkPts;    // the chunking of the nonlocal upload
 constexpr size_t kZStageMax = 96 * 1024;         // staged rows must fit this (bytes)
+template <typename CT, int CB>
+__host__ __device__ constexpr int zstage_ld() { return CB + (int)(16 / sizeof(CT)); }
 template <typename CT, int CB, int NPMAX>
 __device__ __forceinline__ void nl_apply_z_staged_body(
     int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
@@ -272,9 +275,10 @@ __device__ __forceinline__ void nl_apply_z_staged_body(
     for (int q = 0; q < CB; q++)
         ov[q] = (live && n0 + q < ncol) ? out[(long)(n0 + q) * ldo + p] : CT{0, 0};
     const int r0 = chunk_row_ptr[c], nr = chunk_row_ptr[c + 1] - r0;
+    constexpr int LDS = zstage_ld<CT, CB>();
     for (int e = threadIdx.x; e < nr * CB; e += blockDim.x) {
         const int r = e / CB, cc = e % CB;
-        S[e] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : CT{0, 0};
+        S[r * LDS + cc] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : CT{0, 0};
     }
     __syncthreads();
     if (!live) return;
@@ -286,7 +290,7 @@ __device__ __forceinline__ void nl_apply_z_staged_body(
         const int4 meta = ent_meta[e];
         const int np = meta.y, ndc = meta.z;
         const double *__restrict__ ch = chi + ent_chi[e];
-        const CT *srow = S + (long)ent_slot[e] * CB;
+        const CT *srow = S + (long)ent_slot[e] * LDS;
         const double2 ph = img_phase[meta.w];  // e^{-i theta} = (cos, -sin)
 #pragma unroll
         for (int j = 0; j < NPMAX; j++) {
@@ -294,7 +298,7 @@ __device__ __forceinline__ void nl_apply_z_staged_body(
             const double cv = __ldg(ch + (long)j * ndc);
             const CT t{(RT)(cv * ph.x), (RT)(-cv * ph.y)};
 #pragma unroll
-            for (int q = 0; q < CB; q++) acc[q] = cadd(acc[q], cmul(t, srow[j * CB + q]));
+            for (int q = 0; q < CB; q++) acc[q] = cadd(acc[q], cmul(t, srow[j * LDS + q]));
         }
     }
 #pragma unroll
@@ -597,7 +601,7 @@ static int nonlocal_z(sgpu_ctx *ctx, int ncol, const CT *x, long ldx, CT *out, l
     {
         ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
         constexpr int CB = zapply_cb<CT>();
-        const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * CB;
+        const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * zstage_ld<CT, CB>();
         if (nl.nchunk > 0 && stage <= kZStageMax) {
             const dim3 sg(nl.nchunk, (ncol + CB - 1) / CB);
             auto launch = [&](auto kern) -> int {
@@ -819,7 +823,8 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
     int maxcol = 0;
     for (int b = 0; b < nblk; b++) maxcol = std::max(maxcol, blk[b].ncol);
     if (has_nl) {  // shared-memory size of the staged apply, set before any capture
-        const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * zapply_cb<CT>();
+        const size_t stage =
+            sizeof(CT) * (size_t)nl.max_chunk_rows * zstage_ld<CT, zapply_cb<CT>()>();
         if (nl.nchunk > 0 && stage <= kZStageMax) {
             const int sm = (int)std::max<size_t>(stage, 16);
             SGPU_CUDA_TRY(cudaFuncSetAttribute(k_nl_apply_zb_staged<CT, 9>,
@@ -868,7 +873,7 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
             if (has_nl) {
                 ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
                 constexpr int CB = zapply_cb<CT>();
-                const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * CB;
+                const size_t stage = sizeof(CT) * (size_t)nl.max_chunk_rows * zstage_ld<CT, CB>();
                 if (nl.nchunk > 0 && stage <= kZStageMax) {
                     const dim3 sg(nl.nchunk, (unsigned)((maxcol + CB - 1) / CB), nblk);
                     const size_t sm = std::max<size_t>(stage, 16);

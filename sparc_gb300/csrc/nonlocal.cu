@@ -451,9 +451,11 @@ __global__ void __launch_bounds__(256, 2)
 
 // Apply, staged: one block per (chunk of kApplyChunk consecutive covered points, block of CB
 // columns). The alpha rows of every atom that touches the chunk are staged once in shared
-// memory (rows listed in chunk_rows), and each thread accumulates its point's CB outputs from
-// there; the output block is read-modified-written once. Neighbouring covered points share
-// atoms, so one staged row serves many threads.
+// memory (rows listed in chunk_rows, each padded by 16 bytes so that rows start four banks
+// apart: up to eight distinct rows per 16-byte warp read are served in one pass), and each
+// thread accumulates its point's CB outputs from there with 16-byte reads; the output block
+// is read-modified-written once. Neighbouring covered points share atoms, so one staged row
+// serves many threads.
 template <typename T, int CB, int NPMAX>
 __global__ void __launch_bounds__(kApplyChunk)
     k_nl_apply_staged(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
@@ -463,8 +465,11 @@ __global__ void __launch_bounds__(kApplyChunk)
                       const T *__restrict__ alpha, long lda, T scale, T *__restrict__ out,
                       long ldo)
 {
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int LDS = CB + VW;  // padded row: consecutive rows start four banks apart
+    using V = typename VecOf<T, VW>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *S = reinterpret_cast<T *>(smem_raw);  // [rows][CB]
+    T *S = reinterpret_cast<T *>(smem_raw);  // [rows][LDS]
     const int c = blockIdx.x;
     const int n0 = blockIdx.y * CB;
     const int cidx = c * kApplyChunk + threadIdx.x;
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(kApplyChunk)
     const int r0 = chunk_row_ptr[c], nr = chunk_row_ptr[c + 1] - r0;
     for (int e = threadIdx.x; e < nr * CB; e += blockDim.x) {
         const int r = e / CB, cc = e % CB;
-        S[e] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : T(0);
+        S[r * LDS + cc] = n0 + cc < ncol ? alpha[(long)chunk_rows[r0 + r] * lda + n0 + cc] : T(0);
     }
     __syncthreads();
     if (!live) return;
@@ -490,7 +495,7 @@ __global__ void __launch_bounds__(kApplyChunk)
         const int4 meta = ent_meta[e];  // (first projector row, projector count, ndc, image)
         const int np = meta.y, ndc = meta.z;
         const T *__restrict__ ch = chi + ent_chi[e];
-        const T *__restrict__ srow = S + (long)ent_slot[e] * CB;
+        const T *__restrict__ srow = S + (long)ent_slot[e] * LDS;
         T cvs[NPMAX];
 #pragma unroll
         for (int j = 0; j < NPMAX; j++) cvs[j] = j < np ? __ldg(ch + (long)j * ndc) : T(0);
@@ -498,8 +503,14 @@ __global__ void __launch_bounds__(kApplyChunk)
         for (int j = 0; j < NPMAX; j++) {
             if (j >= np) break;
             const T cv = cvs[j];
+            const V *sv = reinterpret_cast<const V *>(srow + j * LDS);
 #pragma unroll
-            for (int q = 0; q < CB; q++) acc[q] += cv * srow[j * CB + q];
+            for (int q = 0; q < CB / VW; q++) {
+                const V a = sv[q];
+                const T *ae = reinterpret_cast<const T *>(&a);
+#pragma unroll
+                for (int w = 0; w < VW; w++) acc[q * VW + w] += cv * ae[w];
+            }
         }
     }
 #pragma unroll
@@ -610,7 +621,7 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
     constexpr int CB = apply_cb<T>();
     constexpr int VW = sizeof(T) == 4 ? 4 : 2;
     constexpr int SCB = sizeof(T) == 4 ? 32 : 16;  // columns per block of the staged form
-    const size_t stage = sizeof(T) * (size_t)nl.max_chunk_rows * SCB;
+    const size_t stage = sizeof(T) * (size_t)nl.max_chunk_rows * (SCB + 16 / sizeof(T));
     if (ctx->nl_apply_variant == 1 && nl.nchunk > 0 && stage <= kApplyStageMax) {
         const dim3 sg(nl.nchunk, (ncol + SCB - 1) / SCB);
         ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);

@@ -304,6 +304,16 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// the same copies to a shared-space byte address
+__device__ __forceinline__ void cp_async4s(unsigned sa, const void *gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8s(unsigned sa, const void *gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group()
 {
@@ -340,8 +350,9 @@ __device__ __forceinline__ void b22_block(const StencilParams<float> &p,
         float2 L[R + 1];
 #pragma unroll
         for (int m = 0; m <= R; m++) L[m] = *reinterpret_cast<const float2 *>(srow + 2 * m);
-        float ax0 = p.c0 * cen.x, ax1 = p.c0 * cen.y;
-        float ay0 = 0.f, ay1 = 0.f, az0 = 0.f, az1 = 0.f;
+        // packed (f32x2) forms of the scalar sequence: each lane rounds exactly as fmaf / * / +
+        float2 ax = __fmul2_rn(cen, make_float2(p.c0, p.c0));
+        float2 ay = make_float2(0.f, 0.f), az = ay;
 #pragma unroll
         for (int r = 1; r <= R; r++) {
             float2 lo, hi;
@@ -356,22 +367,15 @@ __device__ __forceinline__ void b22_block(const StencilParams<float> &p,
             const float2 ys = __fadd2_rn(yv[R + rr - r], yv[R + rr + r]);
             const float2 zsum = rr ? __fadd2_rn(qb[(U + R - r) % Q], qb[(U + R + r) % Q])
                                    : __fadd2_rn(qa[(U + R - r) % Q], qa[(U + R + r) % Q]);
-            ax0 = fmaf(xs.x, p.wx[r], ax0); ax1 = fmaf(xs.y, p.wx[r], ax1);
-            ay0 = fmaf(ys.x, p.wy[r], ay0); ay1 = fmaf(ys.y, p.wy[r], ay1);
-            az0 = fmaf(zsum.x, p.wz[r], az0); az1 = fmaf(zsum.y, p.wz[r], az1);
+            ax = __ffma2_rn(xs, make_float2(p.wx[r], p.wx[r]), ax);
+            ay = __ffma2_rn(ys, make_float2(p.wy[r], p.wy[r]), ay);
+            az = __ffma2_rn(zsum, make_float2(p.wz[r], p.wz[r]), az);
         }
-        float o0 = ax0 + (ay0 + az0), o1 = ax1 + (ay1 + az1);
-        if (hasv) {
-            o0 = fmaf(p.bv, vc[rr].x * cen.x, o0);
-            o1 = fmaf(p.bv, vc[rr].y * cen.y, o1);
-        }
-        o0 *= p.s1;
-        o1 *= p.s1;
-        if (hasz) {
-            o0 = fmaf(p.s2, zc[rr].x, o0);
-            o1 = fmaf(p.s2, zc[rr].y, o1);
-        }
-        o[rr] = make_float2(o0, o1);
+        float2 ov = __fadd2_rn(ax, __fadd2_rn(ay, az));
+        if (hasv) ov = __ffma2_rn(make_float2(p.bv, p.bv), __fmul2_rn(vc[rr], cen), ov);
+        ov = __fmul2_rn(ov, make_float2(p.s1, p.s1));
+        if (hasz) ov = __ffma2_rn(make_float2(p.s2, p.s2), zc[rr], ov);
+        o[rr] = ov;
     }
 }
 
@@ -595,7 +599,10 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     float *__restrict__ oc = p.out + (long)col * p.ldo;
 
     // this thread's copies of a plane: in-plane source offset and ring-slot destination
-    int gofs[S::NU], sofs[S::NU];
+    // (shared-space byte address within slot 0; -1: no copy)
+    int gofs[S::NU];
+    int sofs[S::NU];
+    const unsigned sring = (unsigned)__cvta_generic_to_shared(ring);
 #pragma unroll
     for (int u = 0; u < S::NU; u++) {
         const int e = tid + u * S::NT;
@@ -612,49 +619,61 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
                 c = R + (e2 % S::HROW) * S::EW;
             }
             gofs[u] = wrapi(y0 - R + r, p.Ny) * p.Nx + wrapi(x0 - R + c, p.Nx);
-            sofs[u] = r * W + c;
+            sofs[u] = (int)sizeof(float) * (r * W + c);
         }
     }
-    // group of step k: plane k+R+D into the ring, and the potential / recurrence term of
-    // plane k+D; a group is committed (possibly empty) for every step
-    auto issue = [&](int k) {
-        if (k + D < ze) {
-            const int kp = k + R + D;
-            const float *pl = xc + wrapi(kp, p.Nz) * NxNy;
-            float *dst = ring + (kp % S::NR) * S::SLOT;
+    const unsigned svz = (unsigned)__cvta_generic_to_shared(vzs + 2 * ty * BX + 2 * tx);
+    const float *vsrc = p.v ? p.v + gx0 + row0 : nullptr;
+    const float *zsrc = zc ? zc + gx0 + row0 : nullptr;
+    const int drow = row1 - row0, dx = gx1 - gx0;
+    const int NzNxNy = p.Nz * NxNy;
+
+    // Copy groups, one committed per step (possibly empty): ring plane number kp (offset pw,
+    // slot rs) and, when vzon, the potential / recurrence term of plane offset vo (slot vs).
+    int pw = zs * NxNy, rs = zs % S::NR;  // next ring plane to copy: zs
+    int vo = zs * NxNy, vs = zs % S::NV;  // next potential plane to copy: zs
+    auto issue = [&](bool ringon, bool vzon) {
+        if (ringon) {
+            const float *pl = xc + pw;
+            const unsigned dst = sring + (unsigned)(rs * S::SLOT * (int)sizeof(float));
 #pragma unroll
             for (int u = 0; u < S::NU; u++) {
                 if (sofs[u] >= 0) {
-                    if constexpr (VEC) cp_async8(dst + sofs[u], pl + gofs[u]);
-                    else cp_async4(dst + sofs[u], pl + gofs[u]);
+                    if constexpr (VEC) cp_async8s(dst + sofs[u], pl + gofs[u]);
+                    else cp_async4s(dst + sofs[u], pl + gofs[u]);
                 }
             }
-            const int kv = k + D;
-            if (kv >= zs) {
-                const int pk = kv * NxNy;
-                float *vd = vzs + (kv % S::NV) * 2 * BX * BY + 2 * ty * BX + 2 * tx;
-                const float *srcs[2] = {p.v, zc};
+            pw += NxNy;
+            if (pw == NzNxNy) pw = 0;
+            rs = rs + 1 == S::NR ? 0 : rs + 1;
+        }
+        if (vzon) {
+            const unsigned d = svz + (unsigned)(vs * 2 * BX * BY * (int)sizeof(float));
+            const float *srcs[2] = {vsrc, zsrc};
 #pragma unroll
-                for (int a = 0; a < 2; a++) {
-                    if (!srcs[a]) continue;
-                    float *d = vd + a * BX * BY;
-                    if constexpr (VEC) {
-                        cp_async8(d, srcs[a] + pk + gx0 + row0);
-                        cp_async8(d + BX, srcs[a] + pk + gx0 + row1);
-                    } else {
-                        cp_async4(d, srcs[a] + pk + gx0 + row0);
-                        cp_async4(d + 1, srcs[a] + pk + gx1 + row0);
-                        cp_async4(d + BX, srcs[a] + pk + gx0 + row1);
-                        cp_async4(d + BX + 1, srcs[a] + pk + gx1 + row1);
-                    }
+            for (int a = 0; a < 2; a++) {
+                if (!srcs[a]) continue;
+                const float *g = srcs[a] + vo;
+                const unsigned da = d + (unsigned)(a * BX * BY * (int)sizeof(float));
+                if constexpr (VEC) {
+                    cp_async8s(da, g);
+                    cp_async8s(da + BX * sizeof(float), g + drow);
+                } else {
+                    cp_async4s(da, g);
+                    cp_async4s(da + sizeof(float), g + dx);
+                    cp_async4s(da + BX * sizeof(float), g + drow);
+                    cp_async4s(da + (BX + 1) * sizeof(float), g + drow + dx);
                 }
             }
+            vo += NxNy;
+            vs = vs + 1 == S::NV ? 0 : vs + 1;
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
 
     // prologue: the register queue holds planes zs-R .. zs+R-1; the ring receives planes
-    // zs .. zs+R+D-1 (the groups of steps zs-R-D .. zs-1)
+    // zs .. zs+R+D-1 and the potential planes zs .. zs+D-1 (the groups of steps
+    // zs-R-D .. zs-1: group j copies ring plane zs+j and potential plane zs+j-R)
     float2 qa[Q], qb[Q];
 #pragma unroll
     for (int m = 0; m < 2 * R; m++) {
@@ -662,7 +681,13 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
         qa[m] = ld_pair<VEC>(xc, pl + gx0 + row0, pl + gx1 + row0);
         qb[m] = ld_pair<VEC>(xc, pl + gx0 + row1, pl + gx1 + row1);
     }
-    for (int j = 0; j < R + D; j++) issue(zs - R - D + j);
+    for (int j = 0; j < R + D; j++) {
+        const int kstep = zs - R - D + j;  // the step this group belongs to
+        issue(kstep + D < ze, j >= R && kstep + D < ze);
+    }
+    int sk = zs % S::NR;      // ring slot of plane k
+    int svk = zs % S::NV;     // potential slot of plane k
+    int ko = zs * NxNy;       // offset of plane k
 
 #define SGPU_RING_STEP(U)                                                                        \
     {                                                                                            \
@@ -670,19 +695,20 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
         if (k < ze) {                                                                            \
             cp_async_wait_group<D - 1>();                                                        \
             __syncthreads();                                                                     \
-            issue(k);                                                                            \
-            const float *sl = ring + (k % S::NR) * S::SLOT;                                      \
-            const float *sq = ring + ((k + R) % S::NR) * S::SLOT + (2 * ty + R) * W + R + 2 * tx; \
+            issue(k + D < ze, k + D < ze);                                                       \
+            const float *sl = ring + sk * S::SLOT;                                               \
+            const int skr = sk + R >= S::NR ? sk + R - S::NR : sk + R;                           \
+            const float *sq = ring + skr * S::SLOT + (2 * ty + R) * W + R + 2 * tx;              \
             qa[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq);                       \
             qb[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq + W);                   \
-            const float *vz = vzs + (k % S::NV) * 2 * BX * BY + 2 * ty * BX + 2 * tx;            \
+            const float *vz = vzs + svk * 2 * BX * BY + 2 * ty * BX + 2 * tx;                    \
             float2 vcs[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};                      \
             float2 zcs[2] = {vcs[0], vcs[1]};                                                    \
-            if (p.v) {                                                                           \
+            if (vsrc) {                                                                          \
                 vcs[0] = *reinterpret_cast<const float2 *>(vz);                                  \
                 vcs[1] = *reinterpret_cast<const float2 *>(vz + BX);                             \
             }                                                                                    \
-            if (zc) {                                                                            \
+            if (zsrc) {                                                                          \
                 zcs[0] = *reinterpret_cast<const float2 *>(vz + BX * BY);                        \
                 zcs[1] = *reinterpret_cast<const float2 *>(vz + BX * BY + BX);                   \
             }                                                                                    \
@@ -691,8 +717,11 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
                 yv[t] = *reinterpret_cast<const float2 *>(sl + (2 * ty + t) * W + R + 2 * tx);   \
             float2 o[2];                                                                         \
             b22_block<R, Q, (U)>(p, sl + (2 * ty + R) * W + 2 * tx, W, yv, qa, qb, vcs, zcs,     \
-                                 p.v != nullptr, zc != nullptr, o);                              \
-            b22_store<VEC>(oc, k * NxNy, row0, row1, gx0, gx1, r0ok, r1ok, in0, in1, o);         \
+                                 vsrc != nullptr, zsrc != nullptr, o);                           \
+            b22_store<VEC>(oc, ko, row0, row1, gx0, gx1, r0ok, r1ok, in0, in1, o);               \
+            sk = sk + 1 == S::NR ? 0 : sk + 1;                                                   \
+            svk = svk + 1 == S::NV ? 0 : svk + 1;                                                \
+            ko += NxNy;                                                                          \
         }                                                                                        \
     }
 
