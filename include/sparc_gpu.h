@@ -418,8 +418,10 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
 /* Fix the form of the real nonlocal apply (0: one thread per covered point over all column
  * blocks; 1: alpha rows staged in shared memory per chunk of covered points; 2: as 0 with the
  * point's Chi values loaded once before the column loop; 3: FP32 only, a dense product per
- * chunk of covered points over the alpha rows of the chunk's atoms); sgpu_autotune times all
- * four. Forms 0-2 give identical results; form 3 sums in another order (FP32 rounding). */
+ * chunk of covered points over the alpha rows of the chunk's atoms; 4: FP32 only, per range of
+ * covered points with the output tile in shared memory); sgpu_autotune times all five.
+ * Forms 0-2 give identical results; forms 3 and 4 sum in other orders (FP32 rounding; form 4
+ * adds the contributions of overlapping spheres in no fixed order). */
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
 
 /* Fix the form of the FP32 nonlocal projection (0: one block per segment of one image's
@@ -432,8 +434,8 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
  * pointer may be NULL. */
 int sgpu_get_variants(sgpu_ctx *ctx, int *stencil, int *nl_apply, int *nl_project);
 
-/* Milliseconds per launch that the last sgpu_autotune measured for the four nonlocal apply
- * forms (apply_ms[4]) and the two FP32 projection forms (project_ms[2]); zeros before any
+/* Milliseconds per launch that the last sgpu_autotune measured for the five nonlocal apply
+ * forms (apply_ms[5]) and the two FP32 projection forms (project_ms[2]); zeros before any
  * tuning or without projectors. Either pointer may be NULL. */
 int sgpu_get_tuning(sgpu_ctx *ctx, double *apply_ms, double *project_ms);
 

@@ -475,8 +475,8 @@ class Context:
         return dict(stencil=s.value, nl_apply=a.value, nl_project=p.value)
 
     def tuning(self):
-        """Per-form milliseconds of the last autotune: dict(nl_apply=[4], nl_project=[2])."""
-        a, p = np.zeros(4), np.zeros(2)
+        """Per-form milliseconds of the last autotune: dict(nl_apply=[5], nl_project=[2])."""
+        a, p = np.zeros(5), np.zeros(2)
         _check(lib().sgpu_get_tuning(self._h, _ptr(a), _ptr(p)))
         return dict(nl_apply=a.tolist(), nl_project=p.tolist())
 

@@ -1,7 +1,8 @@
 // Autotuner for the FP32 filter kernels: times each tile / register-blocking variant of the
 // fused stencil + Chebyshev update, and each form of the nonlocal apply (per point over all
 // column blocks, alpha rows staged per chunk of covered points, per point with its Chi
-// values hoisted out of the column loop, or, in FP32, a dense product per chunk), and each
+// values hoisted out of the column loop, or, in FP32, a dense product per chunk or the range
+// form with the output tile in shared memory), and each
 // form of the FP32 projection (per image
 // segment, or per range of consecutive covered points), on scratch blocks of the
 // context's grid and projector set, and keeps the fastest of each. The stencil variants
@@ -73,7 +74,7 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
             const int saved_a = ctx->nl_apply_variant;
             float tbest = 1e30f;
             int abest = saved_a;
-            for (int v = 0; v < 4 && rc == SGPU_OK; v++) {
+            for (int v = 0; v < 5 && rc == SGPU_OK; v++) {
                 ctx->nl_apply_variant = v;
                 float t = 0.f, tmin = 1e30f;
                 for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
@@ -146,8 +147,8 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant)
 
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant)
 {
-    if (!ctx || variant < 0 || variant > 3) {
-        set_error("sgpu_set_nonlocal_apply_variant: variant must be 0 .. 3");
+    if (!ctx || variant < 0 || variant > 4) {
+        set_error("sgpu_set_nonlocal_apply_variant: variant must be 0 .. 4");
         return SGPU_ERR_ARG;
     }
     ctx->nl_apply_variant = variant;
@@ -170,7 +171,7 @@ int sgpu_get_tuning(sgpu_ctx *ctx, double *apply_ms, double *project_ms)
         set_error("sgpu_get_tuning: null context");
         return SGPU_ERR_ARG;
     }
-    for (int v = 0; v < 4 && apply_ms; v++) apply_ms[v] = ctx->tune_apply_ms[v];
+    for (int v = 0; v < 5 && apply_ms; v++) apply_ms[v] = ctx->tune_apply_ms[v];
     for (int v = 0; v < 2 && project_ms; v++) project_ms[v] = ctx->tune_project_ms[v];
     return SGPU_OK;
 }

@@ -205,9 +205,9 @@ __global__ void __launch_bounds__(256)
         for (int it = warp; it < ni; it += 8) {
             const int2 row = item_row[ib + it];  // (first projector row, projector count)
             const int e0 = item_e0[ib + it] - eb, e1 = item_e0[ib + it + 1] - eb;
-            float acc0[MAXJ], acc1[MAXJ];
+            float2 acc[MAXJ];  // (column 2l, column 2l+1) per projector, packed FMAs
 #pragma unroll
-            for (int j = 0; j < MAXJ; j++) acc0[j] = acc1[j] = 0.f;
+            for (int j = 0; j < MAXJ; j++) acc[j] = make_float2(0.f, 0.f);
             for (int e = e0; e < e1; e++) {
                 const float2 xv = *reinterpret_cast<const float2 *>(xs + lps[e] * XLD + 2 * lane);
                 const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
@@ -216,12 +216,9 @@ __global__ void __launch_bounds__(256)
                     const float4 c4 = cv[q];
                     const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-                    for (int w = 0; w < 4; w++) {
-                        if (q * 4 + w < MAXJ) {
-                            acc0[q * 4 + w] += ce[w] * xv.x;
-                            acc1[q * 4 + w] += ce[w] * xv.y;
-                        }
-                    }
+                    for (int w = 0; w < 4; w++)
+                        if (q * 4 + w < MAXJ)
+                            acc[q * 4 + w] = __ffma2_rn(make_float2(ce[w], ce[w]), xv, acc[q * 4 + w]);
                 }
             }
             const int c0 = n0 + 2 * lane;
@@ -232,10 +229,109 @@ __global__ void __launch_bounds__(256)
                     float *dst = alpha + (long)(row.x + j) * lda + c0;
                     if (c0 + 1 < ncol)  // lda and c0 are even: an 8-byte aligned pair
                         atomicAdd(reinterpret_cast<float2 *>(dst),
-                                  make_float2(s * acc0[j], s * acc1[j]));
+                                  make_float2(s * acc[j].x, s * acc[j].y));
                     else if (c0 < ncol)
-                        atomicAdd(dst, s * acc0[j]);
+                        atomicAdd(dst, s * acc[j].x);
                 }
+            }
+        }
+    }
+}
+
+// Range apply (FP32): the projection's ranges and work items run in reverse. Block = one range;
+// for each group of 64 columns (rotated by the range index) it gathers the output tile of its
+// points (os[point][64], one coalesced read of every covered output element), then each warp
+// takes work items in turn: lane l holds scale * alpha[row j, columns l and l+32] of the item's
+// atom in registers and, for every entry of the item, adds sum_j Chi_j alpha_j into the tile
+// with shared-memory atomics (lanes touch distinct columns; two images over one point meet
+// only in the atomics, so the order of those additions is not fixed). The tile is then written
+// back once. Every covered output element is read and written once per launch, in grid order.
+template <int MAXJ>
+__global__ void __launch_bounds__(256)
+    k_nl_apply_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
+                     const int *__restrict__ rng_item0, const int *__restrict__ item_e0,
+                     const int2 *__restrict__ item_row, const int *__restrict__ pe_lp,
+                     const float *__restrict__ pe_chi, const int *__restrict__ cov_pt, int ncol,
+                     const float *__restrict__ alpha, long lda, float scale,
+                     float *__restrict__ out, long ldo)
+{
+    constexpr int NC = 64, OLD = NC + 1;             // columns per group, padded tile row
+    constexpr int MAXJP = (MAXJ + 3) / 4 * 4;
+    constexpr int GB = 32;                           // gathers in flight per thread
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *cs = reinterpret_cast<float *>(smem_raw);  // [entries][MAXJP]
+    const int r = blockIdx.x;
+    const int p0 = rng_pt0[r], npt = rng_pt0[r + 1] - p0;
+    const int eb = rng_ent0[r], ne = rng_ent0[r + 1] - eb;
+    const int ib = rng_item0[r], ni = rng_item0[r + 1] - ib;
+    float *os = cs + (size_t)ne * MAXJP;                          // [kRangePts][OLD]
+    int *lps = reinterpret_cast<int *>(os + kRangePts * OLD);     // [entries]
+    int *gps = lps + ne;                                          // [kRangePts]
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+    for (int i = t; i < npt; i += 256) gps[i] = cov_pt[p0 + i];
+    for (int i = t; i < ne; i += 256) lps[i] = pe_lp[eb + i];
+    {
+        const float4 *src = reinterpret_cast<const float4 *>(pe_chi + (long)eb * MAXJP);
+        float4 *dst = reinterpret_cast<float4 *>(cs);
+        for (int i = t; i < ne * (MAXJP / 4); i += 256) dst[i] = __ldg(src + i);
+    }
+    const int ngroup = (ncol + NC - 1) / NC;
+    for (int gi = 0; gi < ngroup; gi++) {
+        const int n0 = ((gi + r) % ngroup) * NC;
+        __syncthreads();  // staging done / previous tile written back
+        for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
+            float v[GB];
+#pragma unroll
+            for (int u = 0; u < GB; u++) {
+                const int idx = base + t + u * 256;
+                const int lp = idx % kRangePts, c = idx / kRangePts;
+                v[u] = (lp < npt && n0 + c < ncol) ? out[(long)(n0 + c) * ldo + gps[lp]] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < GB; u++) {
+                const int idx = base + t + u * 256;
+                os[(idx % kRangePts) * OLD + idx / kRangePts] = v[u];
+            }
+        }
+        __syncthreads();
+        const int ca = n0 + lane, cb = n0 + lane + 32;
+        for (int it = warp; it < ni; it += 8) {
+            const int2 row = item_row[ib + it];  // (first projector row, projector count)
+            const int e0 = item_e0[ib + it] - eb, e1 = item_e0[ib + it + 1] - eb;
+            float2 a[MAXJ];  // scale * alpha of columns (lane, lane + 32)
+#pragma unroll
+            for (int j = 0; j < MAXJ; j++) {
+                a[j] = make_float2(0.f, 0.f);
+                if (j < row.y) {
+                    const float *ar = alpha + (long)(row.x + j) * lda;
+                    a[j] = make_float2(ca < ncol ? scale * __ldg(ar + ca) : 0.f,
+                                       cb < ncol ? scale * __ldg(ar + cb) : 0.f);
+                }
+            }
+            for (int e = e0; e < e1; e++) {
+                const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
+                float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < MAXJP / 4; q++) {
+                    const float4 c4 = cv[q];
+                    const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                    for (int w = 0; w < 4; w++)
+                        if (q * 4 + w < MAXJ) s = __ffma2_rn(make_float2(ce[w], ce[w]), a[q * 4 + w], s);
+                }
+                float *o = os + lps[e] * OLD;
+                atomicAdd(o + lane, s.x);
+                atomicAdd(o + lane + 32, s.y);
+            }
+        }
+        __syncthreads();
+        for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
+#pragma unroll
+            for (int u = 0; u < GB; u++) {
+                const int idx = base + t + u * 256;
+                const int lp = idx % kRangePts, c = idx / kRangePts;
+                if (lp < npt && n0 + c < ncol) out[(long)(n0 + c) * ldo + gps[lp]] = os[lp * OLD + c];
             }
         }
     }
@@ -423,21 +519,20 @@ __global__ void __launch_bounds__(256, 2)
         }
     }
     __syncthreads();
-    float acc[HC];
+    float2 acc[HC / 2];  // column pairs, packed FMAs
 #pragma unroll
-    for (int q = 0; q < HC; q++) acc[q] = 0.f;
+    for (int q = 0; q < HC / 2; q++) acc[q] = make_float2(0.f, 0.f);
     const float4 *Ah = reinterpret_cast<const float4 *>(As + half * HC);
 #pragma unroll 2
     for (int k = 0; k < nr; k++) {
         const float cv = Cs[(size_t)k * kApplyChunk + pt];
+        const float2 cv2 = make_float2(cv, cv);
         const float4 *a4 = Ah + (size_t)k * (NC / 4);
 #pragma unroll
         for (int q = 0; q < HC / 4; q++) {
             const float4 a = a4[q];
-            acc[4 * q] += cv * a.x;
-            acc[4 * q + 1] += cv * a.y;
-            acc[4 * q + 2] += cv * a.z;
-            acc[4 * q + 3] += cv * a.w;
+            acc[2 * q] = __ffma2_rn(cv2, make_float2(a.x, a.y), acc[2 * q]);
+            acc[2 * q + 1] = __ffma2_rn(cv2, make_float2(a.z, a.w), acc[2 * q + 1]);
         }
     }
     if (!live) return;
@@ -445,19 +540,21 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
     for (int q = 0; q < HC; q++) ov[q] = cb + q < ncol ? out[(long)(cb + q) * ldo + p] : 0.f;
 #pragma unroll
-    for (int q = 0; q < HC; q++)
-        if (cb + q < ncol) out[(long)(cb + q) * ldo + p] = ov[q] + scale * acc[q];
+    for (int q = 0; q < HC; q++) {
+        const float a = q % 2 ? acc[q / 2].y : acc[q / 2].x;
+        if (cb + q < ncol) out[(long)(cb + q) * ldo + p] = ov[q] + scale * a;
+    }
 }
 
 // Apply, staged: one block per (chunk of kApplyChunk consecutive covered points, block of CB
 // columns). The alpha rows of every atom that touches the chunk are staged once in shared
 // memory (rows listed in chunk_rows, each padded by 16 bytes so that rows start four banks
 // apart: up to eight distinct rows per 16-byte warp read are served in one pass), and each
-// thread accumulates its point's CB outputs from there with 16-byte reads; the output block
-// is read-modified-written once. Neighbouring covered points share atoms, so one staged row
+// thread accumulates its point's CB outputs from there with 16-byte reads; then the output
+// block is read-modified-written once. Neighbouring covered points share atoms, so one staged row
 // serves many threads.
 template <typename T, int CB, int NPMAX>
-__global__ void __launch_bounds__(kApplyChunk)
+__global__ void __launch_bounds__(kApplyChunk, 4)
     k_nl_apply_staged(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
                       const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
                       const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
@@ -475,11 +572,6 @@ __global__ void __launch_bounds__(kApplyChunk)
     const int cidx = c * kApplyChunk + threadIdx.x;
     const bool live = cidx < ncov;
     const long p = live ? cov_pt[cidx] : 0;
-    // the thread's outputs are read first so their latency overlaps the staging
-    T ov[CB];
-#pragma unroll
-    for (int q = 0; q < CB; q++)
-        ov[q] = (live && n0 + q < ncol) ? out[(long)(n0 + q) * ldo + p] : T(0);
     const int r0 = chunk_row_ptr[c], nr = chunk_row_ptr[c + 1] - r0;
     for (int e = threadIdx.x; e < nr * CB; e += blockDim.x) {
         const int r = e / CB, cc = e % CB;
@@ -508,11 +600,24 @@ __global__ void __launch_bounds__(kApplyChunk)
             for (int q = 0; q < CB / VW; q++) {
                 const V a = sv[q];
                 const T *ae = reinterpret_cast<const T *>(&a);
+                if constexpr (sizeof(T) == 4) {  // packed pairs: same rounding per lane
 #pragma unroll
-                for (int w = 0; w < VW; w++) acc[q * VW + w] += cv * ae[w];
+                    for (int w = 0; w < VW; w += 2) {
+                        const float2 r = __ffma2_rn(make_float2(cv, cv), make_float2(ae[w], ae[w + 1]),
+                                                    make_float2(acc[q * VW + w], acc[q * VW + w + 1]));
+                        acc[q * VW + w] = r.x;
+                        acc[q * VW + w + 1] = r.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int w = 0; w < VW; w++) acc[q * VW + w] += cv * ae[w];
+                }
             }
         }
     }
+    T ov[CB];  // the output block: all loads in flight together
+#pragma unroll
+    for (int q = 0; q < CB; q++) ov[q] = n0 + q < ncol ? out[(long)(n0 + q) * ldo + p] : T(0);
 #pragma unroll
     for (int q = 0; q < CB; q++)
         if (n0 + q < ncol) out[(long)(n0 + q) * ldo + p] = ov[q] + scale * acc[q];
@@ -646,6 +751,30 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
         return SGPU_OK;
     }
     if constexpr (sizeof(T) == 4) {
+        if (ctx->nl_apply_variant == 4 && nl.nrange > 0) {
+            const size_t rsm = sizeof(float) * ((size_t)nl.max_range_ent * nl.range_jp +
+                                                (size_t)kRangePts * 65) +
+                               sizeof(int) * ((size_t)nl.max_range_ent + kRangePts);
+            ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+#define SGPU_RAPPLY(MJ)                                                                      \
+    {                                                                                        \
+        auto kern = k_nl_apply_range<MJ>;                                                    \
+        SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                           (int)rsm));                                       \
+        kern<<<nl.nrange, 256, rsm, st>>>(nl.rng_pt0, nl.rng_ent0, nl.rng_item0, nl.item_e0, \
+                                          nl.item_row, nl.pe_lp, nl.pe_chi32, nl.cov_pt,     \
+                                          ncol, alpha, lda, (float)scale, out, ldo);         \
+    }
+            if (nl.range_jp == 12)
+                SGPU_RAPPLY(9)
+            else if (nl.range_jp == 20)
+                SGPU_RAPPLY(18)
+            else
+                SGPU_RAPPLY(32)
+#undef SGPU_RAPPLY
+            SGPU_CUDA_TRY(cudaGetLastError());
+            return SGPU_OK;
+        }
         const size_t dsm = sizeof(float) * (size_t)nl.max_chunk_rows * (64 + kApplyChunk);
         if (ctx->nl_apply_variant == 3 && nl.nchunk > 0 && dsm <= kApplyDenseMax) {
             SGPU_CUDA_TRY(cudaFuncSetAttribute(k_nl_apply_dense,

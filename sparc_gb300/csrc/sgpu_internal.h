@@ -151,9 +151,10 @@ struct sgpu_ctx {
     int stencil_variant = 0;   // FP32 stencil kernel variant (autotune.cu)
     bool stencil_tuned = false;
     int nl_apply_variant = 0;  // real nonlocal apply: 0 per point over all columns, 1 staged,
-                               // 2 per point with the Chi values hoisted, 3 dense per chunk
+                               // 2 per point with the Chi values hoisted, 3 dense per chunk,
+                               // 4 per range with the output tile in shared memory
     int nl_project_variant = 0;  // FP32 projection: 0 per image segment, 1 per point range
-    double tune_apply_ms[4] = {0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last autotune timings
+    double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on

@@ -313,6 +313,10 @@ __device__ __forceinline__ void cp_async8s(unsigned sa, const void *gmem)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16s(unsigned sa, const void *gmem)  // L2 only
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group()
@@ -555,27 +559,32 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
 // from global memory, so no step waits on a global load issued in the same step. One barrier
 // per plane: after it the slot of plane k-1 is free and receives plane k+R+D. Same arithmetic
 // (b22_block) as k_stencil_f32_b22, so the results are identical.
-template <int R, int BX, int BY, int D, bool VEC>
+// EW = floats per copy: 4 (16-byte copies that bypass L1; needs Nx % 4 == 0 and 16-byte
+// aligned columns, and the x-halo is widened to 8 points so every copy is aligned), 2 (8-byte)
+// or 1. XO = shared-memory column of the tile's first point.
+template <int R, int BX, int BY, int D, int EW_>
 struct RingShape {
-    static constexpr int W = BX + 2 * R, H = BY + 2 * R;
+    static constexpr int EW = EW_;
+    static constexpr int XO = EW == 4 ? (R + 3) / 4 * 4 : R;
+    static constexpr int W = BX + 2 * XO, H = BY + 2 * R;
     static constexpr int SLOT = H * W;     // one plane with its halo (the corners stay unused)
     static constexpr int NR = R + D + 1;   // ring slots: planes k .. k+R+D
     static constexpr int NV = D + 1;       // potential / recurrence-term slots: planes k .. k+D
     static constexpr int NT = BX / 2 * (BY / 2);
-    static constexpr int EW = VEC ? 2 : 1;  // floats per copy
     static constexpr int CROW = W / EW, HROW = BX / EW;
     static constexpr int NCOPY = BY * CROW + 2 * R * HROW;  // copies per plane
     static constexpr int NU = (NCOPY + NT - 1) / NT;        // copies per thread and plane
     static constexpr size_t smem_bytes = sizeof(float) * ((size_t)NR * SLOT + (size_t)NV * 2 * BX * BY);
 };
 
-template <int R, int BX, int BY, int MINB, bool VEC, int D>
+template <int R, int BX, int BY, int MINB, int EW, int D>
 __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     k_stencil_f32_ring(const StencilParams<float> p)
 {
-    using S = RingShape<R, BX, BY, D, VEC>;
+    using S = RingShape<R, BX, BY, D, EW>;
+    constexpr bool VEC = EW >= 2;
     constexpr int Q = 2 * R + 1;
-    constexpr int W = S::W;
+    constexpr int W = S::W, XO = S::XO;
     static_assert(Q == 13 && R % 2 == 0 && D >= 1, "the unrolled z-loop is written for radius 6");
     extern __shared__ __align__(16) float ring[];
     float *const vzs = ring + S::NR * S::SLOT;  // [NV][2][BY][BX]: potential, recurrence term
@@ -612,13 +621,13 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             int r, c;
             if (e < BY * S::CROW) {
                 r = R + e / S::CROW;
-                c = (e % S::CROW) * S::EW;
+                c = (e % S::CROW) * EW;
             } else {
                 const int e2 = e - BY * S::CROW, hr = e2 / S::HROW;
                 r = hr < R ? hr : hr + BY;
-                c = R + (e2 % S::HROW) * S::EW;
+                c = XO + (e2 % S::HROW) * EW;
             }
-            gofs[u] = wrapi(y0 - R + r, p.Ny) * p.Nx + wrapi(x0 - R + c, p.Nx);
+            gofs[u] = wrapi(y0 - R + r, p.Ny) * p.Nx + wrapi(x0 - XO + c, p.Nx);
             sofs[u] = (int)sizeof(float) * (r * W + c);
         }
     }
@@ -639,7 +648,8 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
 #pragma unroll
             for (int u = 0; u < S::NU; u++) {
                 if (sofs[u] >= 0) {
-                    if constexpr (VEC) cp_async8s(dst + sofs[u], pl + gofs[u]);
+                    if constexpr (EW == 4) cp_async16s(dst + sofs[u], pl + gofs[u]);
+                    else if constexpr (EW == 2) cp_async8s(dst + sofs[u], pl + gofs[u]);
                     else cp_async4s(dst + sofs[u], pl + gofs[u]);
                 }
             }
@@ -698,7 +708,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             issue(k + D < ze, k + D < ze);                                                       \
             const float *sl = ring + sk * S::SLOT;                                               \
             const int skr = sk + R >= S::NR ? sk + R - S::NR : sk + R;                           \
-            const float *sq = ring + skr * S::SLOT + (2 * ty + R) * W + R + 2 * tx;              \
+            const float *sq = ring + skr * S::SLOT + (2 * ty + R) * W + XO + 2 * tx;             \
             qa[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq);                       \
             qb[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq + W);                   \
             const float *vz = vzs + svk * 2 * BX * BY + 2 * ty * BX + 2 * tx;                    \
@@ -714,10 +724,10 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             }                                                                                    \
             float2 yv[2 * R + 2];                                                                \
             _Pragma("unroll") for (int t = 0; t < 2 * R + 2; t++)                                \
-                yv[t] = *reinterpret_cast<const float2 *>(sl + (2 * ty + t) * W + R + 2 * tx);   \
+                yv[t] = *reinterpret_cast<const float2 *>(sl + (2 * ty + t) * W + XO + 2 * tx);  \
             float2 o[2];                                                                         \
-            b22_block<R, Q, (U)>(p, sl + (2 * ty + R) * W + 2 * tx, W, yv, qa, qb, vcs, zcs,     \
-                                 vsrc != nullptr, zsrc != nullptr, o);                           \
+            b22_block<R, Q, (U)>(p, sl + (2 * ty + R) * W + XO - R + 2 * tx, W, yv, qa, qb,     \
+                                 vcs, zcs, vsrc != nullptr, zsrc != nullptr, o);                 \
             b22_store<VEC>(oc, ko, row0, row1, gx0, gx1, r0ok, r1ok, in0, in1, o);               \
             sk = sk + 1 == S::NR ? 0 : sk + 1;                                                   \
             svk = svk + 1 == S::NV ? 0 : svk + 1;                                                \
@@ -735,11 +745,11 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     cp_async_wait_all();
 }
 
-template <int R, int BX, int BY, int MINB, bool VEC, int D>
+template <int R, int BX, int BY, int MINB, int EW, int D>
 int launch_ring(const StencilParams<float> &q, dim3 grid, cudaStream_t st)
 {
-    constexpr size_t smem = RingShape<R, BX, BY, D, VEC>::smem_bytes;
-    auto kern = k_stencil_f32_ring<R, BX, BY, MINB, VEC, D>;
+    constexpr size_t smem = RingShape<R, BX, BY, D, EW>::smem_bytes;
+    auto kern = k_stencil_f32_ring<R, BX, BY, MINB, EW, D>;
     SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
     kern<<<grid, dim3(BX / 2, BY / 2), smem, st>>>(q);
@@ -804,6 +814,10 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     auto al8 = [](const void *ptr) { return ((uintptr_t)ptr & 7u) == 0; };
     const bool vec = (ctx->Nx % 2 == 0) && al8(x) && al8(out) && ldx % 2 == 0 && ldo % 2 == 0 &&
                      (!p.z || (al8(z) && ldz % 2 == 0)) && (!p.v || al8(v));
+    // the plane ring copies x in 16-byte pieces when every row of every column is 16-byte
+    // aligned (the potential and recurrence term still move in 8-byte pieces)
+    auto al16 = [](const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; };
+    const bool quad = vec && ctx->Nx % 4 == 0 && al16(x) && ldx % 4 == 0;
     const int maxz = 65535 / nslab;
     for (int c0i = 0; c0i < ncol; c0i += maxz) {
         int nc = ncol - c0i < maxz ? ncol - c0i : maxz;
@@ -837,16 +851,20 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                     k_stencil_f32_b22<R, 32, 16, 3, false><<<grid, dim3(16, 8), 0, st>>>(q);
                 break;
             case 5:  // 2x2 32x16 from the plane ring, planes one step ahead
-                if (vec)
-                    SGPU_TRY((launch_ring<R, 32, 16, 4, true, 1>(q, grid, st)));
+                if (quad)
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 4, 1>(q, grid, st)));
+                else if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 2, 1>(q, grid, st)));
                 else
-                    SGPU_TRY((launch_ring<R, 32, 16, 4, false, 1>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 1, 1>(q, grid, st)));
                 break;
             case 6:  // 2x2 32x16 from the plane ring, planes two steps ahead
-                if (vec)
-                    SGPU_TRY((launch_ring<R, 32, 16, 3, true, 2>(q, grid, st)));
+                if (quad)
+                    SGPU_TRY((launch_ring<R, 32, 16, 3, 4, 2>(q, grid, st)));
+                else if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 16, 3, 2, 2>(q, grid, st)));
                 else
-                    SGPU_TRY((launch_ring<R, 32, 16, 3, false, 2>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 3, 1, 2>(q, grid, st)));
                 break;
             default:
                 k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);

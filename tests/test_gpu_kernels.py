@@ -161,11 +161,12 @@ def test_nonlocal_apply_forms_identical(gpu_available, dtype):
             outs.append(Y)
     np.testing.assert_array_equal(outs[0], outs[1])
     np.testing.assert_array_equal(outs[0], outs[2])
-    if dtype == np.float32:  # the dense per-chunk form sums in another order
-        ctx.set_nonlocal_apply_variant(3)
-        X = x.copy(); Y = np.zeros_like(x)
-        ctx.ChebyshevFiltering_f32(X, Y, 3, 0.5, 50.0, -1.0)
-        assert rel_err(Y.astype(np.float64), outs[0].astype(np.float64)) < 1e-5
+    if dtype == np.float32:  # the dense and range forms sum in other orders
+        for v in (3, 4):
+            ctx.set_nonlocal_apply_variant(v)
+            X = x.copy(); Y = np.zeros_like(x)
+            ctx.ChebyshevFiltering_f32(X, Y, 3, 0.5, 50.0, -1.0)
+            assert rel_err(Y.astype(np.float64), outs[0].astype(np.float64)) < 1e-5, v
 
 
 @pytest.mark.parametrize("natom,rc,lmax", [(7, 1.6, 2), (40, 3.0, 2), (12, 2.0, 3)])
