@@ -5,18 +5,16 @@
 //   alpha_J[j, n] *= Gamma_J[j]                   (:843-866)
 //   Hx[grid_pos_J] += Chi_J alpha_J               (dgemm + scatter, :869-884)
 //
-// GPU form:
-//   * project: a gathered GEMM. One thread block per segment of at most kSegPts points of
-//     one atom image: the segment's grid positions and Chi rows are staged in shared memory
-//     once, then the block walks all column groups, gathering x[grid_pos, group] into shared
-//     memory chunk by chunk and accumulating alpha[j, n] in registers; one atomic add per
-//     (projector, column) and segment, with dV * Gamma folded in.
-//   * apply: owner-computes over a CSR of covered grid points, so each output element is
-//     written by exactly one thread (no atomics on the orbital block; overlapping spheres are
-//     summed in registers). The staged form gives each block a chunk of consecutive covered
-//     points and a block of columns, with the alpha rows of the chunk's atoms staged in shared
-//     memory; the unstaged form (one thread per point over all column blocks, alpha from L1)
-//     serves chunks whose atoms' rows would not fit.
+// GPU forms (the autotuner picks per context; see each kernel):
+//   * project: a gathered GEMM with one atomic add per (projector, column) and block, dV *
+//     Gamma folded in. Segment form: one block per segment of at most kSegPts points of one
+//     atom image. Range form (FP32): one block per range of consecutive covered points, all
+//     images over it, so each covered x element is read once and in grid order.
+//   * apply: owner-computes over a CSR of covered grid points (per point over column blocks;
+//     with alpha rows staged per chunk; with the Chi values hoisted; a dense product per
+//     chunk), each output element written by one thread, or the range form (FP32), which
+//     gathers a range's output tile into shared memory, adds every image's contribution there
+//     and writes the tile back once.
 #include <algorithm>
 #include <numeric>
 
