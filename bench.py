@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution blocks")
     ap.add_argument("--no-c4", action="store_true", help="skip the 216-atom SCF block")
     ap.add_argument("--no-c3", action="store_true", help="skip the batched k-point/spin block")
+    ap.add_argument("--c3-only", action="store_true",
+                    help="print only the batched k-point/spin block (profiling)")
     ap.add_argument("--stencil-variant", type=int, default=None,
                     help="use this FP32 stencil variant instead of the tuned one (profiling)")
     ap.add_argument("--nl-apply", type=int, default=None,
@@ -412,6 +414,10 @@ def main():
         dist.init_process_group(backend="nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.c3_only:
+        print(json.dumps({"batched_c3": batched_c3_block(sg, torch, dev, device=local,
+                                                         steps=args.steps)}), flush=True)
+        return
 
     wl = microbench_workload(N=N3, ncol=args.ncol, with_vectors=False)
     g = wl["grid"]

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256)
 {
     constexpr int NC = 64, XLD = NC + 2;             // columns per group, padded x row
     constexpr int MAXJP = (MAXJ + 3) / 4 * 4;        // staged Chi values per entry
-    constexpr int GB = 32;                           // gathers in flight per thread
+    constexpr int GB = 16;                           // gathers in flight per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *xs = reinterpret_cast<float *>(smem_raw);  // [kRangePts][XLD]
     float *cs = xs + kRangePts * XLD;                 // [entries][MAXJP]
