@@ -444,7 +444,7 @@ def main():
                    "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
                    "k_stencil_f32_b22<32x16, 3 blocks/SM>",
                    "k_stencil_f32_ring<32x16, 1 plane ahead>",
-                   "k_stencil_f32_ring<32x16, 2 planes ahead>"][variant]
+                   "k_stencil_f32_ring<32x16, 2 planes ahead, potential from L2>"][variant]
 
     gen = torch.Generator(device=dev)
     gen.manual_seed(1234 + rank)

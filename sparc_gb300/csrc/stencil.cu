@@ -562,8 +562,9 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
 // EW = floats per copy: 4 (16-byte copies that bypass L1; needs Nx % 4 == 0 and 16-byte
 // aligned columns, and the x-halo is widened to 8 points so every copy is aligned), 2 (8-byte)
 // or 1. XO = shared-memory column of the tile's first point.
-template <int R, int BX, int BY, int D, int EW_>
+template <int R, int BX, int BY, int D, int EW_, bool VG = false>
 struct RingShape {
+    static constexpr int NA = VG ? 1 : 2;  // staged arrays per potential slot (VG: z only)
     static constexpr int EW = EW_;
     static constexpr int XO = EW == 4 ? (R + 3) / 4 * 4 : R;
     static constexpr int W = BX + 2 * XO, H = BY + 2 * R;
@@ -574,14 +575,14 @@ struct RingShape {
     static constexpr int CROW = W / EW, HROW = BX / EW;
     static constexpr int NCOPY = BY * CROW + 2 * R * HROW;  // copies per plane
     static constexpr int NU = (NCOPY + NT - 1) / NT;        // copies per thread and plane
-    static constexpr size_t smem_bytes = sizeof(float) * ((size_t)NR * SLOT + (size_t)NV * 2 * BX * BY);
+    static constexpr size_t smem_bytes = sizeof(float) * ((size_t)NR * SLOT + (size_t)NV * NA * BX * BY);
 };
 
-template <int R, int BX, int BY, int MINB, int EW, int D>
+template <int R, int BX, int BY, int MINB, int EW, int D, bool VG>
 __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     k_stencil_f32_ring(const StencilParams<float> p)
 {
-    using S = RingShape<R, BX, BY, D, EW>;
+    using S = RingShape<R, BX, BY, D, EW, VG>;
     constexpr bool VEC = EW >= 2;
     constexpr int Q = 2 * R + 1;
     constexpr int W = S::W, XO = S::XO;
@@ -658,13 +659,14 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             rs = rs + 1 == S::NR ? 0 : rs + 1;
         }
         if (vzon) {
-            const unsigned d = svz + (unsigned)(vs * 2 * BX * BY * (int)sizeof(float));
-            const float *srcs[2] = {vsrc, zsrc};
+            const unsigned d = svz + (unsigned)(vs * S::NA * BX * BY * (int)sizeof(float));
+            const float *srcs[2] = {VG ? nullptr : vsrc, zsrc};
 #pragma unroll
             for (int a = 0; a < 2; a++) {
                 if (!srcs[a]) continue;
                 const float *g = srcs[a] + vo;
-                const unsigned da = d + (unsigned)(a * BX * BY * (int)sizeof(float));
+                const int ai = VG ? 0 : a;  // array index within the slot
+                const unsigned da = d + (unsigned)(ai * BX * BY * (int)sizeof(float));
                 if constexpr (VEC) {
                     cp_async8s(da, g);
                     cp_async8s(da + BX * sizeof(float), g + drow);
@@ -711,16 +713,22 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             const float *sq = ring + skr * S::SLOT + (2 * ty + R) * W + XO + 2 * tx;             \
             qa[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq);                       \
             qb[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq + W);                   \
-            const float *vz = vzs + svk * 2 * BX * BY + 2 * ty * BX + 2 * tx;                    \
+            const float *vz = vzs + svk * S::NA * BX * BY + 2 * ty * BX + 2 * tx;                \
             float2 vcs[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};                      \
             float2 zcs[2] = {vcs[0], vcs[1]};                                                    \
             if (vsrc) {                                                                          \
-                vcs[0] = *reinterpret_cast<const float2 *>(vz);                                  \
-                vcs[1] = *reinterpret_cast<const float2 *>(vz + BX);                             \
+                if constexpr (VG) { /* shared by all columns: from L2 */                         \
+                    vcs[0] = ld_pair<VEC>(vsrc, ko, ko + dx);                                    \
+                    vcs[1] = ld_pair<VEC>(vsrc, ko + drow, ko + drow + dx);                      \
+                } else {                                                                         \
+                    vcs[0] = *reinterpret_cast<const float2 *>(vz);                              \
+                    vcs[1] = *reinterpret_cast<const float2 *>(vz + BX);                         \
+                }                                                                                \
             }                                                                                    \
             if (zsrc) {                                                                          \
-                zcs[0] = *reinterpret_cast<const float2 *>(vz + BX * BY);                        \
-                zcs[1] = *reinterpret_cast<const float2 *>(vz + BX * BY + BX);                   \
+                const float *zz = vz + (VG ? 0 : BX * BY);                                       \
+                zcs[0] = *reinterpret_cast<const float2 *>(zz);                                  \
+                zcs[1] = *reinterpret_cast<const float2 *>(zz + BX);                             \
             }                                                                                    \
             float2 yv[2 * R + 2];                                                                \
             _Pragma("unroll") for (int t = 0; t < 2 * R + 2; t++)                                \
@@ -745,11 +753,11 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     cp_async_wait_all();
 }
 
-template <int R, int BX, int BY, int MINB, int EW, int D>
+template <int R, int BX, int BY, int MINB, int EW, int D, bool VG>
 int launch_ring(const StencilParams<float> &q, dim3 grid, cudaStream_t st)
 {
-    constexpr size_t smem = RingShape<R, BX, BY, D, EW>::smem_bytes;
-    auto kern = k_stencil_f32_ring<R, BX, BY, MINB, EW, D>;
+    constexpr size_t smem = RingShape<R, BX, BY, D, EW, VG>::smem_bytes;
+    auto kern = k_stencil_f32_ring<R, BX, BY, MINB, EW, D, VG>;
     SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
     kern<<<grid, dim3(BX / 2, BY / 2), smem, st>>>(q);
@@ -796,7 +804,7 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     const bool f32 = sizeof(T) == 4;
     // FP32 variants (autotune.cu): 0 paired 32x16, 1 2x2-blocked 32x16, 2 2x2-blocked 64x8,
     // 3 paired 64x8, 4 2x2-blocked 32x16 with 3 blocks per SM, 5 and 6 2x2-blocked 32x16 fed
-    // from the shared-memory plane ring one and two planes ahead
+    // from the shared-memory plane ring one and two planes ahead (6: potential from L2)
     const int variant = f32 ? ctx->stencil_variant : 0;
     const bool wide = variant == 2 || variant == 3;
     const int tbx = f32 ? (wide ? 64 : BXP) : BX;
@@ -852,19 +860,20 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                 break;
             case 5:  // 2x2 32x16 from the plane ring, planes one step ahead
                 if (quad)
-                    SGPU_TRY((launch_ring<R, 32, 16, 4, 4, 1>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 4, 1, false>(q, grid, st)));
                 else if (vec)
-                    SGPU_TRY((launch_ring<R, 32, 16, 4, 2, 1>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 2, 1, false>(q, grid, st)));
                 else
-                    SGPU_TRY((launch_ring<R, 32, 16, 4, 1, 1>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 1, 1, false>(q, grid, st)));
                 break;
-            case 6:  // 2x2 32x16 from the plane ring, planes two steps ahead
+            case 6:  // 2x2 32x16 from the plane ring, planes two steps ahead; the potential
+                     // (one vector for all columns) read from L2 so 4 blocks fit per SM
                 if (quad)
-                    SGPU_TRY((launch_ring<R, 32, 16, 3, 4, 2>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 4, 2, true>(q, grid, st)));
                 else if (vec)
-                    SGPU_TRY((launch_ring<R, 32, 16, 3, 2, 2>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 2, 2, true>(q, grid, st)));
                 else
-                    SGPU_TRY((launch_ring<R, 32, 16, 3, 1, 2>(q, grid, st)));
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 1, 2, true>(q, grid, st)));
                 break;
             default:
                 k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);
