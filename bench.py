@@ -513,7 +513,10 @@ def main():
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
-        traffic = tj.get("fp32_bytes_per_launch_at_bench")
+        for ent in tj.get("kernels", []):  # the captured kernel that matches the tuned one
+            if kernel_name.startswith(ent["prefix"]):
+                traffic = ent["fp32_bytes_per_launch_at_bench"]
+                break
 
     # --- e2e: drop-in call with FP64 pinned host arrays (FP32 arithmetic inside)
     Xh0 = X0[:, :].double().cpu().pin_memory()
