@@ -430,8 +430,9 @@ def main():
     ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
                      nl["grid_pos"], nl["chi"])
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
-    # pick the FP32 stencil variant for this grid (all variants give identical results)
-    variant, variant_ms = ctx.autotune(ncol=min(ncol, 64))
+    # pick the FP32 kernel forms for this grid and block width (stencil variants give
+    # identical results)
+    variant, variant_ms = ctx.autotune(ncol=ncol)
     if args.stencil_variant is not None:
         variant = args.stencil_variant
         ctx.set_stencil_variant(variant)

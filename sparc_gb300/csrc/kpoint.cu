@@ -50,18 +50,46 @@ struct StencilZParams {
     KParams k;
 };
 
-// one point per thread, z-register queue, shared plane with x/y halo (as the real kernel);
-// every fetched value is multiplied by the Bloch factor of its unwrapped position
-template <typename CT, int R, int BX, int BY>
+// One point per thread, z-register queue with the plane k+R+1 in flight, the current plane
+// plus its x/y halo in shared memory (two buffers, one barrier per plane), halo / potential /
+// recurrence-term values for the next plane prefetched into registers one plane ahead (the
+// scheme of the real FP64 kernel). Every fetched value is multiplied by the Bloch factor of its
+// unwrapped position. The tile is blockDim.x x blockDim.y (chosen per grid by zstencil_tile so
+// that small grids waste few threads), both at least R; the shared planes are dynamic.
+template <typename CT>
+struct ZW {  // FP32 copies of the FD weights and scalars, converted once per thread
+    float wx[kMaxFDn + 1], wy[kMaxFDn + 1], wz[kMaxFDn + 1], c0, s1, s2, bv;
+};
+
+template <typename CT, int R>
 __device__ __forceinline__ void stencil_z_body(const StencilZParams<CT> &p, int col, int slab)
 {
     using RT = typename Real<CT>::type;
-    __shared__ CT s[BY + 2 * R][BX + 2 * R];
+    extern __shared__ __align__(16) unsigned char zst_raw[];
+    const int BX = blockDim.x, BY = blockDim.y;
+    const int SW = BX + 2 * R, SP = (BY + 2 * R) * SW;  // shared row length, plane size
+    CT *sp = reinterpret_cast<CT *>(zst_raw);             // [2][BY + 2R][BX + 2R]
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     const int zs = slab * p.zlen;
     const int ze = min(zs + p.zlen, p.Nz);
     if (zs >= ze) return;
+    // complex64 works with FP32 copies of the weights (no FP64 conversion per use); complex128
+    // reads them from the kernel parameters directly
+    constexpr bool F32 = sizeof(RT) == 4;
+    ZW<CT> w;
+    if constexpr (F32) {
+#pragma unroll
+        for (int r = 0; r <= R; r++) {
+            w.wx[r] = (float)p.wx[r]; w.wy[r] = (float)p.wy[r]; w.wz[r] = (float)p.wz[r];
+        }
+        w.c0 = (float)p.c0; w.s1 = (float)p.s1; w.s2 = (float)p.s2; w.bv = (float)p.bv;
+    }
+    auto WX = [&](int r) -> RT { if constexpr (F32) return w.wx[r]; else return p.wx[r]; };
+    auto WY = [&](int r) -> RT { if constexpr (F32) return w.wy[r]; else return p.wy[r]; };
+    auto WZ = [&](int r) -> RT { if constexpr (F32) return w.wz[r]; else return p.wz[r]; };
+    const RT c0 = F32 ? (RT)w.c0 : (RT)p.c0, s1 = F32 ? (RT)w.s1 : (RT)p.s1;
+    const RT s2 = F32 ? (RT)w.s2 : (RT)p.s2, bvr = F32 ? (RT)w.bv : (RT)p.bv;
     const int i = x0 + tx, j = y0 + ty;
     const bool active = (i < p.Nx) && (j < p.Ny);
     const int gi = wrapz(i, p.Nx), gj = wrapz(j, p.Ny);
@@ -100,48 +128,88 @@ __device__ __forceinline__ void stencil_z_body(const StencilZParams<CT> &p, int 
                    : d == 1 ? fz_p : cmul(f_own, phase<CT>(d * p.k.kLz));
         return cmul(val, f);
     };
-    CT q[2 * R + 1];
+    CT q[2 * R + 2];  // q[m] = plane k - R + m; q[2R+1] (plane k+R+1) is in flight
 #pragma unroll
-    for (int m = 0; m < 2 * R; m++) q[m] = zload(zs - R + m);
-    for (int k = zs; k < ze; k++) {
-        q[2 * R] = zload(k + R);
+    for (int m = 0; m <= 2 * R; m++) q[m] = zload(zs - R + m);
+    CT h0{0, 0}, h1{0, 0}, h2{0, 0}, h3{0, 0}, vv{0, 0}, zz{0, 0};
+    auto prefetch = [&](int k) {  // halo, potential and recurrence term of plane k
         const long pk = (long)k * NxNy;
-        __syncthreads();
-        s[ty + R][tx + R] = q[R];
-        if (hx) {
-            s[ty + R][tx] = cmul(__ldg(xc + pk + hxl), f_xl);
-            s[ty + R][tx + BX + R] = cmul(__ldg(xc + pk + hxr), f_xr);
-        }
-        if (hy) {
-            s[ty][tx + R] = cmul(__ldg(xc + pk + hyl), f_yl);
-            s[ty + BY + R][tx + R] = cmul(__ldg(xc + pk + hyr), f_yr);
-        }
+        if (hx) { h0 = cmul(__ldg(xc + pk + hxl), f_xl); h1 = cmul(__ldg(xc + pk + hxr), f_xr); }
+        if (hy) { h2 = cmul(__ldg(xc + pk + hyl), f_yl); h3 = cmul(__ldg(xc + pk + hyr), f_yr); }
+        if (p.v) vv.x = (RT)(p.bv * p.v[own + pk]);
+        if (p.v32) vv.x = bvr * p.v32[own + pk];
+        if (zc) zz = zc[own + pk];
+    };
+    prefetch(zs);
+    for (int k = zs; k < ze; k++) {
+        CT *s = sp + (k & 1) * SP;
+        q[2 * R + 1] = zload(k + R + 1);
+        s[(ty + R) * SW + tx + R] = q[R];
+        if (hx) { s[(ty + R) * SW + tx] = h0; s[(ty + R) * SW + tx + BX + R] = h1; }
+        if (hy) { s[ty * SW + tx + R] = h2; s[(ty + BY + R) * SW + tx + R] = h3; }
+        const RT vcur = vv.x;
+        const CT zcur = zz;
+        if (k + 1 < ze) prefetch(k + 1);
         __syncthreads();
         if (active) {
-            CT res = cscale(q[R], (RT)p.c0);
+            // three independent chains (x, y, z) of fused multiply-adds per component
+            CT rx = cscale(q[R], c0), ry{0, 0}, rz{0, 0};
+            const CT *srow = s + (ty + R) * SW + tx + R;
 #pragma unroll
             for (int r = 1; r <= R; r++) {
-                const CT rx = cscale(cadd(s[ty + R][tx + R - r], s[ty + R][tx + R + r]), (RT)p.wx[r]);
-                const CT ry = cscale(cadd(s[ty + R - r][tx + R], s[ty + R + r][tx + R]), (RT)p.wy[r]);
-                const CT rz = cscale(cadd(q[R - r], q[R + r]), (RT)p.wz[r]);
-                res = cadd(res, cadd(cadd(rx, ry), rz));
+                const CT sx = cadd(srow[-r], srow[r]);
+                const CT sy = cadd(srow[-r * SW], srow[r * SW]);
+                const CT sz = cadd(q[R - r], q[R + r]);
+                const RT a = WX(r), b = WY(r), c = WZ(r);
+                rx.x = fma(sx.x, a, rx.x); rx.y = fma(sx.y, a, rx.y);
+                ry.x = fma(sy.x, b, ry.x); ry.y = fma(sy.y, b, ry.y);
+                rz.x = fma(sz.x, c, rz.x); rz.y = fma(sz.y, c, rz.y);
             }
-            const long pt = own + pk;
-            if (p.v) res = cadd(res, cscale(q[R], (RT)(p.bv * p.v[pt])));
-            if (p.v32) res = cadd(res, cscale(q[R], (RT)p.bv * p.v32[pt]));
-            CT o = cscale(res, (RT)p.s1);
-            if (zc) o = cadd(o, cscale(zc[pt], (RT)p.s2));
-            oc[pt] = o;
+            CT res = cadd(rx, cadd(ry, rz));
+            if (p.v || p.v32) res = cadd(res, cscale(q[R], vcur));
+            CT o = cscale(res, s1);
+            if (zc) o = cadd(o, cscale(zcur, s2));
+            oc[own + (long)k * NxNy] = o;
         }
 #pragma unroll
-        for (int m = 0; m < 2 * R; m++) q[m] = q[m + 1];
+        for (int m = 0; m <= 2 * R; m++) q[m] = q[m + 1];
     }
 }
 
-template <typename CT, int R, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY) k_stencil_z(const StencilZParams<CT> p)
+// Threads per block of the complex stencil: complex128 (FP64-pipe bound, more registers per
+// point) at most 256, complex64 at most 512.
+template <typename CT>
+__host__ __device__ constexpr int zstencil_threads() { return sizeof(CT) == 16 ? 256 : 512; }
+
+// Tile of the complex stencil for an Nx x Ny plane: the widest x extent in [16, 64] with the
+// least padding, then the tallest y extent in [R, maxt / bx] with the least padding.
+static void zstencil_tile(int Nx, int Ny, int R, int maxt, int *bx, int *by)
 {
-    stencil_z_body<CT, R, BX, BY>(p, blockIdx.z / p.nslab, blockIdx.z % p.nslab);
+    int best = 1 << 30;
+    *bx = 32;
+    for (int t = std::min(64, std::max(16, Nx)); t >= 16; t--) {
+        const int waste = (Nx + t - 1) / t * t - Nx;
+        if (waste < best) { best = waste; *bx = t; }
+    }
+    best = 1 << 30;
+    *by = R;
+    for (int t = std::max(R, maxt / *bx); t >= R; t--) {
+        if (*bx * t > maxt) continue;
+        const int waste = (Ny + t - 1) / t * t - Ny;
+        if (waste < best) { best = waste; *by = t; }
+    }
+}
+
+template <typename CT>
+static size_t zstencil_smem(int bx, int by, int R)
+{
+    return sizeof(CT) * 2 * (size_t)(bx + 2 * R) * (by + 2 * R);
+}
+
+template <typename CT, int R>
+__global__ void __launch_bounds__(zstencil_threads<CT>()) k_stencil_z(const StencilZParams<CT> p)
+{
+    stencil_z_body<CT, R>(p, blockIdx.z / p.nslab, blockIdx.z % p.nslab);
 }
 
 // projection: block = (atom image g, group of 32 columns), threads stride over the image's
@@ -371,8 +439,8 @@ struct BConst {
     const float *veff32;
 };
 
-template <typename CT, int R, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY)
+template <typename CT, int R>
+__global__ void __launch_bounds__(zstencil_threads<CT>())
     k_stencil_zb(const BBlock<CT> *__restrict__ blocks, const BCoef *__restrict__ coef,
                  const int2 *__restrict__ work, const BConst cs, int deg, int in_sel,
                  int out_sel, int z_sel)
@@ -393,7 +461,7 @@ __global__ void __launch_bounds__(BX *BY)
     for (int r = 0; r <= kMaxFDn; r++) { p.wx[r] = cs.wx[r]; p.wy[r] = cs.wy[r]; p.wz[r] = cs.wz[r]; }
     p.c0 = cf.c0; p.bv = 1.0; p.s1 = cf.s1; p.s2 = cf.s2;
     p.k.kLx = B.kL[0]; p.k.kLy = B.kL[1]; p.k.kLz = B.kL[2];
-    stencil_z_body<CT, R, BX, BY>(p, bc.y, slab);
+    stencil_z_body<CT, R>(p, bc.y, slab);
 }
 
 // grid (image, column group); cg[y] = (block, first column)
@@ -519,7 +587,7 @@ static int stencil_z(sgpu_ctx *ctx, const double *k, int ncol, double a, double 
                      const double *v, const float *v32, const CT *x, long ldx, CT *out,
                      long ldo, double s1, double s2, const CT *z, long ldz, cudaStream_t st)
 {
-    constexpr int R = 6, BX = 32, BY = 8;
+    constexpr int R = 6;
     if (ctx->FDn != R) {
         set_error("stencil: only FD order 12 (radius 6) is built");
         return SGPU_ERR_ARG;
@@ -546,6 +614,11 @@ static int stencil_z(sgpu_ctx *ctx, const double *k, int ncol, double a, double 
     p.k.kLx = k[0] * ks->L[0];
     p.k.kLy = k[1] * ks->L[1];
     p.k.kLz = k[2] * ks->L[2];
+    int BX, BY;
+    zstencil_tile(ctx->Nx, ctx->Ny, R, zstencil_threads<CT>(), &BX, &BY);
+    const size_t zsm = zstencil_smem<CT>(BX, BY, R);
+    SGPU_CUDA_TRY(cudaFuncSetAttribute(k_stencil_z<CT, R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsm));
     const int tilesx = (ctx->Nx + BX - 1) / BX, tilesy = (ctx->Ny + BY - 1) / BY;
     long blocks1 = (long)tilesx * tilesy * ncol;
     int nslab = 1;
@@ -560,7 +633,7 @@ static int stencil_z(sgpu_ctx *ctx, const double *k, int ncol, double a, double 
         q.out = out + (long)c0i * ldo;
         if (q.z) q.z = z + (long)c0i * ldz;
         ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
-        k_stencil_z<CT, R, BX, BY><<<dim3(tilesx, tilesy, nc * nslab), dim3(BX, BY), 0, st>>>(q);
+        k_stencil_z<CT, R><<<dim3(tilesx, tilesy, nc * nslab), dim3(BX, BY), zsm, st>>>(q);
     }
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
@@ -694,7 +767,7 @@ template <typename CT>
 static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
                              cudaStream_t st)
 {
-    constexpr int R = 6, BX = 32, BY = 8;
+    constexpr int R = 6;
     KpointState *ks;
     SGPU_TRY(kstate(ctx, &ks));
     const Nonlocal &nl = ctx->nl;
@@ -812,6 +885,11 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
     cs.Nx = ctx->Nx; cs.Ny = ctx->Ny; cs.Nz = ctx->Nz; cs.m = m; cs.Nd = Nd;
     cs.veff64 = ctx->veff64;
     cs.veff32 = ctx->veff32;
+    int BX, BY;
+    zstencil_tile(ctx->Nx, ctx->Ny, R, zstencil_threads<CT>(), &BX, &BY);
+    const size_t zsm = zstencil_smem<CT>(BX, BY, R);  // attribute set before any capture
+    SGPU_CUDA_TRY(cudaFuncSetAttribute(k_stencil_zb<CT, R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsm));
     const int tilesx = (ctx->Nx + BX - 1) / BX, tilesy = (ctx->Ny + BY - 1) / BY;
     int nslab = 1;
     while ((long)tilesx * tilesy * totcols * nslab < 152L * 8 && ctx->Nz / (nslab * 2) >= 8)
@@ -865,9 +943,9 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
             for (long w0 = 0; w0 < totcols; w0 += maxw) {
                 const long nw = std::min(maxw, totcols - w0);
                 ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
-                k_stencil_zb<CT, R, BX, BY><<<dim3(tilesx, tilesy, (unsigned)(nw * nslab)),
-                                              dim3(BX, BY), 0, st>>>(dB, dC, dW + w0, cs, j, in,
-                                                                     out, zsel);
+                k_stencil_zb<CT, R><<<dim3(tilesx, tilesy, (unsigned)(nw * nslab)),
+                                      dim3(BX, BY), zsm, st>>>(dB, dC, dW + w0, cs, j, in, out,
+                                                               zsel);
                 ctx->launches++;
             }
             if (has_nl) {

@@ -604,8 +604,8 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         Y32 = X32 + nb;
     }
     struct G4 { float *p; ~G4() { if (p) cudaFree(p); } } g32{X32};
-    if (mixed && !ctx->stencil_tuned)
-        SGPU_TRY(sgpu_autotune(ctx, std::min(Ns, 64), nullptr, nullptr));
+    if (mixed && !ctx->stencil_tuned)  // tuned at the block width the filter runs at
+        SGPU_TRY(sgpu_autotune(ctx, Ns, nullptr, nullptr));
     k_init_orbitals<<<152 * 8, 256, 0, st>>>(X64, nb, prm->seed);
     ctx->launches++;
     if (mixed) SGPU_TRY(convert_cols<double, float>(X64, nb, X32, nb, nb, 1, st));
