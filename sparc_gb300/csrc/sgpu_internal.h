@@ -16,8 +16,8 @@ namespace sgpu {
 
 constexpr int kMaxFDn = 6;  // the library is specialised for FD order 12 (radius 6)
 constexpr int kApplyChunkPts = 128;  // covered points per chunk of the staged nonlocal apply
-constexpr int kRangePts = 256;       // covered points per range of the range projection
-constexpr int kRangeMaxEnt = 640;    // entries per range at most (bounds its staged Chi)
+constexpr int kRangePts = 128;       // covered points per range of the range projection
+constexpr int kRangeMaxEnt = 320;    // entries per range at most (bounds its staged Chi)
 constexpr int kRangeItemEnt = 96;    // entries per work item of the range projection at most
 
 // thread-local error text, returned by sgpu_last_error()
