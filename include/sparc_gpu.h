@@ -342,6 +342,10 @@ typedef struct {
     double *history;            /* optional host array of 3 * maxit_scf: per SCF iteration the
                                    free energy, the SCF error and the seconds since the call
                                    began (NULL: not recorded) */
+    double *psi_out;            /* optional (host or device) Nd x Nstates: the final orbitals,
+                                   as the force calculation uses them (NULL: not returned) */
+    double *phi_out;            /* optional Nd: electrostatic potential of the final density */
+    double *vxc_out;            /* optional Nd: exchange-correlation potential of the same */
 } sgpu_scf_params;
 
 typedef struct {
@@ -360,6 +364,41 @@ typedef struct {
 int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b,
              const double *rho_init, const double *rho_core, double *rho_out,
              double *lambda_out, double *occ_out, sgpu_scf_result *res);
+
+/* ------------------------------------------------------------------- forces */
+
+/* Local (pseudocharge) force components of the atoms at atom_pos (as for
+ * sgpu_Generate_PseudoChargeDensity: type-major, nAtomv per type, cutoff 3 per type or NULL,
+ * ref_cutoff REFERENCE_CUTOFF) from the electrostatic potential phi (Nd, host or device),
+ * written to forces (host, 3 * n_atom, overwritten). Replaces Calculate_local_forces_linear
+ * (src/forces.c:157). */
+int sgpu_Calculate_local_forces(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                                const double *atom_pos, const double *cutoff, double ref_cutoff,
+                                const double *phi, double *forces);
+
+/* Nonlocal force components of the context's projector atoms from ncol orbitals X (Nd x ncol,
+ * leading dimension ldi, host or device) with occupations occ (ncol) and occfac (2 without
+ * spin), ADDED to forces (host, 3 * n_atom). Replaces Calculate_nonlocal_forces_linear and
+ * its integrals (src/forces.c:750, :849, :890, :926). */
+int sgpu_Calculate_nonlocal_forces(sgpu_ctx *ctx, int ncol, const double *X, int ldi,
+                                   const double *occ, double occfac, const double *cell,
+                                   double *forces);
+
+/* Core-correction (NLCC) force components from the exchange-correlation potential Vxc (Nd,
+ * host or device), written to forces_xc (host, 3 * n_atom, overwritten); atoms and cutoff as
+ * for sgpu_Calculate_local_forces. Replaces Calculate_forces_xc_linear (src/forces.c:473). */
+int sgpu_Calculate_forces_xc(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                             const double *atom_pos, const double *cutoff, const double *Vxc,
+                             double *forces_xc);
+
+/* Dx = d x / d(direction dir: 0 x, 1 y, 2 z) for ncol columns, periodic FD gradient of the
+ * context's order (host or device arrays). Replaces Gradient_vectors_dir
+ * (src/gradVecRoutines.c:33) for orthogonal cells. */
+int sgpu_Gradient_vectors_dir(sgpu_ctx *ctx, int ncol, const double *cell, const double *x,
+                              int ldi, double *Dx, int ldo, int dir);
+
+/* Subtract the mean force from every atom (Symmetrize_forces, src/forces.c:1399). */
+int sgpu_Symmetrize_forces(int n_atom, double *forces);
 
 /* Device time of the last sgpu_ChebyshevFiltering call's filter loop, in milliseconds. */
 int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms);

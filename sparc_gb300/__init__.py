@@ -37,7 +37,8 @@ EXPORTED = [
     "sgpu_mlp_forward", "sgpu_mlp_loss_grad", "sgpu_mlp_zero_grad", "sgpu_mlp_adam_step",
     "sgpu_Project_Hamiltonian_std", "sgpu_Solve_Standard_EigenProblem",
     "sgpu_set_nonlocal_apply_variant", "sgpu_set_nonlocal_project_variant", "sgpu_get_variants",
-    "sgpu_get_tuning",
+    "sgpu_get_tuning", "sgpu_Calculate_local_forces", "sgpu_Calculate_nonlocal_forces",
+    "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
 ]
 
 
@@ -78,7 +79,9 @@ class ScfParams(ctypes.Structure):
                 ("Esc", ctypes.c_double), ("precision", ctypes.c_int),
                 ("fp64_switch_error", ctypes.c_double), ("graded_tail", ctypes.c_int),
                 ("tail_fp64_degrees", ctypes.c_int), ("seed", ctypes.c_ulonglong),
-                ("verbose", ctypes.c_int), ("history", ctypes.c_void_p)]
+                ("verbose", ctypes.c_int), ("history", ctypes.c_void_p),
+                ("psi_out", ctypes.c_void_p), ("phi_out", ctypes.c_void_p),
+                ("vxc_out", ctypes.c_void_p)]
 
 
 class ScfResult(ctypes.Structure):
@@ -171,6 +174,7 @@ class Context:
         _check(lib().sgpu_set_nonlocal(self._h, len(arrs[0]) - 1, _ptr(arrs[0]), _ptr(arrs[1]),
                                        len(arrs[2]), _ptr(arrs[2]), _ptr(arrs[3]), _ptr(arrs[4]),
                                        _ptr(arrs[5])))
+        self._natom_nl = len(arrs[0]) - 1
 
     def set_grid_coeffs(self, cx, cy, cz, dV):
         cx, cy, cz = (np.ascontiguousarray(c, dtype=np.float64) for c in (cx, cy, cz))
@@ -232,6 +236,55 @@ class Context:
         nat = np.ascontiguousarray(nAtomv, dtype=np.int32)
         pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
         _check(lib().sgpu_CalculateNonlocalProjectors(self._h, _ptr(cell), _ptr(nat), _ptr(pos)))
+        self._natom_nl = int(nat.sum())
+
+    # ---- forces (src/forces.c)
+    def Calculate_local_forces(self, cell, nAtomv, atom_pos, phi, ref_cutoff=0.5, cutoff=None):
+        """Local force components, (n_atom, 3)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        nat = np.ascontiguousarray(nAtomv, dtype=np.int32)
+        pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
+        cut = None if cutoff is None else np.ascontiguousarray(cutoff, dtype=np.float64)
+        f = np.zeros(3 * int(nat.sum()))
+        _check(lib().sgpu_Calculate_local_forces(
+            self._h, _ptr(cell), _ptr(nat), _ptr(pos), _ptr(cut), ctypes.c_double(ref_cutoff),
+            _ptr(np.ascontiguousarray(phi, dtype=np.float64)), _ptr(f)))
+        return f.reshape(-1, 3)
+
+    def Calculate_nonlocal_forces(self, cell, X, occ, occfac=2.0):
+        """Nonlocal force components of the projector atoms from orbitals X (ncol, Nd)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        ncol, ld = self._ncol_ld(X)
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        f = np.zeros(3 * self._nl_natom())
+        _check(lib().sgpu_Calculate_nonlocal_forces(self._h, ncol, _ptr(X), ld, _ptr(occ),
+                                                    ctypes.c_double(occfac), _ptr(cell), _ptr(f)))
+        return f.reshape(-1, 3)
+
+    def Calculate_forces_xc(self, cell, nAtomv, atom_pos, vxc, cutoff=None):
+        """Core-correction (NLCC) force components, (n_atom, 3)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        nat = np.ascontiguousarray(nAtomv, dtype=np.int32)
+        pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
+        cut = None if cutoff is None else np.ascontiguousarray(cutoff, dtype=np.float64)
+        f = np.zeros(3 * int(nat.sum()))
+        _check(lib().sgpu_Calculate_forces_xc(self._h, _ptr(cell), _ptr(nat), _ptr(pos), _ptr(cut),
+                                              _ptr(np.ascontiguousarray(vxc, dtype=np.float64)),
+                                              _ptr(f)))
+        return f.reshape(-1, 3)
+
+    def Gradient_vectors_dir(self, cell, x, dx, direction):
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        ncol, ld = self._ncol_ld(x)
+        _, ldo = self._ncol_ld(dx)
+        _check(lib().sgpu_Gradient_vectors_dir(self._h, ncol, _ptr(cell), _ptr(x), ld, _ptr(dx),
+                                               ldo, int(direction)))
+
+    def _nl_natom(self):
+        if getattr(self, "_natom_nl", None) is None:
+            raise SgpuError("the number of projector atoms is not known: call set_nonlocal or "
+                            "CalculateNonlocalProjectors first")
+        return self._natom_nl
 
     # ---- hot path (x, y: (ncol, Nd) C-contiguous == Nd x ncol column-major, ld = Nd)
     def _ncol_ld(self, x):
@@ -429,8 +482,10 @@ class Context:
                                              ctypes.byref(e)))
         return e.value
 
-    def scf(self, params, b, rho_init, rho_core=None, Nstates=None):
-        """Run sgpu_scf; returns (result dict, final density, eigenvalues, occupations)."""
+    def scf(self, params, b, rho_init, rho_core=None, Nstates=None, fields=None):
+        """Run sgpu_scf; returns (result dict, final density, eigenvalues, occupations). With
+        fields a dict, it also receives the final orbitals ("psi", Nstates x Nd), the
+        electrostatic potential ("phi") and the exchange-correlation potential ("vxc")."""
         Ns = params.Nstates
         rho = np.zeros(self.Nd)
         lam = np.zeros(Ns)
@@ -441,11 +496,19 @@ class Context:
         rc_ = None if rho_core is None else np.ascontiguousarray(rho_core, dtype=np.float64)
         hist = np.full(3 * max(1, params.maxit_scf), np.nan)
         params.history = hist.ctypes.data
+        if fields is not None:
+            fields["psi"] = np.zeros((Ns, self.Nd))
+            fields["phi"] = np.zeros(self.Nd)
+            fields["vxc"] = np.zeros(self.Nd)
+            params.psi_out = fields["psi"].ctypes.data
+            params.phi_out = fields["phi"].ctypes.data
+            params.vxc_out = fields["vxc"].ctypes.data
         try:
             _check(lib().sgpu_scf(self._h, ctypes.byref(params), _ptr(b), _ptr(r0), _ptr(rc_),
                                   _ptr(rho), _ptr(lam), _ptr(occ), ctypes.byref(res)))
         finally:
             params.history = None
+            params.psi_out = params.phi_out = params.vxc_out = None
         out = res.as_dict()
         h = hist.reshape(-1, 3)[:out["scf_iters"]]
         out["history"] = {"Etot": h[:, 0].tolist(), "scf_error": h[:, 1].tolist(),

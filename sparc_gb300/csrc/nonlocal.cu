@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256)
 // only in the atomics, so the order of those additions is not fixed). The tile is then written
 // back once. Every covered output element is read and written once per launch, in grid order.
 template <int MAXJ>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_nl_apply_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
                      const int *__restrict__ rng_item0, const int *__restrict__ item_e0,
                      const int2 *__restrict__ item_row, const int *__restrict__ pe_lp,
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256)
 {
     constexpr int NC = 64, OLD = NC + 1;             // columns per group, padded tile row
     constexpr int MAXJP = (MAXJ + 3) / 4 * 4;
-    constexpr int GB = 32;                           // gathers in flight per thread
+    constexpr int GB = 8;                            // gathers in flight per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *cs = reinterpret_cast<float *>(smem_raw);  // [entries][MAXJP]
     const int r = blockIdx.x;
@@ -647,7 +647,7 @@ long nonlocal_alpha_ld(int ncol, int elem_bytes)
 
 template <typename T, int MAXJ>
 static int project_launch(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
-                          cudaStream_t st)
+                          const T *gamma, T dV, cudaStream_t st)
 {
     constexpr int NC = sizeof(T) == 4 ? 128 : 64, PCH = 64;
     constexpr int VW = 16 / sizeof(T), MAXJP = (MAXJ + VW - 1) / VW * VW;
@@ -661,8 +661,7 @@ static int project_launch(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alph
     ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
     kern<<<nl.nseg, kProjThreads, smem, st>>>(
         nl.seg_img, nl.seg_start, nl.img_atom, nl.img_ndc, nl.img_off, nl.img_chi_off,
-        nl.grid_pos, chi_of<T>(nl), nl.ip_displ, gamma_of<T>(nl), ncol, x, ldx, alpha, lda,
-        (T)ctx->dV);
+        nl.grid_pos, chi_of<T>(nl), nl.ip_displ, gamma, ncol, x, ldx, alpha, lda, dV);
     return SGPU_OK;
 }
 
@@ -683,6 +682,34 @@ static int project_range_launch(sgpu_ctx *ctx, int ncol, const float *x, long ld
     return SGPU_OK;
 }
 
+// alpha += gamma * dV * Chi^T x with the segment kernel (the FP64 path and the plain
+// projection of the force integrals)
+template <typename T>
+static int project_segments(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
+                            const T *gamma, T dV, cudaStream_t st)
+{
+    const Nonlocal &nl = ctx->nl;
+    if (nl.max_np <= 9)
+        SGPU_TRY(project_launch<T, 9>(ctx, ncol, x, ldx, alpha, lda, gamma, dV, st));
+    else if (nl.max_np <= 18)
+        SGPU_TRY(project_launch<T, 18>(ctx, ncol, x, ldx, alpha, lda, gamma, dV, st));
+    else if (nl.max_np <= 32)
+        SGPU_TRY(project_launch<T, 32>(ctx, ncol, x, ldx, alpha, lda, gamma, dV, st));
+    else {
+        set_error("nonlocal: more than 32 projectors per atom is not built");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
+int launch_nonlocal_project_plain(sgpu_ctx *ctx, int ncol, const double *x, long ldx,
+                                  double *alpha, long lda, const double *ones, cudaStream_t st)
+{
+    if (!ctx->has_nl || ctx->nl.nimg == 0 || ncol <= 0) return SGPU_OK;
+    return project_segments<double>(ctx, ncol, x, ldx, alpha, lda, ones, 1.0, st);
+}
+
 template <typename T>
 int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
                             cudaStream_t st)
@@ -701,18 +728,7 @@ int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *al
             return SGPU_OK;
         }
     }
-    if (nl.max_np <= 9)
-        SGPU_TRY(project_launch<T, 9>(ctx, ncol, x, ldx, alpha, lda, st));
-    else if (nl.max_np <= 18)
-        SGPU_TRY(project_launch<T, 18>(ctx, ncol, x, ldx, alpha, lda, st));
-    else if (nl.max_np <= 32)
-        SGPU_TRY(project_launch<T, 32>(ctx, ncol, x, ldx, alpha, lda, st));
-    else {
-        set_error("nonlocal: more than 32 projectors per atom is not built");
-        return SGPU_ERR_ARG;
-    }
-    SGPU_CUDA_TRY(cudaGetLastError());
-    return SGPU_OK;
+    return project_segments<T>(ctx, ncol, x, ldx, alpha, lda, gamma_of<T>(nl), (T)ctx->dV, st);
 }
 
 template <typename T>

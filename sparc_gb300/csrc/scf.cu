@@ -781,6 +781,16 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
         }
     }
     if (rho_out) SGPU_CUDA_TRY(cudaMemcpyAsync(rho_out, d_rho, sizeof(double) * N, cudaMemcpyDefault, st));
+    // what the force calculation reads: the last rotated orbitals and the potentials of the
+    // final (mixed) density, as the reference leaves them when its SCF loop ends
+    if (prm->psi_out) {
+        if (mixed) SGPU_TRY(convert_cols<float, double>(X32, nb, X64, nb, nb, 1, st));
+        SGPU_CUDA_TRY(cudaMemcpyAsync(prm->psi_out, X64, sizeof(double) * nb, cudaMemcpyDefault, st));
+    }
+    if (prm->phi_out)
+        SGPU_CUDA_TRY(cudaMemcpyAsync(prm->phi_out, d_phi, sizeof(double) * N, cudaMemcpyDefault, st));
+    if (prm->vxc_out)
+        SGPU_CUDA_TRY(cudaMemcpyAsync(prm->vxc_out, d_vxc, sizeof(double) * N, cudaMemcpyDefault, st));
     if (lambda_out) std::copy(lam.begin(), lam.end(), lambda_out);
     if (occ_out) std::copy(occ.begin(), occ.end(), occ_out);
     SGPU_CUDA_TRY(cudaStreamSynchronize(st));

@@ -166,6 +166,7 @@ struct PcImage {
     int xs, ys, zs;     // first grid index of the clipped rb-box
     int nx, ny, nz;     // box extents
     int type;
+    int atom;           // index of the atom (type-major order)
 };
 
 struct PcWeights {
@@ -246,6 +247,129 @@ __global__ void __launch_bounds__(256) k_pseudocharge(
     }
     const double tot = block_sum(esc, red);
     if (threadIdx.x == 0 && tot != 0.0) atomicAdd(esc_acc, tot);
+}
+
+struct D1Weights {
+    double d[3 * (kMaxFDn + 1)];  // first-derivative weights per offset and direction (x, y, z)
+};
+
+// Local forces (Calculate_local_forces_linear, src/forces.c:157-434). One thread per point of
+// one image's rb-box: bJ and bJ_ref as k_pseudocharge forms them, the D1 gradient of
+// VcJ = VJ_ref - VJ from the values at the stencil points, and the cell fields b + b_ref,
+// grad(phi) and grad(Vc) (gphi, gvc: three Nd blocks each). The image's sum of
+//   -bJ grad(phi) + (grad(VcJ) (b + b_ref) - grad(Vc) (bJ + bJ_ref)) / 2
+// times dV is added to the force of its atom.
+__global__ void __launch_bounds__(256) k_local_forces(
+    const PcImage *__restrict__ imgs, PsdDevSet P, PcWeights W, D1Weights G, int FDn, int Nx,
+    int Ny, double dx, double dy, double dz, double ref_cutoff, const double *__restrict__ b,
+    const double *__restrict__ bref, const double *__restrict__ gphi,
+    const double *__restrict__ gvc, long Nd, double dV, double *__restrict__ forces)
+{
+    __shared__ double red[8];
+    const PcImage im = imgs[blockIdx.y];
+    const long npts = (long)im.nx * im.ny * im.nz;
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double f[3] = {0.0, 0.0, 0.0};
+    if (p < npts) {
+        const PsdDev &ps = P.t[im.type];
+        const double Z = (double)ps.Znucl;
+        const int i = (int)(p % im.nx);
+        const int j = (int)((p / im.nx) % im.ny);
+        const int k = (int)(p / ((long)im.nx * im.ny));
+        const double xsh = im.x0 - dx * (im.xs - FDn);
+        const double ysh = im.y0 - dy * (im.ys - FDn);
+        const double zsh = im.z0 - dz * (im.zs - FDn);
+        const double xc = (i + FDn) * dx - xsh, yc = (j + FDn) * dy - ysh,
+                     zc = (k + FDn) * dz - zsh;
+        const double R0 = sqrt(xc * xc + yc * yc + zc * zc);
+        double s = W.w0 * vloc_at(ps, R0), sr = W.w0 * vref_at(R0, ref_cutoff, Z);
+        double dvc[3] = {0.0, 0.0, 0.0};
+        for (int r = 1; r <= FDn; r++) {
+            const double xm = (i + FDn - r) * dx - xsh, xp = (i + FDn + r) * dx - xsh;
+            const double ym = (j + FDn - r) * dy - ysh, yp = (j + FDn + r) * dy - ysh;
+            const double zm = (k + FDn - r) * dz - zsh, zp = (k + FDn + r) * dz - zsh;
+            const double Rs[6] = {sqrt(xm * xm + yc * yc + zc * zc), sqrt(xp * xp + yc * yc + zc * zc),
+                                  sqrt(xc * xc + ym * ym + zc * zc), sqrt(xc * xc + yp * yp + zc * zc),
+                                  sqrt(xc * xc + yc * yc + zm * zm), sqrt(xc * xc + yc * yc + zp * zp)};
+            double v[6], vr[6];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                v[q] = vloc_at(ps, Rs[q]);
+                vr[q] = vref_at(Rs[q], ref_cutoff, Z);
+            }
+            s += (v[0] + v[1]) * W.w[3 * r] + (v[2] + v[3]) * W.w[3 * r + 1] +
+                 (v[4] + v[5]) * W.w[3 * r + 2];
+            sr += (vr[0] + vr[1]) * W.w[3 * r] + (vr[2] + vr[3]) * W.w[3 * r + 1] +
+                  (vr[4] + vr[5]) * W.w[3 * r + 2];
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                dvc[d] += ((vr[2 * d + 1] - v[2 * d + 1]) - (vr[2 * d] - v[2 * d])) * G.d[3 * r + d];
+        }
+        const long g = (long)(im.zs + k) * Nx * Ny + (long)(im.ys + j) * Nx + (im.xs + i);
+        const double bb = b[g] + bref[g], bj = s + sr;
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            f[d] = -s * gphi[d * Nd + g] + 0.5 * (dvc[d] * bb - gvc[d * Nd + g] * bj);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const double t = block_sum(f[d], red);
+        if (threadIdx.x == 0) atomicAdd(&forces[3 * im.atom + d], t * dV);
+        __syncthreads();
+    }
+}
+
+// Core-correction (NLCC) forces (Calculate_forces_xc_linear, src/forces.c:473-700): one thread
+// per point of one image's rb-box; the D1 gradient of the splined core density rho_c,J (zero
+// beyond the table) from its values at the stencil points, times Vxc, summed over the box and
+// added (times dV) to the force of the image's atom.
+__global__ void __launch_bounds__(256) k_xc_forces(
+    const PcImage *__restrict__ imgs, PsdDevSet P, D1Weights G, int FDn, int Nx, int Ny,
+    double dx, double dy, double dz, const double *__restrict__ vxc, double dV,
+    double *__restrict__ forces)
+{
+    __shared__ double red[8];
+    const PcImage im = imgs[blockIdx.y];
+    const long npts = (long)im.nx * im.ny * im.nz;
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    double f[3] = {0.0, 0.0, 0.0};
+    if (p < npts) {
+        const PsdDev &ps = P.t[im.type];
+        const int i = (int)(p % im.nx);
+        const int j = (int)((p / im.nx) % im.ny);
+        const int k = (int)(p / ((long)im.nx * im.ny));
+        const double xsh = im.x0 - dx * (im.xs - FDn);
+        const double ysh = im.y0 - dy * (im.ys - FDn);
+        const double zsh = im.z0 - dz * (im.zs - FDn);
+        const double xc = (i + FDn) * dx - xsh, yc = (j + FDn) * dy - ysh,
+                     zc = (k + FDn) * dz - zsh;
+        auto rhoc = [&](double R) {
+            return R <= ps.rchrg ? spline_at(ps.grid, ps.rhoc, ps.yd_rhoc, ps.size, ps.uniform, R)
+                                 : 0.0;
+        };
+        double drc[3] = {0.0, 0.0, 0.0};
+        for (int r = 1; r <= FDn; r++) {
+            const double xm = (i + FDn - r) * dx - xsh, xp = (i + FDn + r) * dx - xsh;
+            const double ym = (j + FDn - r) * dy - ysh, yp = (j + FDn + r) * dy - ysh;
+            const double zm = (k + FDn - r) * dz - zsh, zp = (k + FDn + r) * dz - zsh;
+            drc[0] += (rhoc(sqrt(xp * xp + yc * yc + zc * zc)) -
+                       rhoc(sqrt(xm * xm + yc * yc + zc * zc))) * G.d[3 * r];
+            drc[1] += (rhoc(sqrt(xc * xc + yp * yp + zc * zc)) -
+                       rhoc(sqrt(xc * xc + ym * ym + zc * zc))) * G.d[3 * r + 1];
+            drc[2] += (rhoc(sqrt(xc * xc + yc * yc + zp * zp)) -
+                       rhoc(sqrt(xc * xc + yc * yc + zm * zm))) * G.d[3 * r + 2];
+        }
+        const long g = (long)(im.zs + k) * Nx * Ny + (long)(im.ys + j) * Nx + (im.xs + i);
+        const double v = vxc[g];
+#pragma unroll
+        for (int d = 0; d < 3; d++) f[d] = v * drc[d];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const double t = block_sum(f[d], red);
+        if (threadIdx.x == 0) atomicAdd(&forces[3 * im.atom + d], t * dV);
+        __syncthreads();
+    }
 }
 
 // sums over the cell: [0] b, [1] rho_at, [2] (b + bref) * Vc
@@ -402,6 +526,100 @@ static int deliver(const double *src, double *dst, long n, cudaStream_t st)
     if (!dst) return SGPU_OK;
     SGPU_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDefault, st));
     return SGPU_OK;
+}
+
+// Images of every atom whose rb-box meets the cell, with the box clipped to the cell
+// (GetInfluencingAtoms, src/electrostatics.c:578): rb = cutoff[3 * type + d], or the values of
+// the last cut-off call when cutoff is NULL. maxpts: the largest box.
+static int pc_images(const sgpu_ctx *ctx, const SetupState &s, const double *cell,
+                     const double h[3], const int *nAtomv, const double *atom_pos,
+                     const double *cutoff, const char *who, std::vector<PcImage> &imgs,
+                     long *maxpts)
+{
+    const int N[3] = {ctx->Nx, ctx->Ny, ctx->Nz};
+    imgs.clear();
+    *maxpts = 0;
+    int atom = 0;
+    for (size_t t = 0; t < s.types.size(); t++) {
+        double rb[3];
+        for (int d = 0; d < 3; d++) {
+            rb[d] = cutoff ? cutoff[3 * t + d] : s.types[t].cutoff[d];
+            if (!(rb[d] > 0)) {
+                set_error(std::string(who) + ": no cut-off for type " + std::to_string(t) +
+                          " (call sgpu_Calculate_PseudochargeCutoff)");
+                return SGPU_ERR_STATE;
+            }
+        }
+        for (int a = 0; a < nAtomv[t]; a++, atom++) {
+            const double *p0 = atom_pos + 3 * atom;
+            int lo[3], hi[3];
+            for (int d = 0; d < 3; d++) image_range(p0[d], cell[d], rb[d], &lo[d], &hi[d]);
+            for (int rr = lo[2]; rr <= hi[2]; rr++) {
+                const double z = p0[2] + cell[2] * rr;
+                if (z < -rb[2] || z >= N[2] * h[2] + rb[2]) continue;
+                for (int qq = lo[1]; qq <= hi[1]; qq++) {
+                    const double y = p0[1] + cell[1] * qq;
+                    if (y < -rb[1] || y >= N[1] * h[1] + rb[1]) continue;
+                    for (int pp = lo[0]; pp <= hi[0]; pp++) {
+                        const double x = p0[0] + cell[0] * pp;
+                        if (x < -rb[0] || x >= N[0] * h[0] + rb[0]) continue;
+                        const double c[3] = {x, y, z};
+                        int s0[3], e0[3];
+                        for (int d = 0; d < 3; d++) {
+                            s0[d] = std::max(0, (int)std::ceil((c[d] - rb[d]) / h[d]));
+                            e0[d] = std::min(N[d] - 1, (int)std::floor((c[d] + rb[d]) / h[d]));
+                        }
+                        if (e0[0] < s0[0] || e0[1] < s0[1] || e0[2] < s0[2]) continue;
+                        PcImage im{x, y, z, s0[0], s0[1], s0[2], e0[0] - s0[0] + 1,
+                                   e0[1] - s0[1] + 1, e0[2] - s0[2] + 1, (int)t, atom};
+                        *maxpts = std::max(*maxpts, (long)im.nx * im.ny * im.nz);
+                        imgs.push_back(im);
+                    }
+                }
+            }
+        }
+    }
+    return SGPU_OK;
+}
+
+// Runs k_pseudocharge over the images into zeroed device arrays b, bref, vc, rho, core (each
+// Nd) and esc_acc (one value).
+static int pseudocharge_fields(sgpu_ctx *ctx, const SetupState &s, const double h[3],
+                               const std::vector<PcImage> &imgs, long maxpts,
+                               double ref_cutoff, double *db, double *dbref, double *dvc,
+                               double *drho, double *dcore, double *esc_acc, cudaStream_t st)
+{
+    if (imgs.empty()) return SGPU_OK;
+    PcImage *dimg = nullptr;
+    SGPU_CUDA_TRY(cudaMallocAsync(&dimg, sizeof(PcImage) * imgs.size(), st));
+    int rc = SGPU_OK;
+    if (cudaMemcpyAsync(dimg, imgs.data(), sizeof(PcImage) * imgs.size(),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        rc = SGPU_ERR_CUDA;
+    } else {
+        PcWeights W{};
+        const double s4 = -0.25 / M_PI;
+        for (int r = 0; r <= ctx->FDn; r++) {
+            W.w[3 * r] = ctx->cx[r] * s4;
+            W.w[3 * r + 1] = ctx->cy[r] * s4;
+            W.w[3 * r + 2] = ctx->cz[r] * s4;
+        }
+        W.w0 = (ctx->cx[0] + ctx->cy[0] + ctx->cz[0]) * s4;
+        // one grid row of blocks per image; images beyond 65535 go in further launches
+        for (size_t i0 = 0; i0 < imgs.size(); i0 += 65535) {
+            const unsigned ny = (unsigned)std::min<size_t>(65535, imgs.size() - i0);
+            dim3 grid((unsigned)((maxpts + 255) / 256), ny);
+            ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+            k_pseudocharge<<<grid, 256, 0, st>>>(dimg + i0, device_views(s), W, ctx->FDn,
+                                                 ctx->Nx, ctx->Ny, h[0], h[1], h[2],
+                                                 ref_cutoff, db, dbref, dvc, drho, dcore,
+                                                 esc_acc);
+        }
+        if (cudaGetLastError() != cudaSuccess) rc = SGPU_ERR_CUDA;
+    }
+    cudaFreeAsync(dimg, st);
+    if (rc != SGPU_OK) set_error("pseudocharge: CUDA error");
+    return rc;
 }
 
 }  // namespace sgpu
@@ -667,87 +885,25 @@ int sgpu_Generate_PseudoChargeDensity(sgpu_ctx *ctx, const double *cell, const i
     cudaStream_t st = ctx->stream;
     double h[3];
     grid_spacing(ctx, cell, h);
-    const int N[3] = {ctx->Nx, ctx->Ny, ctx->Nz};
     // images of every atom whose rb-box meets the cell (GetInfluencingAtoms)
     std::vector<PcImage> imgs;
     long maxpts = 0;
-    int atom = 0;
-    for (size_t t = 0; t < s->types.size(); t++) {
-        double rb[3];
-        for (int d = 0; d < 3; d++) {
-            rb[d] = cutoff ? cutoff[3 * t + d] : s->types[t].cutoff[d];
-            if (!(rb[d] > 0)) {
-                set_error("sgpu_Generate_PseudoChargeDensity: no cut-off for type " +
-                          std::to_string(t) + " (call sgpu_Calculate_PseudochargeCutoff)");
-                return SGPU_ERR_STATE;
-            }
-        }
-        for (int a = 0; a < nAtomv[t]; a++, atom++) {
-            const double *p0 = atom_pos + 3 * atom;
-            int lo[3], hi[3];
-            for (int d = 0; d < 3; d++) image_range(p0[d], cell[d], rb[d], &lo[d], &hi[d]);
-            for (int rr = lo[2]; rr <= hi[2]; rr++) {
-                const double z = p0[2] + cell[2] * rr;
-                if (z < -rb[2] || z >= N[2] * h[2] + rb[2]) continue;
-                for (int qq = lo[1]; qq <= hi[1]; qq++) {
-                    const double y = p0[1] + cell[1] * qq;
-                    if (y < -rb[1] || y >= N[1] * h[1] + rb[1]) continue;
-                    for (int pp = lo[0]; pp <= hi[0]; pp++) {
-                        const double x = p0[0] + cell[0] * pp;
-                        if (x < -rb[0] || x >= N[0] * h[0] + rb[0]) continue;
-                        const double c[3] = {x, y, z};
-                        int s0[3], e0[3];
-                        for (int d = 0; d < 3; d++) {
-                            s0[d] = std::max(0, (int)std::ceil((c[d] - rb[d]) / h[d]));
-                            e0[d] = std::min(N[d] - 1, (int)std::floor((c[d] + rb[d]) / h[d]));
-                        }
-                        if (e0[0] < s0[0] || e0[1] < s0[1] || e0[2] < s0[2]) continue;
-                        PcImage im{x, y, z, s0[0], s0[1], s0[2], e0[0] - s0[0] + 1,
-                                   e0[1] - s0[1] + 1, e0[2] - s0[2] + 1, (int)t};
-                        maxpts = std::max(maxpts, (long)im.nx * im.ny * im.nz);
-                        imgs.push_back(im);
-                    }
-                }
-            }
-        }
-    }
+    SGPU_TRY(pc_images(ctx, *s, cell, h, nAtomv, atom_pos, cutoff,
+                       "sgpu_Generate_PseudoChargeDensity", imgs, &maxpts));
     const long Nd = ctx->Nd;
     // device buffers: b, bref, vc, rho, core, sums(4)
     double *buf = nullptr;
     SGPU_CUDA_TRY(cudaMallocAsync(&buf, sizeof(double) * (5 * Nd + 8), st));
     double *db = buf, *dbref = buf + Nd, *dvc = buf + 2 * Nd, *drho = buf + 3 * Nd,
            *dcore = buf + 4 * Nd, *sums = buf + 5 * Nd;
-    PcImage *dimg = nullptr;
     int rc = SGPU_OK;
     do {
         if (cudaMemsetAsync(buf, 0, sizeof(double) * (5 * Nd + 8), st) != cudaSuccess) {
             rc = SGPU_ERR_CUDA; break;
         }
-        if (!imgs.empty()) {
-            if (cudaMallocAsync(&dimg, sizeof(PcImage) * imgs.size(), st) != cudaSuccess ||
-                cudaMemcpyAsync(dimg, imgs.data(), sizeof(PcImage) * imgs.size(),
-                                cudaMemcpyHostToDevice, st) != cudaSuccess) {
-                rc = SGPU_ERR_CUDA; break;
-            }
-            PcWeights W{};
-            const double s4 = -0.25 / M_PI;
-            for (int r = 0; r <= ctx->FDn; r++) {
-                W.w[3 * r] = ctx->cx[r] * s4;
-                W.w[3 * r + 1] = ctx->cy[r] * s4;
-                W.w[3 * r + 2] = ctx->cz[r] * s4;
-            }
-            W.w0 = (ctx->cx[0] + ctx->cy[0] + ctx->cz[0]) * s4;
-            // one grid row of blocks per image; images beyond 65535 go in further launches
-            for (size_t i0 = 0; i0 < imgs.size(); i0 += 65535) {
-                const unsigned ny = (unsigned)std::min<size_t>(65535, imgs.size() - i0);
-                dim3 grid((unsigned)((maxpts + 255) / 256), ny);
-                ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
-                k_pseudocharge<<<grid, 256, 0, st>>>(dimg + i0, device_views(*s), W, ctx->FDn,
-                                                     ctx->Nx, ctx->Ny, h[0], h[1], h[2],
-                                                     ref_cutoff, db, dbref, dvc, drho, dcore,
-                                                     sums + 3);
-            }
-        }
+        if ((rc = pseudocharge_fields(ctx, *s, h, imgs, maxpts, ref_cutoff, db, dbref, dvc,
+                                      drho, dcore, sums + 3, st)) != SGPU_OK)
+            break;
         {
             ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
             k_charge_sums<<<2 * 152, 256, 0, st>>>(db, dbref, dvc, drho, Nd, sums);
@@ -776,12 +932,172 @@ int sgpu_Generate_PseudoChargeDensity(sgpu_ctx *ctx, const double *cell, const i
         if ((rc = deliver(dcore, rho_core, Nd, st)) != SGPU_OK) break;
     } while (0);
     if (rc != SGPU_OK && rc == SGPU_ERR_CUDA) set_error("sgpu_Generate_PseudoChargeDensity: CUDA error");
-    if (dimg) cudaFreeAsync(dimg, st);
     cudaFreeAsync(buf, st);
     if (cudaStreamSynchronize(st) != cudaSuccess && rc == SGPU_OK) {
         set_error("sgpu_Generate_PseudoChargeDensity: CUDA error");
         rc = SGPU_ERR_CUDA;
     }
+    return rc;
+}
+
+// shared by the force entry points: the images of the atoms' rb-boxes on the device
+struct ForceImages {
+    std::vector<PcImage> imgs;
+    long maxpts = 0;
+    int n_atom = 0;
+    double h[3];
+};
+
+static int force_images(sgpu_ctx *ctx, SetupState *s, const double *cell, const int *nAtomv,
+                        const double *atom_pos, const double *cutoff, const char *who,
+                        ForceImages *fi)
+{
+    grid_spacing(ctx, cell, fi->h);
+    fi->n_atom = 0;
+    for (size_t t = 0; t < s->types.size(); t++) fi->n_atom += nAtomv[t];
+    return pc_images(ctx, *s, cell, fi->h, nAtomv, atom_pos, cutoff, who, fi->imgs, &fi->maxpts);
+}
+
+static D1Weights d1_weights(const sgpu_ctx *ctx, const double h[3])
+{
+    D1Weights G{};
+    for (int r = 1; r <= ctx->FDn; r++) {  // w1[r] = w2[r] r / 2, so D1 = D2 * h * r / 2
+        G.d[3 * r] = ctx->cx[r] * h[0] * r * 0.5;
+        G.d[3 * r + 1] = ctx->cy[r] * h[1] * r * 0.5;
+        G.d[3 * r + 2] = ctx->cz[r] * h[2] * r * 0.5;
+    }
+    return G;
+}
+
+int sgpu_Calculate_local_forces(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                                const double *atom_pos, const double *cutoff, double ref_cutoff,
+                                const double *phi, double *forces)
+{
+    if (!ctx || !cell || !nAtomv || !atom_pos || !(ref_cutoff > 0) || !phi || !forces) {
+        set_error("sgpu_Calculate_local_forces: bad arguments");
+        return SGPU_ERR_ARG;
+    }
+    SetupState *s;
+    SGPU_TRY(get_setup(ctx, &s));
+    SGPU_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    ForceImages fi;
+    SGPU_TRY(force_images(ctx, s, cell, nAtomv, atom_pos, cutoff, "sgpu_Calculate_local_forces",
+                          &fi));
+    const long Nd = ctx->Nd;
+    // b, bref, vc, rho, core, esc sums (8), grad phi (3 Nd), grad Vc (3 Nd), phi, forces
+    const size_t nbuf = 5 * Nd + 8 + 6 * Nd + Nd + 3 * (size_t)fi.n_atom;
+    double *buf = nullptr;
+    SGPU_CUDA_TRY(cudaMallocAsync(&buf, sizeof(double) * nbuf, st));
+    double *db = buf, *dbref = buf + Nd, *dvc = buf + 2 * Nd, *drho = buf + 3 * Nd,
+           *dcore = buf + 4 * Nd, *sums = buf + 5 * Nd, *gphi = sums + 8, *gvc = gphi + 3 * Nd,
+           *dphi = gvc + 3 * Nd, *dF = dphi + Nd;
+    PcImage *dimg = nullptr;
+    int rc = SGPU_OK;
+    do {
+        if (cudaMemsetAsync(buf, 0, sizeof(double) * nbuf, st) != cudaSuccess ||
+            cudaMemcpyAsync(dphi, phi, sizeof(double) * Nd, cudaMemcpyDefault, st) != cudaSuccess) {
+            rc = SGPU_ERR_CUDA; break;
+        }
+        if ((rc = pseudocharge_fields(ctx, *s, fi.h, fi.imgs, fi.maxpts, ref_cutoff, db, dbref,
+                                      dvc, drho, dcore, sums, st)) != SGPU_OK)
+            break;
+        const D1Weights G = d1_weights(ctx, fi.h);
+        for (int d = 0; d < 3 && rc == SGPU_OK; d++) {
+            double w[kMaxFDn + 1];
+            for (int r = 0; r <= ctx->FDn; r++) w[r] = G.d[3 * r + d];
+            rc = launch_gradient(ctx, 1, dphi, Nd, gphi + d * Nd, Nd, d, w, st);
+            if (rc == SGPU_OK) rc = launch_gradient(ctx, 1, dvc, Nd, gvc + d * Nd, Nd, d, w, st);
+        }
+        if (rc != SGPU_OK) break;
+        if (!fi.imgs.empty()) {
+            if (cudaMallocAsync(&dimg, sizeof(PcImage) * fi.imgs.size(), st) != cudaSuccess ||
+                cudaMemcpyAsync(dimg, fi.imgs.data(), sizeof(PcImage) * fi.imgs.size(),
+                                cudaMemcpyHostToDevice, st) != cudaSuccess) {
+                rc = SGPU_ERR_CUDA; break;
+            }
+            PcWeights W{};
+            const double s4 = -0.25 / M_PI;
+            for (int r = 0; r <= ctx->FDn; r++) {
+                W.w[3 * r] = ctx->cx[r] * s4;
+                W.w[3 * r + 1] = ctx->cy[r] * s4;
+                W.w[3 * r + 2] = ctx->cz[r] * s4;
+            }
+            W.w0 = (ctx->cx[0] + ctx->cy[0] + ctx->cz[0]) * s4;
+            for (size_t i0 = 0; i0 < fi.imgs.size(); i0 += 65535) {
+                const unsigned ny = (unsigned)std::min<size_t>(65535, fi.imgs.size() - i0);
+                dim3 grid((unsigned)((fi.maxpts + 255) / 256), ny);
+                ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+                k_local_forces<<<grid, 256, 0, st>>>(dimg + i0, device_views(*s), W, G, ctx->FDn,
+                                                     ctx->Nx, ctx->Ny, fi.h[0], fi.h[1], fi.h[2],
+                                                     ref_cutoff, db, dbref, gphi, gvc, Nd,
+                                                     ctx->dV, dF);
+            }
+            if (cudaGetLastError() != cudaSuccess) { rc = SGPU_ERR_CUDA; break; }
+        }
+        if (cudaMemcpyAsync(forces, dF, sizeof(double) * 3 * fi.n_atom, cudaMemcpyDefault,
+                            st) != cudaSuccess)
+            rc = SGPU_ERR_CUDA;
+    } while (0);
+    if (dimg) cudaFreeAsync(dimg, st);
+    cudaFreeAsync(buf, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == SGPU_OK) rc = SGPU_ERR_CUDA;
+    if (rc == SGPU_ERR_CUDA) set_error("sgpu_Calculate_local_forces: CUDA error");
+    return rc;
+}
+
+int sgpu_Calculate_forces_xc(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                             const double *atom_pos, const double *cutoff, const double *Vxc,
+                             double *forces_xc)
+{
+    if (!ctx || !cell || !nAtomv || !atom_pos || !Vxc || !forces_xc) {
+        set_error("sgpu_Calculate_forces_xc: bad arguments");
+        return SGPU_ERR_ARG;
+    }
+    SetupState *s;
+    SGPU_TRY(get_setup(ctx, &s));
+    SGPU_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    ForceImages fi;
+    SGPU_TRY(force_images(ctx, s, cell, nAtomv, atom_pos, cutoff, "sgpu_Calculate_forces_xc",
+                          &fi));
+    const long Nd = ctx->Nd;
+    double *buf = nullptr;
+    const size_t nbuf = Nd + 3 * (size_t)fi.n_atom;
+    SGPU_CUDA_TRY(cudaMallocAsync(&buf, sizeof(double) * nbuf, st));
+    double *dvxc = buf, *dF = buf + Nd;
+    PcImage *dimg = nullptr;
+    int rc = SGPU_OK;
+    do {
+        if (cudaMemsetAsync(dF, 0, sizeof(double) * 3 * fi.n_atom, st) != cudaSuccess ||
+            cudaMemcpyAsync(dvxc, Vxc, sizeof(double) * Nd, cudaMemcpyDefault, st) != cudaSuccess) {
+            rc = SGPU_ERR_CUDA; break;
+        }
+        if (!fi.imgs.empty()) {
+            if (cudaMallocAsync(&dimg, sizeof(PcImage) * fi.imgs.size(), st) != cudaSuccess ||
+                cudaMemcpyAsync(dimg, fi.imgs.data(), sizeof(PcImage) * fi.imgs.size(),
+                                cudaMemcpyHostToDevice, st) != cudaSuccess) {
+                rc = SGPU_ERR_CUDA; break;
+            }
+            const D1Weights G = d1_weights(ctx, fi.h);
+            for (size_t i0 = 0; i0 < fi.imgs.size(); i0 += 65535) {
+                const unsigned ny = (unsigned)std::min<size_t>(65535, fi.imgs.size() - i0);
+                dim3 grid((unsigned)((fi.maxpts + 255) / 256), ny);
+                ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+                k_xc_forces<<<grid, 256, 0, st>>>(dimg + i0, device_views(*s), G, ctx->FDn, ctx->Nx,
+                                                  ctx->Ny, fi.h[0], fi.h[1], fi.h[2], dvxc,
+                                                  ctx->dV, dF);
+            }
+            if (cudaGetLastError() != cudaSuccess) { rc = SGPU_ERR_CUDA; break; }
+        }
+        if (cudaMemcpyAsync(forces_xc, dF, sizeof(double) * 3 * fi.n_atom, cudaMemcpyDefault,
+                            st) != cudaSuccess)
+            rc = SGPU_ERR_CUDA;
+    } while (0);
+    if (dimg) cudaFreeAsync(dimg, st);
+    cudaFreeAsync(buf, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == SGPU_OK) rc = SGPU_ERR_CUDA;
+    if (rc == SGPU_ERR_CUDA) set_error("sgpu_Calculate_forces_xc: CUDA error");
     return rc;
 }
 

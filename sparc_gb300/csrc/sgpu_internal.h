@@ -206,6 +206,15 @@ long nonlocal_alpha_ld(int ncol, int elem_bytes);
 template <typename T>
 int launch_nonlocal_project(sgpu_ctx *ctx, int ncol, const T *x, long ldx, T *alpha, long lda,
                             cudaStream_t st);
+// alpha += Chi^T x (no dV, no Gamma: ones holds ntot ones), the segment kernel in FP64
+int launch_nonlocal_project_plain(sgpu_ctx *ctx, int ncol, const double *x, long ldx,
+                                  double *alpha, long lda, const double *ones, cudaStream_t st);
+
+// ---- forces (forces.cu)
+// out[:, n] = D1 derivative of x[:, n] along dir (0 x, 1 y, 2 z), periodic; w[1..FDn] are the
+// first-derivative weights of that direction (w[0] unused)
+int launch_gradient(sgpu_ctx *ctx, int ncol, const double *x, long ldx, double *out, long ldo,
+                    int dir, const double *w, cudaStream_t st);
 template <typename T>
 int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, double scale,
                           T *out, long ldo, cudaStream_t st);

@@ -123,11 +123,24 @@ class CellSystem:
         p.verbose = verbose
         return p
 
-    def scf(self, params, rho_init=None):
-        """Run the SCF from the superposition of atomic densities (or from rho_init)."""
+    def scf(self, params, rho_init=None, fields=None):
+        """Run the SCF from the superposition of atomic densities (or from rho_init); with
+        fields a dict, also return the final orbitals and potentials there (Context.scf)."""
         f = self.fields
         r0 = f["rho_at"] if rho_init is None else rho_init
-        return self.ctx.scf(params, f["b"], r0, f["rho_core"] if self.nlcc else None)
+        return self.ctx.scf(params, f["b"], r0, f["rho_core"] if self.nlcc else None,
+                            fields=fields)
+
+    def forces(self, fields, occ, occfac=2.0):
+        """Atomic forces (n_atom, 3) in Ha/Bohr after an SCF that filled fields (psi, phi,
+        vxc) and returned occ: local + nonlocal (+ core correction) with the mean removed, as
+        Calculate_EGS_Forces (src/forces.c:49) assembles them."""
+        F = self.ctx.Calculate_local_forces(self.L, self.nAtomv, self.atom_pos, fields["phi"],
+                                            ref_cutoff=self.ref_cutoff)
+        F = F + self.ctx.Calculate_nonlocal_forces(self.L, fields["psi"], occ, occfac)
+        if self.nlcc:
+            F = F + self.ctx.Calculate_forces_xc(self.L, self.nAtomv, self.atom_pos, fields["vxc"])
+        return F - F.mean(axis=0)
 
     def close(self):
         self.ctx.close()

@@ -104,9 +104,43 @@ def test_scf_from_own_setup_matches_reference_program(gpu_available, precision):
     cs = CellSystem(sysd["L"], N, sysd["species"], {"Si": load_tables(
         os.path.join(GOLDEN, "psp_Si.npz"))})
     prm = cs.scf_params(Nstates=32, cheb_degree=20, precision=precision)
-    res, rho, lam, occ = cs.scf(prm)
+    fields = {}
+    res, rho, lam, occ = cs.scf(prm, fields=fields)
     assert res["converged"] == 1
     assert abs(res["Etot"] / cs.n_atom - ref["Etot_per_atom"]) < 1e-5
     occupied = np.array(ref["occ"]) > 1e-3
     assert np.abs(lam[occupied] - np.array(ref["lambda"])[occupied]).max() < 1e-5
     assert abs(res["Esc"] - ref["Esc"]) < 1e-6
+    # forces (local + nonlocal + core correction, mean removed) within 1e-4 Ha/Bohr of the
+    # reference program's
+    F = cs.forces(fields, occ)
+    Fref = np.array(ref["forces"])
+    assert F.shape == Fref.shape
+    assert np.abs(F - Fref).max() < 1e-4, np.abs(F - Fref).max()
+
+
+def test_gradient_of_periodic_functions(gpu_available):
+    """sgpu_Gradient_vectors_dir (order-12 FD, periodic) against analytic derivatives of
+    resolved periodic functions, in each direction and for a non-cubic cell."""
+    from sparc_gb300.synthetic import fd_d2_coeffs
+    N = (24, 20, 28)
+    L = (7.3, 6.1, 8.9)
+    h = [L[d] / N[d] for d in range(3)]
+    ctx = sg.Context(N[0], N[1], N[2], 6, fd_d2_coeffs(6, h[0]), fd_d2_coeffs(6, h[1]),
+                     fd_d2_coeffs(6, h[2]), h[0] * h[1] * h[2])
+    x = np.arange(N[0]) * h[0]
+    y = np.arange(N[1]) * h[1]
+    z = np.arange(N[2]) * h[2]
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    k = [2 * np.pi / L[d] for d in range(3)]
+    f = np.sin(k[0] * X + 0.3) * np.cos(2 * k[1] * Y) * np.sin(k[2] * Z + 1.1)
+    dfs = [k[0] * np.cos(k[0] * X + 0.3) * np.cos(2 * k[1] * Y) * np.sin(k[2] * Z + 1.1),
+           -2 * k[1] * np.sin(k[0] * X + 0.3) * np.sin(2 * k[1] * Y) * np.sin(k[2] * Z + 1.1),
+           k[2] * np.sin(k[0] * X + 0.3) * np.cos(2 * k[1] * Y) * np.cos(k[2] * Z + 1.1)]
+    f2 = np.stack([f.reshape(-1), 2 * f.reshape(-1)])
+    for d in range(3):
+        out = np.zeros_like(f2)
+        ctx.Gradient_vectors_dir(L, f2, out, d)
+        ref = dfs[d].reshape(-1)
+        assert np.abs(out[0] - ref).max() < 1e-6 * np.abs(ref).max(), d
+        np.testing.assert_allclose(out[1], 2 * out[0], rtol=0, atol=1e-13)
