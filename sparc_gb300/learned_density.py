@@ -153,6 +153,18 @@ def initial_density(torch, cs, net, dev):
     return rho
 
 
+def write_density_cube(cs, rho, path, title="Electron density"):
+    """Write a density of the CellSystem's current geometry as a cube file that SPARC reads
+    with INPUT_DENS_FILE: <path> and READ_INIT_DENS: 1 (sparc_gb300/cube.py)."""
+    from .cube import write_cube
+    atoms, a = [], 0
+    for t, n in zip(cs.tables, cs.nAtomv):
+        for _ in range(int(n)):
+            atoms.append((int(t["Zatom"]), float(t["Znucl"]), tuple(cs.atom_pos[a])))
+            a += 1
+    write_cube(path, rho, cs.N, cs.L, atoms, title=title)
+
+
 def scf_settings(cs, precision, Nstates=160, cheb_degree=20, rho_trigger=4):
     """SCF parameters of the data generation and the evaluation; rho_trigger is the number of
     filter passes of the first SCF iteration (the reference's rhoTrigger, default 4)."""
@@ -294,6 +306,10 @@ def main():
                     help="held-out snapshots per evaluation mode (default: all)")
     ap.add_argument("--rho-triggers", default="4",
                     help="filter passes of the first SCF iteration to evaluate (comma list)")
+    ap.add_argument("--cube", default=None,
+                    help="with --load: write the learned initial density of snapshot "
+                         "--cube-snapshot as a cube file for SPARC's INPUT_DENS_FILE, and stop")
+    ap.add_argument("--cube-snapshot", type=int, default=0)
     args = ap.parse_args()
     import torch
     from .psp8 import load_tables
@@ -310,6 +326,14 @@ def main():
         train_snapshots=ntrain, test_snapshots=args.test, train_points=ntrain * 52 ** 3)
     if args.load:
         net = DensityMLP.load(args.load)
+        if args.cube:
+            L, pos, _, _ = si64_snapshot(args.cube_snapshot)
+            cs.set_geometry((L, L, L), [("Si", pos)])
+            rho0 = initial_density(torch, cs, net, dev)
+            write_density_cube(cs, rho0, args.cube, title="Learned initial density")
+            print(json.dumps(dict(cube=args.cube, snapshot=args.cube_snapshot,
+                                  electrons=float(rho0.sum() * cs.dV))))
+            return
     else:
         t0 = time.perf_counter()
         descs, targs, info = generate(torch, cs, list(range(ntrain)), dev, args.precision,

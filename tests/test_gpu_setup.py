@@ -144,3 +144,19 @@ def test_gradient_of_periodic_functions(gpu_available):
         ref = dfs[d].reshape(-1)
         assert np.abs(out[0] - ref).max() < 1e-6 * np.abs(ref).max(), d
         np.testing.assert_allclose(out[1], 2 * out[0], rtol=0, atol=1e-13)
+
+
+def test_density_cube_from_cell_system(gpu_available, tmp_path):
+    """The cube bridge on a device set-up: rho_at of Si8 written with its atoms and read back."""
+    from sparc_gb300.cube import read_cube
+    from sparc_gb300.learned_density import write_density_cube
+    sysd = systems.si8_c1()
+    cs = CellSystem(sysd["L"], (26, 26, 26), sysd["species"], {"Si": load_tables(
+        os.path.join(GOLDEN, "psp_Si.npz"))})
+    path = str(tmp_path / "rho_at.cube")
+    write_density_cube(cs, cs.fields["rho_at"], path)
+    rho, N, steps, atoms = read_cube(path)
+    assert N == (26, 26, 26) and len(atoms) == cs.n_atom
+    assert all(a[0] == 14 and a[1] == 4.0 for a in atoms)
+    np.testing.assert_allclose(rho, cs.fields["rho_at"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(rho.sum() * cs.dV, cs.Nelectron, rtol=1e-9)
