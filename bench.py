@@ -186,6 +186,29 @@ def scf_block(sg, device=0, repeats=2):
                      "fp64_switch_iter": res["fp64_switch_iter"]}
     out["speedup_mixed_vs_fp64"] = round(out["fp64"]["time_s"] / out["mixed"]["time_s"], 3)
     ctx.close()
+    # forces on the device from the library's own set-up (psp8 tables -> pseudocharges,
+    # projectors -> SCF -> local + nonlocal + core-correction forces), against the reference
+    # program's forces of the same input
+    golden = os.path.join(ROOT, "tests", "golden")
+    sys.path.insert(0, golden)
+    import systems
+    from sparc_gb300.psp8 import load_tables
+    from sparc_gb300.setup import CellSystem
+    sysd = systems.si8_c1()
+    cs = CellSystem(sysd["L"], (26, 26, 26), sysd["species"],
+                    {"Si": load_tables(os.path.join(golden, "psp_Si.npz"))}, device=device)
+    Fref = np.array(ref["forces"])
+    for name, prec in (("fp64", 64), ("mixed", 32)):
+        fields = {}
+        res, rho, lam, occ = cs.scf(cs.scf_params(Nstates=32, cheb_degree=20, precision=prec),
+                                    fields=fields)
+        t0 = time.perf_counter()
+        F = cs.forces(fields, occ)
+        tf = time.perf_counter() - t0
+        out[f"forces_{name}"] = {"max_abs_err_vs_ref_Ha_per_Bohr": float(np.abs(F - Fref).max()),
+                                 "max_abs_force": float(np.abs(Fref).max()),
+                                 "time_s": round(tf, 4)}
+    cs.close()
     return out
 
 
@@ -239,7 +262,7 @@ def scf_c4_block(sg, torch=None, device=0):
     # one untimed SCF iteration in each precision first: library handles, workspaces, module
     # loading and the FP32 kernel tuning are paid there, not by the first timed run
     for kw in (dict(precision=64), mixed):
-        cs.scf(cs.scf_params(Nstates=520, cheb_degree=24, maxit_scf=1, **kw))
+        cs.scf(cs.scf_params(Nstates=520, cheb_degree=24, maxit_scf=1, **kw), fields={})
     e64 = None
     for name, (kw, rt, learned) in runs.items():
         prm = cs.scf_params(Nstates=520, cheb_degree=24, **kw)
@@ -252,7 +275,12 @@ def scf_c4_block(sg, torch=None, device=0):
             tp = time.perf_counter()
             rho0 = initial_density(torch, cs, net, dev)
             t_pred = time.perf_counter() - tp
-        res, rho, lam, occ = cs.scf(prm, rho_init=rho0)
+        fields = {}
+        res, rho, lam, occ = cs.scf(prm, rho_init=rho0, fields=fields)
+        tf = time.perf_counter()
+        F = cs.forces(fields, occ)  # after the timed SCF: forces are reported, not timed in it
+        tf = time.perf_counter() - tf
+        del fields
         e = res["Etot"] / cs.n_atom
         e_target = ref["Etot_per_atom"] if ref else (e64 if e64 is not None else e)
         it, ts = energy_reached(res["history"], e_target, cs.n_atom, 1e-5)
@@ -264,12 +292,15 @@ def scf_c4_block(sg, torch=None, device=0):
                "time_to_1e-5_Ha_per_atom_s": None if ts is None else round(ts + t_pred, 3)}
         if learned:
             rec["predict_s"] = round(t_pred, 3)
+        rec["forces_time_s"] = round(tf, 3)
         if name == "fp64":
-            e64, lam64 = e, lam
+            e64, lam64, F64 = e, lam, F
+            rec["max_abs_force"] = float(np.abs(F).max())
         else:
             rec["dE_per_atom_vs_fp64_gpu"] = abs(e - e64)
             occd = occ > 1e-3
             rec["max_occ_eig_diff_vs_fp64_gpu"] = float(np.abs(lam[occd] - lam64[occd]).max())
+            rec["max_force_diff_vs_fp64_gpu"] = float(np.abs(F - F64).max())
         if ref:
             rec["dE_per_atom_vs_ref"] = abs(e - ref["Etot_per_atom"])
             lr, orr = np.array(ref["lambda"]), np.array(ref["occ"])

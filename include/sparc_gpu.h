@@ -351,7 +351,7 @@ typedef struct {
 typedef struct {
     int scf_iters, converged, fp64_switch_iter;
     double Etot, Eband, E1, E2, E3, Exc, Esc, Entropy, Efermi, scf_error;
-    double time_s;              /* wall time of the call */
+    double time_s;              /* wall time of the SCF (without the optional field outputs) */
     double filter_ms;           /* device time of filter + projection products */
 } sgpu_scf_result;
 
