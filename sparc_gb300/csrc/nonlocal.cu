@@ -140,6 +140,34 @@ __global__ void __launch_bounds__(kProjThreads)
     }
 }
 
+// Gathers the tile src[gps[lp], n0 + c] (lp < npt, c < NC, column n0 + c < ncol; zero
+// elsewhere) into dst[lp * LD + c] with 4-byte cp.async copies, all of a thread's copies in
+// flight together; returns once the tile is complete for this thread (the caller's barrier
+// makes it complete for the block). 256 threads.
+template <int LD, int NC>
+__device__ __forceinline__ void gather_tile(const float *__restrict__ src, long lds, int n0,
+                                            int ncol, const int *__restrict__ gps, int npt,
+                                            float *__restrict__ dst)
+{
+    static_assert(kRangePts * NC % 256 == 0, "whole copies per thread");
+#pragma unroll 8
+    for (int u = 0; u < kRangePts * NC / 256; u++) {
+        const int idx = threadIdx.x + u * 256;
+        const int lp = idx % kRangePts, c = idx / kRangePts;
+        float *d = dst + lp * LD + c;
+        if (lp < npt && n0 + c < ncol) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(d);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa),
+                         "l"(src + (long)(n0 + c) * lds + gps[lp])
+                         : "memory");
+        } else {
+            *d = 0.f;
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Range projection (FP32): block = one range of at most kRangePts consecutive covered points
 // (grid order). The range's entries, regrouped by image into work items, have their Chi rows
 // (range_jp values each) and point indices staged in shared memory once. For each group of
@@ -159,7 +187,6 @@ __global__ void __launch_bounds__(256)
 {
     constexpr int NC = 64, XLD = NC + 2;             // columns per group, padded x row
     constexpr int MAXJP = (MAXJ + 3) / 4 * 4;        // staged Chi values per entry
-    constexpr int GB = 16;                           // gathers in flight per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *xs = reinterpret_cast<float *>(smem_raw);  // [kRangePts][XLD]
     float *cs = xs + kRangePts * XLD;                 // [entries][MAXJP]
@@ -184,21 +211,7 @@ __global__ void __launch_bounds__(256)
     for (int gi = 0; gi < ngroup; gi++) {
         const int n0 = ((gi + r) % ngroup) * NC;
         __syncthreads();  // staging done / previous group consumed
-        for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
-            float v[GB];
-#pragma unroll
-            for (int u = 0; u < GB; u++) {
-                const int idx = base + t + u * 256;
-                const int lp = idx % kRangePts, c = idx / kRangePts;
-                v[u] = (lp < npt && n0 + c < ncol) ? __ldg(x + (long)(n0 + c) * ldx + gps[lp])
-                                                   : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < GB; u++) {
-                const int idx = base + t + u * 256;
-                xs[(idx % kRangePts) * XLD + idx / kRangePts] = v[u];
-            }
-        }
+        gather_tile<XLD, NC>(x, ldx, n0, ncol, gps, npt, xs);
         __syncthreads();
         for (int it = warp; it < ni; it += 8) {
             const int2 row = item_row[ib + it];  // (first projector row, projector count)
@@ -255,7 +268,6 @@ __global__ void __launch_bounds__(256, 4)
 {
     constexpr int NC = 64, OLD = NC + 1;             // columns per group, padded tile row
     constexpr int MAXJP = (MAXJ + 3) / 4 * 4;
-    constexpr int GB = 8;                            // gathers in flight per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *cs = reinterpret_cast<float *>(smem_raw);  // [entries][MAXJP]
     const int r = blockIdx.x;
@@ -278,20 +290,7 @@ __global__ void __launch_bounds__(256, 4)
     for (int gi = 0; gi < ngroup; gi++) {
         const int n0 = ((gi + r) % ngroup) * NC;
         __syncthreads();  // staging done / previous tile written back
-        for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
-            float v[GB];
-#pragma unroll
-            for (int u = 0; u < GB; u++) {
-                const int idx = base + t + u * 256;
-                const int lp = idx % kRangePts, c = idx / kRangePts;
-                v[u] = (lp < npt && n0 + c < ncol) ? out[(long)(n0 + c) * ldo + gps[lp]] : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < GB; u++) {
-                const int idx = base + t + u * 256;
-                os[(idx % kRangePts) * OLD + idx / kRangePts] = v[u];
-            }
-        }
+        gather_tile<OLD, NC>(out, ldo, n0, ncol, gps, npt, os);
         __syncthreads();
         const int ca = n0 + lane, cb = n0 + lane + 32;
         for (int it = warp; it < ni; it += 8) {
@@ -324,13 +323,11 @@ __global__ void __launch_bounds__(256, 4)
             }
         }
         __syncthreads();
-        for (int base = 0; base < kRangePts * NC; base += 256 * GB) {
-#pragma unroll
-            for (int u = 0; u < GB; u++) {
-                const int idx = base + t + u * 256;
-                const int lp = idx % kRangePts, c = idx / kRangePts;
-                if (lp < npt && n0 + c < ncol) out[(long)(n0 + c) * ldo + gps[lp]] = os[lp * OLD + c];
-            }
+#pragma unroll 8
+        for (int u = 0; u < kRangePts * NC / 256; u++) {
+            const int idx = t + u * 256;
+            const int lp = idx % kRangePts, c = idx / kRangePts;
+            if (lp < npt && n0 + c < ncol) out[(long)(n0 + c) * ldo + gps[lp]] = os[lp * OLD + c];
         }
     }
 }
