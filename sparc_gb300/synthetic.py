@@ -49,7 +49,8 @@ def gaussian_potential(rng, N, h, ncenters=64, amp=-2.0, width=1.5):
 
 
 def real_ylm(l, dx, dy, dz, r):
-    """Real spherical harmonics for l <= 2, in the order m = -l..l (unit-normalised)."""
+    """Real spherical harmonics for l <= 3, in the order m = -l..l (unit-normalised): 2l+1
+    functions."""
     rs = np.where(r > 1e-12, r, 1.0)
     X, Y, Z = dx / rs, dy / rs, dz / rs
     if l == 0:
@@ -57,10 +58,21 @@ def real_ylm(l, dx, dy, dz, r):
     if l == 1:
         c = math.sqrt(3.0 / (4.0 * math.pi))
         return [c * Y, c * Z, c * X]
-    c1 = 0.5 * math.sqrt(15.0 / math.pi)
-    c2 = 0.25 * math.sqrt(5.0 / math.pi)
-    c3 = 0.25 * math.sqrt(15.0 / math.pi)
-    return [c1 * X * Y, c1 * Y * Z, c2 * (3 * Z * Z - 1), c1 * X * Z, c3 * (X * X - Y * Y)]
+    if l == 2:
+        c1 = 0.5 * math.sqrt(15.0 / math.pi)
+        c2 = 0.25 * math.sqrt(5.0 / math.pi)
+        c3 = 0.25 * math.sqrt(15.0 / math.pi)
+        return [c1 * X * Y, c1 * Y * Z, c2 * (3 * Z * Z - 1), c1 * X * Z, c3 * (X * X - Y * Y)]
+    if l == 3:
+        a = 0.25 * math.sqrt(35.0 / (2.0 * math.pi))
+        b = 0.5 * math.sqrt(105.0 / math.pi)
+        c = 0.25 * math.sqrt(21.0 / (2.0 * math.pi))
+        d = 0.25 * math.sqrt(7.0 / math.pi)
+        e = 0.25 * math.sqrt(105.0 / math.pi)
+        return [a * (3 * X * X - Y * Y) * Y, b * X * Y * Z, c * Y * (5 * Z * Z - 1),
+                d * Z * (5 * Z * Z - 3), c * X * (5 * Z * Z - 1), e * (X * X - Y * Y) * Z,
+                a * (X * X - 3 * Y * Y) * X]
+    raise ValueError("real_ylm: l <= 3 only")
 
 
 def synthetic_nonlocal(rng, N, h, natom=64, rc=6.0, lmax=2):

@@ -47,3 +47,21 @@ def test_oracle_detects_planted_error():
     cx[3] *= 1.0 + 1e-9
     o = Oracle(dict(grid, cx=cx), nl)
     assert rel_err(o.lap_plus_diag(1.0, 0.0, 0.0, None, d["x"][:1]), d["lap"]) > 1e-12
+
+
+@pytest.mark.parametrize("lmax", [0, 1, 2, 3])
+def test_synthetic_projector_sets_are_consistent(lmax):
+    """The synthetic nonlocal sets used by the kernel tests hold exactly sum(ndc) x nproj Chi
+    values and in-range grid positions (the kernels and the oracle read them as such)."""
+    import numpy as np
+    from sparc_gb300.synthetic import synthetic_nonlocal
+    rng = np.random.default_rng(lmax)
+    N = (20, 18, 16)
+    nl = synthetic_nonlocal(rng, N, 0.4, natom=5, rc=2.0, lmax=lmax)
+    nproj = (lmax + 1) ** 2
+    assert np.all(np.diff(nl["ip_displ"]) == nproj)
+    assert len(nl["gamma"]) == 5 * nproj
+    assert len(nl["chi"]) == int(np.sum(nl["img_ndc"])) * nproj
+    assert len(nl["grid_pos"]) == int(np.sum(nl["img_ndc"]))
+    assert nl["grid_pos"].min() >= 0 and nl["grid_pos"].max() < np.prod(N)
+    assert np.all(np.isfinite(nl["chi"]))
