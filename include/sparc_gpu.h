@@ -459,8 +459,8 @@ int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant);
  * point's Chi values loaded once before the column loop; 3: FP32 only, a dense product per
  * chunk of covered points over the alpha rows of the chunk's atoms; 4: FP32 only, per range of
  * covered points with the output tile in shared memory); sgpu_autotune times all five.
- * Forms 0-2 give identical results; forms 3 and 4 sum in other orders (FP32 rounding; form 4
- * adds the contributions of overlapping spheres in no fixed order). */
+ * Forms 0-2 give identical results; forms 3 and 4 sum in other (fixed) orders, so they agree
+ * with 0-2 to FP32 rounding. */
 int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
 
 /* Fix the form of the FP32 nonlocal projection (0: one block per segment of one image's

@@ -219,6 +219,7 @@ __global__ void __launch_bounds__(256)
             float2 acc[MAXJ];  // (column 2l, column 2l+1) per projector, packed FMAs
 #pragma unroll
             for (int j = 0; j < MAXJ; j++) acc[j] = make_float2(0.f, 0.f);
+#pragma unroll 2
             for (int e = e0; e < e1; e++) {
                 const float2 xv = *reinterpret_cast<const float2 *>(xs + lps[e] * XLD + 2 * lane);
                 const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
@@ -252,15 +253,16 @@ __global__ void __launch_bounds__(256)
 // Range apply (FP32): the projection's ranges and work items run in reverse. Block = one range;
 // for each group of 64 columns (rotated by the range index) it gathers the output tile of its
 // points (os[point][64], one coalesced read of every covered output element), then each warp
-// takes work items in turn: lane l holds scale * alpha[row j, columns l and l+32] of the item's
-// atom in registers and, for every entry of the item, adds sum_j Chi_j alpha_j into the tile
-// with shared-memory atomics (lanes touch distinct columns; two images over one point meet
-// only in the atomics, so the order of those additions is not fixed). The tile is then written
-// back once. Every covered output element is read and written once per launch, in grid order.
+// owns kRangeWarpPts consecutive points of the tile: it walks the work items in order and,
+// for the item's entries on its points (item_wsplit gives their range per warp), lane l holds
+// scale * alpha[row j, columns l and l+32] of the item's atom in registers and adds
+// sum_j Chi_j alpha_j into its tile rows. The tile is then written back once: every covered
+// output element is read and written once per launch, in grid order, and the additions per
+// point run in a fixed order (item order).
 template <int MAXJ>
 __global__ void __launch_bounds__(256, 4)
     k_nl_apply_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
-                     const int *__restrict__ rng_item0, const int *__restrict__ item_e0,
+                     const int *__restrict__ rng_item0, const int *__restrict__ item_wsplit,
                      const int2 *__restrict__ item_row, const int *__restrict__ pe_lp,
                      const float *__restrict__ pe_chi, const int *__restrict__ cov_pt, int ncol,
                      const float *__restrict__ alpha, long lda, float scale,
@@ -293,9 +295,14 @@ __global__ void __launch_bounds__(256, 4)
         gather_tile<OLD, NC>(out, ldo, n0, ncol, gps, npt, os);
         __syncthreads();
         const int ca = n0 + lane, cb = n0 + lane + 32;
-        for (int it = warp; it < ni; it += 8) {
+        // warp w owns the tile rows of points [w * kRangeWarpPts, (w + 1) * kRangeWarpPts):
+        // it walks every item but only the item's entries on its own points, so no two warps
+        // write one tile row and the additions per point run in item order
+        for (int it = 0; it < ni; it++) {
+            const int *ws = item_wsplit + (long)(ib + it) * (kRangeWarps + 1);
+            const int e0 = ws[warp] - eb, e1 = ws[warp + 1] - eb;
+            if (e0 == e1) continue;
             const int2 row = item_row[ib + it];  // (first projector row, projector count)
-            const int e0 = item_e0[ib + it] - eb, e1 = item_e0[ib + it + 1] - eb;
             float2 a[MAXJ];  // scale * alpha of columns (lane, lane + 32)
 #pragma unroll
             for (int j = 0; j < MAXJ; j++) {
@@ -306,7 +313,8 @@ __global__ void __launch_bounds__(256, 4)
                                        cb < ncol ? scale * __ldg(ar + cb) : 0.f);
                 }
             }
-            for (int e = e0; e < e1; e++) {
+#pragma unroll 4
+            for (int e = e0; e < e1; e++) {  // entries are independent: four chains in flight
                 const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
                 float2 s = make_float2(0.f, 0.f);
 #pragma unroll
@@ -318,8 +326,8 @@ __global__ void __launch_bounds__(256, 4)
                         if (q * 4 + w < MAXJ) s = __ffma2_rn(make_float2(ce[w], ce[w]), a[q * 4 + w], s);
                 }
                 float *o = os + lps[e] * OLD;
-                atomicAdd(o + lane, s.x);
-                atomicAdd(o + lane + 32, s.y);
+                o[lane] += s.x;
+                o[lane + 32] += s.y;
             }
         }
         __syncthreads();
@@ -772,7 +780,7 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
         auto kern = k_nl_apply_range<MJ>;                                                    \
         SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                            (int)rsm));                                       \
-        kern<<<nl.nrange, 256, rsm, st>>>(nl.rng_pt0, nl.rng_ent0, nl.rng_item0, nl.item_e0, \
+        kern<<<nl.nrange, 256, rsm, st>>>(nl.rng_pt0, nl.rng_ent0, nl.rng_item0, nl.item_wsplit, \
                                           nl.item_row, nl.pe_lp, nl.pe_chi32, nl.cov_pt,     \
                                           ncol, alpha, lda, (float)scale, out, ldo);         \
     }
@@ -849,6 +857,7 @@ void nonlocal_free(Nonlocal &nl)
                     nl.cov_pt,   nl.cov_ptr,  nl.ent_chi, nl.ent_meta, nl.seg_img,
                     nl.seg_start, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows,
                     nl.rng_pt0,  nl.rng_ent0, nl.rng_item0, nl.item_e0, nl.item_row,
+                    nl.item_wsplit,
                     nl.pe_lp,    nl.pe_chi32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -959,7 +968,8 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     // range projection: ranges of at most kRangePts consecutive covered points and
     // kRangeMaxEnt entries; within a range the entries are regrouped by image (then by point)
     // into work items of at most kRangeItemEnt entries, with their Chi rows in FP32
-    std::vector<int> rng_pt0(1, 0), rng_ent0(1, 0), rng_item0(1, 0), item_e0(1, 0), pe_lp;
+    std::vector<int> rng_pt0(1, 0), rng_ent0(1, 0), rng_item0(1, 0), item_e0(1, 0), pe_lp,
+        item_wsplit;
     std::vector<int2> item_row;
     std::vector<float> pe_chi;
     {
@@ -998,6 +1008,7 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
                     k1++;
                 const int4 meta = ent_meta[order[k].second];
                 item_row.push_back(make_int2(meta.x, meta.y));
+                const int first = (int)pe_lp.size();
                 for (size_t u = k; u < k1; u++) {
                     const int e = order[u].second;
                     // the local point: entries of point c lie in [covptr[c], covptr[c+1])
@@ -1009,6 +1020,11 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
                         pe_chi.push_back(j < m.y ? (float)chi[ent_chi[e] + (long)j * m.z] : 0.f);
                 }
                 item_e0.push_back((int)pe_lp.size());
+                // the item's entries by owning warp: points ascend within the item
+                for (int w = 0, e = first; w <= kRangeWarps; w++) {
+                    while (e < (int)pe_lp.size() && pe_lp[e] < w * kRangeWarpPts) e++;
+                    item_wsplit.push_back(e);
+                }
                 k = k1;
             }
             rng_pt0.push_back(p);
@@ -1058,6 +1074,7 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(rng_ent0, rng_ent0.data(), rng_ent0.size());
     UP(rng_item0, rng_item0.data(), rng_item0.size());
     UP(item_e0, item_e0.data(), item_e0.size());
+    UP(item_wsplit, item_wsplit.data(), item_wsplit.size());
     UP(item_row, item_row.data(), item_row.size());
     UP(pe_lp, pe_lp.data(), pe_lp.size());
     UP(pe_chi32, pe_chi.data(), pe_chi.size());

@@ -19,6 +19,9 @@ constexpr int kApplyChunkPts = 128;  // covered points per chunk of the staged n
 constexpr int kRangePts = 128;       // covered points per range of the range projection
 constexpr int kRangeMaxEnt = 320;    // entries per range at most (bounds its staged Chi)
 constexpr int kRangeItemEnt = 96;    // entries per work item of the range projection at most
+constexpr int kRangeWarps = 8;       // warps per range block
+constexpr int kRangeWarpPts = kRangePts / kRangeWarps;  // tile rows owned by one warp (apply)
+static_assert(kRangePts % kRangeWarps == 0, "whole tile rows per warp");
 
 // thread-local error text, returned by sgpu_last_error()
 void set_error(const std::string &msg);
@@ -88,6 +91,8 @@ struct Nonlocal {
     int *rng_ent0 = nullptr;    // nrange + 1: first entry (range order) of each range
     int *rng_item0 = nullptr;   // nrange + 1: first work item of each range
     int *item_e0 = nullptr;     // nitem + 1: first entry (range order) of each item
+    int *item_wsplit = nullptr; // nitem x (kRangeWarps + 1): an item's entries split by the
+                                // warp that owns their point (range apply)
     int2 *item_row = nullptr;   // nitem: (first projector row, projector count)
     int *pe_lp = nullptr;       // entries in range order: point index within the range
     float *pe_chi32 = nullptr;  // entries in range order: Chi values, range_jp per entry
