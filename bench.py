@@ -476,7 +476,11 @@ def main():
                    "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
                    "k_stencil_f32_b22<32x16, 3 blocks/SM>",
                    "k_stencil_f32_ring<32x16, 1 plane ahead>",
-                   "k_stencil_f32_ring<32x16, 2 planes ahead, potential from L2>"][variant]
+                   "k_stencil_f32_ring<32x16, 2 planes ahead, potential from L2>",
+                   "k_stencil_f32_bulk<32x16, 2 planes ahead>",
+                   "k_stencil_f32_bulk<32x16, 1 plane ahead>",
+                   "k_stencil_f32_ring<32x32, 1 plane ahead>",
+                   "k_stencil_f32_ring<32x32, 2 planes ahead, potential from L2>"][variant]
 
     gen = torch.Generator(device=dev)
     gen.manual_seed(1234 + rank)
@@ -549,6 +553,27 @@ def main():
             if kernel_name.startswith(ent["prefix"]):
                 traffic = ent["fp32_bytes_per_launch_at_bench"]
                 break
+
+    # --- the stencil's access mix (two FP32 blocks read, one written) as PyTorch's own
+    # elementwise add over blocks of the same size: the bandwidth a plain 2-read/1-write pass
+    # reaches on this GPU, beside the copy peak
+    Zmix = torch.empty_like(X)
+
+    def mix():
+        torch.add(X, Y, alpha=0.5, out=Zmix)
+
+    for _ in range(3):
+        mix()
+    ev_a = torch.cuda.Event(enable_timing=True)
+    ev_b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev_a.record()
+    for _ in range(5):
+        mix()
+    ev_b.record()
+    torch.cuda.synchronize()
+    mix_gbs = 3 * X.numel() * 4 / (ev_a.elapsed_time(ev_b) / 5 / 1e3) / 1e9
+    del Zmix
 
     # --- e2e: drop-in call with FP64 pinned host arrays (FP32 arithmetic inside)
     Xh0 = X0[:, :].double().cpu().pin_memory()
@@ -625,7 +650,9 @@ def main():
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_src,
                          "traffic": traffic,
-                         "stencil_ms_per_launch": round(stencil_launch_ms, 4)},
+                         "stencil_ms_per_launch": round(stencil_launch_ms, 4),
+                         "elementwise_2r1w_gbs": round(mix_gbs, 1),
+                         "frac_of_elementwise_2r1w": round(achieved / mix_gbs, 4)},
             "kernels_per_step_ms": {
                 "stencil": round(st_ms / nsteps_prof, 3),
                 "nl_project": round(pj_ms / nsteps_prof, 3),

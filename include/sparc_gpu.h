@@ -34,7 +34,9 @@ enum {
     SGPU_ERR_STATE = 4,         /* a required sgpu_set_* call has not been made */
     SGPU_ERR_NOT_CONVERGED = 5, /* an iterative solver hit its iteration cap */
     SGPU_ERR_LINALG = 6,        /* factorisation / eigensolver failure (non-SPD, no conv.) */
-    SGPU_ERR_NONFINITE = 7      /* NaN or Inf detected in an input or a result */
+    SGPU_ERR_NONFINITE = 7,     /* NaN or Inf detected in an input or a result */
+    SGPU_ERR_KERNEL_WAIT = 8    /* a kernel's bounded wait on its own copies ran out: the
+                                 * results of the calls since the last check are invalid */
 };
 
 /* precision of the Chebyshev filter arithmetic */
@@ -407,6 +409,19 @@ int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms);
  * a caller can order its own work or record timing events against it. */
 int sgpu_get_stream(sgpu_ctx *ctx, void **stream);
 
+/* Read and clear the context's kernel status word (synchronises the stream). Kernels that
+ * wait on barriers for their own asynchronous copies give every wait a time limit; a wait
+ * that runs out sets a bit here (1: a stencil plane copy) and the kernel finishes without
+ * hanging. *status = 0 means no wait ran out; otherwise the call returns
+ * SGPU_ERR_KERNEL_WAIT. sgpu_scf and sgpu_autotune check the word themselves. */
+int sgpu_kernel_status(sgpu_ctx *ctx, int *status);
+
+/* Diagnostic of the bounded waits: one block waits, with a bound of 2e6 SM cycles (about a
+ * millisecond), on a barrier phase that nothing completes. The wait runs out, sets bit 2 of
+ * the status word and the block exits; this call returns that word in *status (2 when the
+ * bound works) and leaves it cleared. No copy is in flight and nothing faults. */
+int sgpu_check_wait_bound(sgpu_ctx *ctx, int *status);
+
 /* ------------------------------------------------------ learned initial density */
 /* No counterpart in the reference, which starts each SCF from the superposition of atomic
  * densities (Init_electronDensity, src/orbitalElecDensInit.c:145). A network trained on
@@ -442,7 +457,7 @@ int sgpu_mlp_adam_step(sgpu_mlp *net, float lr, float beta1, float beta2, float 
 /* ------------------------------------------------------------------- kernel tuning */
 
 /* Number of FP32 stencil kernel variants (tile shape, register blocking, plane ring). */
-#define SGPU_STENCIL_VARIANTS 7
+#define SGPU_STENCIL_VARIANTS 11
 
 /* Time every FP32 stencil kernel variant (tile shape and register blocking) on ncol scratch
  * columns of this context's grid, keep the fastest for later calls, and return its index in

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libsparc_gpu.so")
 SGPU_OK = 0
 SGPU_PREC_FP64 = 64
 SGPU_PREC_FP32 = 32
-STENCIL_VARIANTS = 7  # SGPU_STENCIL_VARIANTS
+STENCIL_VARIANTS = 11  # SGPU_STENCIL_VARIANTS
 
 # every entry point declared in include/sparc_gpu.h
 EXPORTED = [
@@ -39,6 +39,7 @@ EXPORTED = [
     "sgpu_set_nonlocal_apply_variant", "sgpu_set_nonlocal_project_variant", "sgpu_get_variants",
     "sgpu_get_tuning", "sgpu_Calculate_local_forces", "sgpu_Calculate_nonlocal_forces",
     "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
+    "sgpu_kernel_status", "sgpu_check_wait_bound",
 ]
 
 
@@ -553,6 +554,20 @@ class Context:
         n = ctypes.c_long()
         _check(lib().sgpu_profile_read(self._h, int(kind), ctypes.byref(ms), ctypes.byref(n)))
         return float(ms.value), int(n.value)
+
+    def kernel_status(self):
+        """Read and clear the kernel status word: 0 when no bounded wait of a kernel ran out
+        (otherwise the call raises, the results since the last check being invalid)."""
+        st = ctypes.c_int()
+        _check(lib().sgpu_kernel_status(self._h, ctypes.byref(st)))
+        return int(st.value)
+
+    def check_wait_bound(self):
+        """Run the bounded-wait diagnostic; returns the status word it left (2 when a wait
+        that nothing completes runs out as it should)."""
+        st = ctypes.c_int()
+        _check(lib().sgpu_check_wait_bound(self._h, ctypes.byref(st)))
+        return int(st.value)
 
     def last_filter_ms(self):
         ms = ctypes.c_float()

@@ -59,6 +59,9 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
             tmin = std::min(tmin, t);
         }
         if (rc != SGPU_OK) break;
+        // a variant whose bounded copy waits ran out is never chosen (its time reads as 1e30)
+        int kst = 0;
+        if (kernel_status_check(ctx, &kst) != SGPU_OK) tmin = 1e30f;
         if (ms) ms[v] = tmin;
         if (tmin < best_ms) { best_ms = tmin; *best = v; }
     }
@@ -137,7 +140,8 @@ extern "C" {
 int sgpu_set_stencil_variant(sgpu_ctx *ctx, int variant)
 {
     if (!ctx || variant < 0 || variant >= kStencilVariants) {
-        set_error("sgpu_set_stencil_variant: variant must be 0..6");
+        set_error("sgpu_set_stencil_variant: variant must be 0.." +
+                  std::to_string(kStencilVariants - 1));
         return SGPU_ERR_ARG;
     }
     ctx->stencil_variant = variant;

@@ -36,6 +36,21 @@ int ws_get(sgpu_ctx *ctx, int slot, size_t bytes, void **out)
     return SGPU_OK;
 }
 
+int kernel_status_check(sgpu_ctx *ctx, int *status)
+{
+    int h = 0;
+    SGPU_CUDA_TRY(cudaMemcpyAsync(&h, ctx->kstatus, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (status) *status = h;
+    if (h == 0) return SGPU_OK;
+    SGPU_CUDA_TRY(cudaMemsetAsync(ctx->kstatus, 0, sizeof(int), ctx->stream));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    set_error("a kernel's bounded wait on its own copies ran out (status " +
+              std::to_string(h) + "); results since the last check are invalid");
+    return SGPU_ERR_KERNEL_WAIT;
+}
+
 static cudaEvent_t prof_event(sgpu_ctx *ctx)
 {
     if (ctx->prof_next >= ctx->prof_pool.size()) {
@@ -183,8 +198,11 @@ int sgpu_create(sgpu_ctx **out, int device, int Nx, int Ny, int Nz, int FDn, con
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->kstatus, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->kstatus, 0, sizeof(int));
     if (e != cudaSuccess) {
         set_error(std::string("sgpu_create: ") + cudaGetErrorString(e));
+        if (ctx->kstatus) cudaFree(ctx->kstatus);
         delete ctx;
         return SGPU_ERR_CUDA;
     }
@@ -221,6 +239,7 @@ int sgpu_destroy(sgpu_ctx *ctx)
     for (auto e : ctx->prof_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->kstatus) cudaFree(ctx->kstatus);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx->mix;
     kpoint_free(ctx);
@@ -420,7 +439,7 @@ int sgpu_ChebyshevFiltering_f32(sgpu_ctx *ctx, int spin, float *X, int ldi, floa
                                         cudaMemcpyDeviceToHost, ctx->stream));
     SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     SGPU_CUDA_TRY(cudaEventElapsedTime(&ctx->last_filter_ms, ctx->ev0, ctx->ev1));
-    return SGPU_OK;
+    return kernel_status_check(ctx);
 }
 
 int sgpu_get_stream(sgpu_ctx *ctx, void **stream)
@@ -478,6 +497,34 @@ int sgpu_profile_read(sgpu_ctx *ctx, int kind, double *total_ms, long *launches)
         *launches = ctx->prof_n[kind];
     }
     return SGPU_OK;
+}
+
+int sgpu_kernel_status(sgpu_ctx *ctx, int *status)
+{
+    SGPU_TRY(check_ctx(ctx));
+    if (!status) {
+        set_error("sgpu_kernel_status: null argument");
+        return SGPU_ERR_ARG;
+    }
+    return kernel_status_check(ctx, status);
+}
+
+int sgpu_check_wait_bound(sgpu_ctx *ctx, int *status)
+{
+    SGPU_TRY(check_ctx(ctx));
+    if (!status) {
+        set_error("sgpu_check_wait_bound: null argument");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_TRY(kernel_status_check(ctx));  // start from a clear word
+    SGPU_TRY(wait_bound_check(ctx));
+    int st = 0;
+    const int rc = kernel_status_check(ctx, &st);
+    *status = st;
+    if (st == 2) return SGPU_OK;  // the bound ran out as it should and the word is clear again
+    if (rc != SGPU_OK) return rc;
+    set_error("sgpu_check_wait_bound: the bounded wait did not report running out");
+    return SGPU_ERR_STATE;
 }
 
 int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms)

@@ -805,7 +805,7 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
     res->fp64_switch_iter = switch_iter;
     res->filter_ms = filter_ms;
     res->time_s = t_scf;
-    return SGPU_OK;
+    return kernel_status_check(ctx);
 }
 
 }  // extern "C"

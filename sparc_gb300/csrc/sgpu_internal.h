@@ -161,6 +161,7 @@ struct sgpu_ctx {
     int nl_project_variant = 0;  // FP32 projection: 0 per image segment, 1 per point range
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int *kstatus = nullptr;    // device word: bits set by kernel waits that ran out
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on
     // the context stream, resolved by sgpu_profile_read
@@ -193,6 +194,12 @@ struct ProfScope {
     ProfScope(sgpu_ctx *c, int k, cudaStream_t s);
     ~ProfScope();
 };
+
+// read and clear ctx->kstatus (synchronises the stream); SGPU_ERR_KERNEL_WAIT when set
+int kernel_status_check(sgpu_ctx *ctx, int *status = nullptr);
+// one block waiting (bounded, about a millisecond) on a barrier phase nothing completes; the
+// wait runs out and sets bit 2 of ctx->kstatus (stencil.cu)
+int wait_bound_check(sgpu_ctx *ctx);
 
 // memory-kind query: true when p is device (or managed) memory this context can use directly
 bool is_device_ptr(const void *p);

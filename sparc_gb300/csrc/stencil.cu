@@ -31,6 +31,7 @@ struct StencilParams {
     int Nx, Ny, Nz, nslab, zlen;
     T wx[kMaxFDn + 1], wy[kMaxFDn + 1], wz[kMaxFDn + 1];
     T c0, bv, s1, s2;
+    int *status;  // kernel status word (bounded waits that ran out set bits here)
 };
 
 __device__ __forceinline__ int wrapi(int i, int n)
@@ -764,6 +765,344 @@ int launch_ring(const StencilParams<float> &q, dim3 grid, cudaStream_t st)
     return SGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Plane ring fed by bulk copies of the tensor memory accelerator, with no block-wide barrier in
+// the plane loop. Each row of a plane's tile (48 floats for the BY centre rows, x-halo
+// included; 32 for the 2R y-halo rows) and each row of the recurrence term's tile (32 floats)
+// moves by one cp.async.bulk (two where the row wraps periodically in x), issued by one lane
+// of warp 0 (ring) or warp 1 (recurrence term); the potential is read from L2 as in the
+// two-planes-ahead cp.async ring. Three sets of mbarriers order the pipeline:
+//   full[s]   one arrival (expect_tx of the plane's bytes) per fill of ring slot s; the bulk
+//             copies complete its transaction count;
+//   zfull[s]  the same for recurrence-term slot s;
+//   empty[s]  each warp arrives (once its lanes have met at __syncwarp) when it has finished
+//             the step of the plane in ring slot s.
+// Step k reuses the ring slot and the recurrence-term slot of plane k-1, so the issuing warps
+// wait on empty for step k-1 and every other warp runs on as soon as its own planes are full:
+// warps drift apart by up to D steps instead of meeting at a barrier each plane.
+// Every wait is bounded (2e9 SM cycles, about one second): a wait that runs out sets bit 1 of the status
+// word, the thread stops waiting and finishes its loop, and thread 0 waits (bounded) for the
+// last fill of every slot before the block exits, so no copy lands after the block is gone.
+// Needs Nx % 4 == 0 and 16-byte aligned rows of x and z (every copy's address and size are
+// then multiples of 16 bytes). Same arithmetic (b22_block) as the other 2x2 kernels.
+constexpr long long kWaitCycles = 2000000000LL;  // bound of one barrier wait (SM cycles)
+
+__device__ __forceinline__ void mbar_init(unsigned a, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned a)
+{
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(unsigned a, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned a, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 " selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(a), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// the bounded spin after a failed first test, kept out of line so that the unrolled plane loop
+// holds one try_wait per wait site
+__device__ __noinline__ bool mbar_wait_slow(unsigned a, unsigned parity, long long limit)
+{
+    const long long t0 = clock64();
+#pragma unroll 1
+    for (;;) {
+#pragma unroll 1
+        for (int i = 0; i < 64; i++)
+            if (mbar_test(a, parity)) return true;
+        if (clock64() - t0 > limit) return false;
+    }
+}
+// wait for the completion of the phase of parity `parity`; false once `limit` SM cycles
+// have passed
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned a, unsigned parity,
+                                                  long long limit = kWaitCycles)
+{
+    return mbar_test(a, parity) || mbar_wait_slow(a, parity, limit);
+}
+
+// A barrier phase that nothing completes, waited on with a bound of `limit` cycles: the wait
+// runs out and sets bit 2 of the status word; one thread then arrives so the phase completes
+// and the barrier is left balanced. Shows the bound and the status path work on the device.
+__global__ void k_wait_bound_check(int *status, long long limit)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        mbar_init(a, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(a, 0, limit);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (!ok) atomicOr(status, 2);
+        mbar_arrive(a);
+    }
+}
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes,
+                                         unsigned mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+// one tile row: n floats of global row `grow` from column xs (wrapped periodically, split
+// wherever it wraps) into shared memory at byte address dst; Nx % 4 == 0 and xs % 4 == 0.
+// The general form, for grids narrower than a tile row; wider grids use the precomputed
+// one- or two-piece split of the row descriptors.
+__device__ __noinline__ void bulk_row_general(unsigned dst, const float *grow, int xs, int n,
+                                              int Nx, unsigned mbar)
+{
+    int gx = xs % Nx;
+    if (gx < 0) gx += Nx;
+#pragma unroll 1
+    while (n > 0) {
+        const int len = min(n, Nx - gx);
+        bulk_g2s(dst, grow + gx, (unsigned)len * 4u, mbar);
+        dst += (unsigned)len * 4u;
+        n -= len;
+        gx = 0;
+    }
+}
+
+template <int R, int BX, int BY, int D>
+struct BulkShape {
+    static constexpr int XO = (R + 3) / 4 * 4;  // x-halo widened to a 16-byte boundary
+    static constexpr int W = BX + 2 * XO, H = BY + 2 * R;
+    static constexpr int SLOT = H * W;
+    static constexpr int NR = R + D + 1;        // ring slots: planes k .. k+R+D
+    static constexpr int NV = D + 1;            // recurrence-term slots: planes k .. k+D
+    static constexpr int NT = BX / 2 * (BY / 2);
+    static constexpr unsigned plane_bytes = sizeof(float) * (BY * W + 2 * R * BX);
+    static constexpr unsigned zplane_bytes = sizeof(float) * BX * BY;
+    static constexpr size_t data_bytes = sizeof(float) * ((size_t)NR * SLOT + (size_t)NV * BX * BY);
+    static constexpr size_t bar_bytes = (8 * (2 * NR + NV) + 15) / 16 * 16;
+    static constexpr int NDESC = 32 + BY;       // row descriptors: ring rows 0.., z rows 32..
+    static constexpr size_t smem_bytes = data_bytes + bar_bytes + 16 * NDESC;
+    static_assert(H <= 32 && BY <= 32 && NR + NV <= 32 && NT >= 64, "one lane per tile row");
+    static_assert(data_bytes % 16 == 0 && (SLOT * sizeof(float)) % 16 == 0, "16-byte slots");
+};
+
+template <int R, int BX, int BY, int MINB, int D>
+__global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
+    k_stencil_f32_bulk(const StencilParams<float> p)
+{
+    using S = BulkShape<R, BX, BY, D>;
+    constexpr int Q = 2 * R + 1;
+    constexpr int W = S::W, XO = S::XO, NR = S::NR, NV = S::NV;
+    static_assert(Q == 13 && R % 2 == 0 && D >= 1, "the unrolled z-loop is written for radius 6");
+    extern __shared__ __align__(16) float ring[];
+    const float *const zsl = ring + NR * S::SLOT;  // [NV][BY][BX] recurrence term
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * (BX / 2) + tx;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+    const int col = blockIdx.z / p.nslab;
+    const int slab = blockIdx.z - col * p.nslab;
+    const int zs = slab * p.zlen;
+    const int ze = min(zs + p.zlen, p.Nz);
+    if (zs >= ze) return;
+
+    const unsigned sring = (unsigned)__cvta_generic_to_shared(ring);
+    const unsigned bfull = sring + (unsigned)S::data_bytes;  // full[NR]
+    const unsigned bzfull = bfull + 8u * NR;                 // zfull[NV]
+    const unsigned bempty = bzfull + 8u * NV;                // empty[NR]
+    // row descriptors {plane offset of the first piece, of the second piece (column 0),
+    // shared byte offset within the slot, total bytes << 16 | bytes of the first piece}
+    int4 *const desc = reinterpret_cast<int4 *>(reinterpret_cast<char *>(ring) + S::data_bytes +
+                                                S::bar_bytes);
+    constexpr int NW = S::NT / 32;
+    if (tid == 0) {
+        for (int s = 0; s < NR; s++) {
+            mbar_init(bfull + 8u * s, 1);
+            mbar_init(bempty + 8u * s, NW);
+        }
+        for (int s = 0; s < NV; s++) mbar_init(bzfull + 8u * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0 && lane < S::H) {
+        const int r = lane;
+        const bool centre = r >= R && r < R + BY;
+        const int n = centre ? W : BX;
+        const int rowoff = wrapi(y0 - R + r, p.Ny) * p.Nx;
+        const int gx = wrapi(centre ? x0 - XO : x0, p.Nx);
+        const int len0 = min(n, p.Nx - gx);
+        desc[r] = make_int4(rowoff + gx, rowoff, (r * W + (centre ? 0 : XO)) * 4,
+                            (n * 4) << 16 | len0 * 4);
+    } else if (warp == 1 && lane < BY) {
+        const int rowoff = wrapi(y0 + lane, p.Ny) * p.Nx;
+        const int len0 = min(BX, p.Nx - x0);
+        desc[32 + lane] = make_int4(rowoff + x0, rowoff, lane * BX * 4, (BX * 4) << 16 | len0 * 4);
+    }
+    __syncthreads();
+    const bool narrow = p.Nx < W;  // a tile row may wrap more than once: general split
+
+    const int i0 = x0 + 2 * tx, j0 = y0 + 2 * ty;
+    const bool in0 = i0 < p.Nx, in1 = i0 + 1 < p.Nx;
+    const bool r0ok = j0 < p.Ny, r1ok = j0 + 1 < p.Ny;
+    const int gx0 = wrapi(i0, p.Nx), gx1 = wrapi(i0 + 1, p.Nx);
+    const int row0 = wrapi(j0, p.Ny) * p.Nx, row1 = wrapi(j0 + 1, p.Ny) * p.Nx;
+    const int NxNy = p.Nx * p.Ny;
+    const float *__restrict__ xc = p.x + (long)col * p.ldx;
+    const float *__restrict__ zc = p.z ? p.z + (long)col * p.ldz : nullptr;
+    float *__restrict__ oc = p.out + (long)col * p.ldo;
+    const float *vsrc = p.v ? p.v + gx0 + row0 : nullptr;
+    const int drow = row1 - row0, dx = gx1 - gx0;
+
+    bool alive = true;    // false once one of this thread's waits has run out
+    unsigned ph = 0;      // parity of the next wait: bits 0..NR-1 full, NR.. zfull
+    unsigned phe = 0;     // parity of the next wait on empty (issuing warps)
+    auto wait = [&](unsigned bar, int bit, unsigned &bits) {
+        if (alive && !mbar_wait_bounded(bar, (bits >> bit) & 1u)) {
+            alive = false;
+            if (p.status) atomicOr(p.status, 1);
+        }
+        bits ^= 1u << bit;
+    };
+    // one row per lane: ring rows from warp 0 (descriptors 0..H-1), recurrence-term rows from
+    // warp 1 (32..32+BY-1); pb = the plane's first element, sbase = the slot's shared address
+    auto issue_row = [&](const int4 d, const float *pb, unsigned sbase, unsigned bar, int xs) {
+        const unsigned b0 = (unsigned)d.w & 0xffffu, tot = (unsigned)d.w >> 16;
+        if (narrow) {
+            bulk_row_general(sbase + d.z, pb + d.y, xs, (int)(tot / 4), p.Nx, bar);
+        } else {
+            bulk_g2s(sbase + d.z, pb + d.x, b0, bar);
+            if (b0 < tot) bulk_g2s(sbase + d.z + b0, pb + d.y, tot - b0, bar);
+        }
+    };
+    // ring plane pl (zs <= pl < 2 Nz) into ring slot s
+    auto issue_ring = [&](int pl, int s) {
+        const unsigned bar = bfull + 8u * s;
+        if (lane == 0) mbar_arrive_tx(bar, S::plane_bytes);
+        __syncwarp();
+        if (lane < S::H) {
+            const bool centre = lane >= R && lane < R + BY;
+            issue_row(desc[lane], xc + (long)(pl >= p.Nz ? pl - p.Nz : pl) * NxNy,
+                      sring + (unsigned)(s * S::SLOT * 4), bar, centre ? x0 - XO : x0);
+        }
+    };
+    // recurrence-term plane pl (zs <= pl < Nz) into its slot s
+    auto issue_z = [&](int pl, int s) {
+        const unsigned bar = bzfull + 8u * s;
+        if (lane == 0) mbar_arrive_tx(bar, S::zplane_bytes);
+        __syncwarp();
+        if (lane < BY)
+            issue_row(desc[32 + lane], zc + (long)pl * NxNy,
+                      sring + (unsigned)((NR * S::SLOT + s * BX * BY) * 4), bar, x0);
+    };
+
+    // prologue: the register queue holds planes zs-R .. zs+R-1 (read directly); the ring
+    // receives planes zs .. zs+R+D-1 and the recurrence term planes zs .. zs+D-1
+    float2 qa[Q], qb[Q];
+#pragma unroll
+    for (int m = 0; m < 2 * R; m++) {
+        const int pl = wrapi(zs - R + m, p.Nz) * NxNy;
+        qa[m] = ld_pair<true>(xc, pl + gx0 + row0, pl + gx1 + row0);
+        qb[m] = ld_pair<true>(xc, pl + gx0 + row1, pl + gx1 + row1);
+    }
+    if (warp == 0) {
+        for (int pl = zs; pl < zs + R + D && pl < ze + R; pl++) issue_ring(pl, pl % NR);
+    } else if (warp == 1 && zc) {
+        for (int pl = zs; pl < zs + D && pl < ze; pl++) issue_z(pl, pl % NV);
+    }
+    int sk = zs % NR;     // ring slot of plane k
+    int svk = zs % NV;    // recurrence-term slot of plane k
+    int ko = zs * NxNy;   // offset of plane k
+
+#define SGPU_BULK_STEP(U)                                                                        \
+    {                                                                                            \
+        const int k = kb + (U);                                                                  \
+        if (k < ze) {                                                                            \
+            /* slots of plane k-1 receive ring plane k+R+D and recurrence-term plane k+D */      \
+            if (k + D < ze && (warp == 0 || (warp == 1 && zc))) {                                \
+                const int se = sk == 0 ? NR - 1 : sk - 1;                                        \
+                if (k > zs) wait(bempty + 8u * se, se, phe);                                     \
+                if (warp == 0) issue_ring(k + R + D, se);                                        \
+                else issue_z(k + D, svk == 0 ? NV - 1 : svk - 1);                                \
+            }                                                                                    \
+            const int skr = sk + R >= NR ? sk + R - NR : sk + R;                                 \
+            if (k < zs + R) wait(bfull + 8u * sk, sk, ph);                                       \
+            wait(bfull + 8u * skr, skr, ph);                                                     \
+            if (zc) wait(bzfull + 8u * svk, NR + svk, ph);                                       \
+            const float *sl = ring + sk * S::SLOT;                                               \
+            const float *sq = ring + skr * S::SLOT + (2 * ty + R) * W + XO + 2 * tx;             \
+            qa[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq);                       \
+            qb[((U) + 2 * R) % Q] = *reinterpret_cast<const float2 *>(sq + W);                   \
+            float2 vcs[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};                      \
+            float2 zcs[2] = {vcs[0], vcs[1]};                                                    \
+            if (vsrc) {                                                                          \
+                vcs[0] = ld_pair<true>(vsrc, ko, ko + dx);                                       \
+                vcs[1] = ld_pair<true>(vsrc, ko + drow, ko + drow + dx);                         \
+            }                                                                                    \
+            if (zc) {                                                                            \
+                const float *zz = zsl + svk * BX * BY + 2 * ty * BX + 2 * tx;                    \
+                zcs[0] = *reinterpret_cast<const float2 *>(zz);                                  \
+                zcs[1] = *reinterpret_cast<const float2 *>(zz + BX);                             \
+            }                                                                                    \
+            float2 yv[2 * R + 2];                                                                \
+            _Pragma("unroll") for (int t = 0; t < 2 * R + 2; t++)                                \
+                yv[t] = *reinterpret_cast<const float2 *>(sl + (2 * ty + t) * W + XO + 2 * tx);  \
+            float2 o[2];                                                                         \
+            b22_block<R, Q, (U)>(p, sl + (2 * ty + R) * W + XO - R + 2 * tx, W, yv, qa, qb,     \
+                                 vcs, zcs, vsrc != nullptr, zc != nullptr, o);                   \
+            __syncwarp();                                                                        \
+            if (lane == 0) mbar_arrive(bempty + 8u * sk);                                        \
+            b22_store<true>(oc, ko, row0, row1, gx0, gx1, r0ok, r1ok, in0, in1, o);              \
+            sk = sk + 1 == NR ? 0 : sk + 1;                                                      \
+            svk = svk + 1 == NV ? 0 : svk + 1;                                                   \
+            ko += NxNy;                                                                          \
+        }                                                                                        \
+    }
+
+    for (int kb = zs; kb < ze; kb += Q) {
+        SGPU_BULK_STEP(0) SGPU_BULK_STEP(1) SGPU_BULK_STEP(2) SGPU_BULK_STEP(3)
+        SGPU_BULK_STEP(4) SGPU_BULK_STEP(5) SGPU_BULK_STEP(6) SGPU_BULK_STEP(7)
+        SGPU_BULK_STEP(8) SGPU_BULK_STEP(9) SGPU_BULK_STEP(10) SGPU_BULK_STEP(11)
+        SGPU_BULK_STEP(12)
+    }
+#undef SGPU_BULK_STEP
+    // no copy may land after the block exits: wait for the last fill of every slot (planes
+    // zs .. ze+R-1 of the ring, zs .. ze-1 of the recurrence term were issued)
+    if (tid == 0) {
+        bool ok = true;
+        for (int s = 0; s < NR; s++) {
+            const int last = ze + R - 1 - ((ze + R - 1 - s) % NR + NR) % NR;
+            if (last >= zs && !mbar_wait_bounded(bfull + 8u * s, ((last - zs) / NR) & 1)) ok = false;
+        }
+        if (zc)
+            for (int s = 0; s < NV; s++) {
+                const int last = ze - 1 - ((ze - 1 - s) % NV + NV) % NV;
+                if (last >= zs && !mbar_wait_bounded(bzfull + 8u * s, ((last - zs) / NV) & 1)) ok = false;
+            }
+        if (!ok && p.status) atomicOr(p.status, 1);
+    }
+}
+
+template <int R, int BX, int BY, int MINB, int D>
+int launch_bulk(const StencilParams<float> &q, dim3 grid, cudaStream_t st)
+{
+    constexpr size_t smem = BulkShape<R, BX, BY, D>::smem_bytes;
+    auto kern = k_stencil_f32_bulk<R, BX, BY, MINB, D>;
+    SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    kern<<<grid, dim3(BX / 2, BY / 2), smem, st>>>(q);
+    return SGPU_OK;
+}
+
 }  // namespace
 
 template <typename T>
@@ -798,17 +1137,21 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     c0 += c;
     p.c0 = (T)c0;
     p.bv = (T)bv; p.s1 = (T)s1; p.s2 = (T)s2;
+    p.status = ctx->kstatus;
     if (!v || fabs(bv) < 1e-14) p.v = nullptr;
     if (!z || s2 == 0.0) p.z = nullptr;
 
     const bool f32 = sizeof(T) == 4;
     // FP32 variants (autotune.cu): 0 paired 32x16, 1 2x2-blocked 32x16, 2 2x2-blocked 64x8,
     // 3 paired 64x8, 4 2x2-blocked 32x16 with 3 blocks per SM, 5 and 6 2x2-blocked 32x16 fed
-    // from the shared-memory plane ring one and two planes ahead (6: potential from L2)
+    // from the shared-memory plane ring one and two planes ahead (6: potential from L2), 7 and
+    // 8 the plane ring fed by bulk copies two and one planes ahead, 9 and 10 the cp.async
+    // plane ring on 32x32 tiles (256 threads, 2 blocks per SM) one and two planes ahead
     const int variant = f32 ? ctx->stencil_variant : 0;
     const bool wide = variant == 2 || variant == 3;
+    const bool tall = variant == 9 || variant == 10;
     const int tbx = f32 ? (wide ? 64 : BXP) : BX;
-    const int tby = f32 ? (wide ? 8 : BYP) : BY;
+    const int tby = f32 ? (wide ? 8 : tall ? 32 : BYP) : BY;
     const int tilesx = (ctx->Nx + tbx - 1) / tbx;
     const int tilesy = (ctx->Ny + tby - 1) / tby;
     // split z into slabs until there are enough blocks to fill 152 SMs several times over
@@ -826,6 +1169,8 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
     // aligned (the potential and recurrence term still move in 8-byte pieces)
     auto al16 = [](const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; };
     const bool quad = vec && ctx->Nx % 4 == 0 && al16(x) && ldx % 4 == 0;
+    // the bulk-copy ring also moves the recurrence term by rows of 16-byte pieces
+    const bool bulk = quad && (!p.z || (al16(z) && ldz % 4 == 0));
     const int maxz = 65535 / nslab;
     for (int c0i = 0; c0i < ncol; c0i += maxz) {
         int nc = ncol - c0i < maxz ? ncol - c0i : maxz;
@@ -875,6 +1220,35 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
                 else
                     SGPU_TRY((launch_ring<R, 32, 16, 4, 1, 2, true>(q, grid, st)));
                 break;
+            case 7:  // plane ring fed by bulk copies, two planes ahead (else as variant 6)
+            case 8:  // the same, one plane ahead
+                if (bulk && variant == 7)
+                    SGPU_TRY((launch_bulk<R, 32, 16, 4, 2>(q, grid, st)));
+                else if (bulk)
+                    SGPU_TRY((launch_bulk<R, 32, 16, 4, 1>(q, grid, st)));
+                else if (quad)
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 4, 2, true>(q, grid, st)));
+                else if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 2, 2, true>(q, grid, st)));
+                else
+                    SGPU_TRY((launch_ring<R, 32, 16, 4, 1, 2, true>(q, grid, st)));
+                break;
+            case 9:  // plane ring on 32x32 tiles, one plane ahead
+                if (quad)
+                    SGPU_TRY((launch_ring<R, 32, 32, 2, 4, 1, false>(q, grid, st)));
+                else if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 32, 2, 2, 1, false>(q, grid, st)));
+                else
+                    SGPU_TRY((launch_ring<R, 32, 32, 2, 1, 1, false>(q, grid, st)));
+                break;
+            case 10:  // plane ring on 32x32 tiles, two planes ahead (potential from L2)
+                if (quad)
+                    SGPU_TRY((launch_ring<R, 32, 32, 2, 4, 2, true>(q, grid, st)));
+                else if (vec)
+                    SGPU_TRY((launch_ring<R, 32, 32, 2, 2, 2, true>(q, grid, st)));
+                else
+                    SGPU_TRY((launch_ring<R, 32, 32, 2, 1, 2, true>(q, grid, st)));
+                break;
             default:
                 k_stencil_f32x2<R, BXP, BYP, 3><<<grid, dim3(BXP / 2, BYP), 0, st>>>(q);
             }
@@ -882,6 +1256,13 @@ int launch_stencil(sgpu_ctx *ctx, int ncol, double a, double bv, double c, const
             k_stencil_orth<T, R, BX, BY><<<grid, dim3(BX, BY), 0, st>>>(q);
         }
     }
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
+int wait_bound_check(sgpu_ctx *ctx)
+{
+    k_wait_bound_check<<<1, 32, 0, ctx->stream>>>(ctx->kstatus, 2000000LL);
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
 }

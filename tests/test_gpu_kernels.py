@@ -120,10 +120,14 @@ def test_fp32_hamiltonian_and_filter_tolerance(gpu_available):
     assert rel_err(X, Xo) < TOL32_FILTER
 
 
-@pytest.mark.parametrize("shape", [(48, 40, 36), (45, 19, 30)])
+@pytest.mark.parametrize("shape", [(48, 40, 36), (45, 19, 30), (52, 20, 17), (8, 12, 6),
+                                   (96, 24, 40)])
 def test_fp32_stencil_variants_identical(gpu_available, shape):
-    """Every FP32 stencil variant (tiles, 2x2 register blocking, 8-byte or 4-byte accesses)
-    gives bit-identical filter output; the autotuner picks one of them."""
+    """Every FP32 stencil variant (tiles, 2x2 register blocking, 8-byte or 4-byte accesses,
+    plane rings fed by cp.async or by bulk copies) gives bit-identical filter output; the
+    autotuner picks one of them. Nx % 4 == 0 shapes take the 16-byte and bulk-copy paths,
+    including tiles cut by the grid edge (52 x 20), rows that wrap several times in x (Nx = 8)
+    and z slabs of exactly the stencil radius (Nz = 6)."""
     grid, nl, veff, rng = _random_case(shape, seed=11, natom=4)
     Nd = shape[0] * shape[1] * shape[2]
     ctx = make_ctx(grid, nl, veff)
@@ -138,7 +142,8 @@ def test_fp32_stencil_variants_identical(gpu_available, shape):
         np.testing.assert_array_equal(Y, outs[0][1])
         np.testing.assert_array_equal(X, outs[0][0])
     best, ms = ctx.autotune(ncol=3)
-    assert 0 <= best < sg.STENCIL_VARIANTS and np.all(ms > 0)
+    assert 0 <= best < sg.STENCIL_VARIANTS and np.all(ms > 0) and np.all(ms < 1e29)
+    assert ctx.kernel_status() == 0
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
@@ -247,3 +252,24 @@ def test_empty_block_is_a_no_op(gpu_available):
     ctx = make_ctx(grid, nl, veff)
     X = np.zeros((0, ctx.Nd)); Y = np.zeros((0, ctx.Nd))
     ctx.ChebyshevFiltering(X, Y, 5, 0.3, 25.0, -2.0)
+
+
+def test_bounded_wait_reports_and_context_stays_usable(gpu_available):
+    """A barrier wait that nothing completes runs out after its bound (about a millisecond
+    here), sets the status word and lets the kernel exit; the context then works as before:
+    a bulk-copy filter afterwards gives the same result as the cp.async ring and leaves the
+    status word clear."""
+    grid, nl, veff, rng = _random_case((48, 40, 36), seed=9, natom=3)
+    ctx = make_ctx(grid, nl, veff)
+    assert ctx.kernel_status() == 0
+    assert ctx.check_wait_bound() == 2
+    assert ctx.kernel_status() == 0
+    x = rng.uniform(-1, 1, (2, ctx.Nd)).astype(np.float32)
+    outs = []
+    for v in (6, 7):
+        ctx.set_stencil_variant(v)
+        X = x.copy(); Y = np.zeros_like(x)
+        ctx.ChebyshevFiltering_f32(X, Y, 4, 0.5, 50.0, -1.0)
+        outs.append(Y)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert ctx.kernel_status() == 0
