@@ -39,7 +39,8 @@ EXPORTED = [
     "sgpu_set_nonlocal_apply_variant", "sgpu_set_nonlocal_project_variant", "sgpu_get_variants",
     "sgpu_get_tuning", "sgpu_Calculate_local_forces", "sgpu_Calculate_nonlocal_forces",
     "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
-    "sgpu_kernel_status", "sgpu_check_wait_bound",
+    "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
+    "sgpu_get_nonlocal_fuse",
 ]
 
 
@@ -561,6 +562,17 @@ class Context:
         st = ctypes.c_int()
         _check(lib().sgpu_kernel_status(self._h, ctypes.byref(st)))
         return int(st.value)
+
+    def set_nonlocal_fuse(self, on):
+        """Carry the nonlocal projections across filter degrees (fused range apply) or not."""
+        _check(lib().sgpu_set_nonlocal_fuse(self._h, 1 if on else 0))
+
+    def nonlocal_fuse(self):
+        """(on, ms of one fused launch at the last tuning)."""
+        on = ctypes.c_int()
+        ms = ctypes.c_double()
+        _check(lib().sgpu_get_nonlocal_fuse(self._h, ctypes.byref(on), ctypes.byref(ms)))
+        return bool(on.value), float(ms.value)
 
     def check_wait_bound(self):
         """Run the bounded-wait diagnostic; returns the status word it left (2 when a wait

@@ -121,6 +121,39 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
                 if (rc == SGPU_OK && tmin < pbest) { pbest = tmin; pv = v; }
             }
             ctx->nl_project_variant = rc == SGPU_OK ? pv : saved_p;
+            // the range apply with the next degree's projection fused: the FP32 filter uses it
+            // when one fused launch beats the fastest apply plus the fastest projection
+            ctx->nl_fuse = false;
+            ctx->tune_fused_ms = 0.0;
+            float *anext = nullptr;
+            const size_t abytes = sizeof(float) * (size_t)ctx->nl.ntot * lda;
+            if (rc == SGPU_OK && ctx->nl.nrange > 0) {
+                if (cudaMallocAsync(&anext, abytes, st) != cudaSuccess) rc = SGPU_ERR_CUDA;
+                float t = 0.f, tmin = 1e30f;
+                for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
+                    if (cudaEventRecord(ctx->ev0, st) != cudaSuccess ||
+                        cudaMemsetAsync(anext, 0, abytes, st) != cudaSuccess) {
+                        rc = SGPU_ERR_CUDA;
+                        break;
+                    }
+                    if ((rc = launch_nonlocal_apply_project(ctx, ncol, alpha, lda, 1.0, Y, Nd,
+                                                            anext, st)) != SGPU_OK)
+                        break;
+                    if (cudaEventRecord(ctx->ev1, st) != cudaSuccess ||
+                        cudaEventSynchronize(ctx->ev1) != cudaSuccess ||
+                        cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) != cudaSuccess) {
+                        rc = SGPU_ERR_CUDA;
+                        break;
+                    }
+                    if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
+                }
+                if (rc == SGPU_OK) {
+                    ctx->tune_fused_ms = tmin;
+                    ctx->nl_fuse = tmin < ctx->tune_apply_ms[ctx->nl_apply_variant] +
+                                              ctx->tune_project_ms[ctx->nl_project_variant];
+                }
+                if (anext) cudaFreeAsync(anext, st);
+            }
             cudaFreeAsync(alpha, st);
         }
     }
@@ -166,6 +199,27 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant)
         return SGPU_ERR_ARG;
     }
     ctx->nl_project_variant = variant;
+    return SGPU_OK;
+}
+
+int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int on)
+{
+    if (!ctx || (on != 0 && on != 1)) {
+        set_error("sgpu_set_nonlocal_fuse: need a context and on = 0 or 1");
+        return SGPU_ERR_ARG;
+    }
+    ctx->nl_fuse = on == 1;
+    return SGPU_OK;
+}
+
+int sgpu_get_nonlocal_fuse(sgpu_ctx *ctx, int *on, double *fused_ms)
+{
+    if (!ctx) {
+        set_error("sgpu_get_nonlocal_fuse: null context");
+        return SGPU_ERR_ARG;
+    }
+    if (on) *on = filter_fuses_projection(ctx) ? 1 : 0;
+    if (fused_ms) *fused_ms = ctx->tune_fused_ms;
     return SGPU_OK;
 }
 

@@ -28,26 +28,60 @@ const float *veff_of<float>(sgpu_ctx *ctx, int spin)
     return ctx->veff32 ? ctx->veff32 + (long)spin * ctx->Nd : nullptr;
 }
 
+// alpha_in (optional): dV * Gamma * Chiᵀ x already formed (ld nonlocal_alpha_ld), so no
+// projection is launched; alpha_out (optional, FP32 with alpha_in): receives dV * Gamma * Chiᵀ
+// of the finished hx from the fused range apply, for the next filter degree.
 template <typename T>
 int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, long ldx, T *hx,
-                    long ldh, double s1, double s2, const T *z, long ldz, cudaStream_t st)
+                    long ldh, double s1, double s2, const T *z, long ldz, cudaStream_t st,
+                    const T *alpha_in, T *alpha_out)
 {
     if (spin < 0 || spin >= ctx->nspin_veff) {
         set_error("Hamiltonian: no local potential set for this spin block");
         return SGPU_ERR_STATE;
     }
-    T *alpha = nullptr;
+    const T *alpha = alpha_in;
     const long lda = nonlocal_alpha_ld(ncol, (int)sizeof(T));
-    if (ctx->has_nl && ctx->nl.ntot > 0) {
-        const size_t bytes = sizeof(T) * (size_t)ctx->nl.ntot * lda;
-        SGPU_TRY(ws_get(ctx, WS_ALPHA, bytes, (void **)&alpha));
-        SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, bytes, st));
-        SGPU_TRY(launch_nonlocal_project<T>(ctx, ncol, x, ldx, alpha, lda, st));
+    const size_t abytes = ctx->has_nl ? sizeof(T) * (size_t)ctx->nl.ntot * lda : 0;
+    if (!alpha && ctx->has_nl && ctx->nl.ntot > 0) {
+        T *a = nullptr;
+        SGPU_TRY(ws_get(ctx, WS_ALPHA, abytes, (void **)&a));
+        SGPU_CUDA_TRY(cudaMemsetAsync(a, 0, abytes, st));
+        SGPU_TRY(launch_nonlocal_project<T>(ctx, ncol, x, ldx, a, lda, st));
+        alpha = a;
     }
     SGPU_TRY(launch_stencil<T>(ctx, ncol, -0.5, 1.0, c, veff_of<T>(ctx, spin), x, ldx, hx, ldh,
                                s1, s2, z, ldz, st));
-    if (alpha) SGPU_TRY(launch_nonlocal_apply<T>(ctx, ncol, alpha, lda, s1, hx, ldh, st));
-    return SGPU_OK;
+    if (!alpha) return SGPU_OK;
+    if constexpr (sizeof(T) == 4) {
+        if (alpha_out) {
+            SGPU_CUDA_TRY(cudaMemsetAsync(alpha_out, 0, abytes, st));
+            return launch_nonlocal_apply_project(ctx, ncol, alpha, lda, s1, hx, ldh, alpha_out,
+                                                 st);
+        }
+    }
+    return launch_nonlocal_apply<T>(ctx, ncol, alpha, lda, s1, hx, ldh, st);
+}
+
+bool filter_fuses_projection(sgpu_ctx *ctx)
+{
+    return ctx->nl_fuse && ctx->has_nl && ctx->nl.ntot > 0 && ctx->nl.nrange > 0;
+}
+
+// The FP32 filter's projection buffers when the projections are carried across degrees:
+// A = dV * Gamma * Chiᵀ X (one projection launch), B the buffer the fused applies alternate
+// with. Both null when the filter does not fuse.
+static int carried_alpha(sgpu_ctx *ctx, int ncol, const float *X, long ldx, float **A, float **B,
+                         cudaStream_t st)
+{
+    *A = *B = nullptr;
+    if (!filter_fuses_projection(ctx)) return SGPU_OK;
+    const long lda = nonlocal_alpha_ld(ncol, 4);
+    const size_t bytes = sizeof(float) * (size_t)ctx->nl.ntot * lda;
+    SGPU_TRY(ws_get(ctx, WS_ALPHA, bytes, (void **)A));
+    SGPU_TRY(ws_get(ctx, WS_ALPHA2, bytes, (void **)B));
+    SGPU_CUDA_TRY(cudaMemsetAsync(*A, 0, bytes, st));
+    return launch_nonlocal_project<float>(ctx, ncol, X, ldx, *A, lda, st);
 }
 
 // On return the filtered block is in Y and the degree m-1 iterate in X, as in the reference.
@@ -74,11 +108,17 @@ int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int n
     const bool route = ((m - 1) % 2) == 1;
     if (route) SGPU_TRY(ws_get(ctx, WS_STAGE_C, sizeof(T) * (size_t)Nd * ncol, (void **)&W));
 
+    // FP32 with the fused range apply: each degree's apply also projects its finished output
+    // for the next degree, alternating between two projection buffers
+    T *acur = nullptr, *anext = nullptr;
+    if constexpr (sizeof(T) == 4) SGPU_TRY(carried_alpha(ctx, ncol, X, ldx, &acur, &anext, st));
+
     // Y_0 = (sigma1/e) (H - c I) X
     T *y0 = route ? W : Y;
     long ly0 = route ? Nd : ldy;
     SGPU_TRY(hamiltonian_dev<T>(ctx, spin, ncol, -c, X, ldx, y0, ly0, sigma1 / e, 0.0, nullptr,
-                                0, st));
+                                0, st, acur, m > 1 ? anext : nullptr));
+    std::swap(acur, anext);
     // (cur, prev) = (Y_j, Y_{j-1}) with Y_{-1} = X
     T *cur = y0, *prev = X;
     long ldc = ly0, ldp = ldx;
@@ -92,7 +132,8 @@ int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int n
         if (route && j == 1) { dst = Y; ldd = ldy; }
         if (route && j == 2) { dst = X; ldd = ldx; }
         SGPU_TRY(hamiltonian_dev<T>(ctx, spin, ncol, -c, cur, ldc, dst, ldd, vscal, -vscal2,
-                                    prev, ldp, st));
+                                    prev, ldp, st, acur, j + 1 < m ? anext : nullptr));
+        std::swap(acur, anext);
         prev = cur; ldp = ldc;
         cur = dst; ldc = ldd;
         sigma = sigma2;
@@ -125,13 +166,18 @@ int chebyshev_graded(sgpu_ctx *ctx, int spin, float *X32, float *Y32, double *X6
     const double sigma1 = sigma;
     const double gamma = 2.0 / sigma1;
     const int m32 = m - k64;
+    float *acur = nullptr, *anext = nullptr;  // carried projections (fused range apply)
+    SGPU_TRY(carried_alpha(ctx, ncol, X32, Nd, &acur, &anext, st));
     SGPU_TRY(hamiltonian_dev<float>(ctx, spin, ncol, -c, X32, Nd, Y32, Nd, sigma1 / e, 0.0,
-                                    nullptr, 0, st));
+                                    nullptr, 0, st, acur, m32 > 1 ? anext : nullptr));
+    std::swap(acur, anext);
     float *cur = Y32, *prev = X32;
     for (int j = 1; j < m32; j++) {
         const double sigma2 = 1.0 / (gamma - sigma);
         SGPU_TRY(hamiltonian_dev<float>(ctx, spin, ncol, -c, cur, Nd, prev, Nd,
-                                        2.0 * sigma2 / e, -sigma * sigma2, prev, Nd, st));
+                                        2.0 * sigma2 / e, -sigma * sigma2, prev, Nd, st, acur,
+                                        j + 1 < m32 ? anext : nullptr));
+        std::swap(acur, anext);
         std::swap(cur, prev);
         sigma = sigma2;
     }
@@ -153,9 +199,10 @@ int chebyshev_graded(sgpu_ctx *ctx, int spin, float *X32, float *Y32, double *X6
 
 template int hamiltonian_dev<double>(sgpu_ctx *, int, int, double, const double *, long,
                                      double *, long, double, double, const double *, long,
-                                     cudaStream_t);
+                                     cudaStream_t, const double *, double *);
 template int hamiltonian_dev<float>(sgpu_ctx *, int, int, double, const float *, long, float *,
-                                    long, double, double, const float *, long, cudaStream_t);
+                                    long, double, double, const float *, long, cudaStream_t,
+                                    const float *, float *);
 template int chebyshev_dev<double>(sgpu_ctx *, int, double *, long, double *, long, int, int,
                                    double, double, double, cudaStream_t);
 template int chebyshev_dev<float>(sgpu_ctx *, int, float *, long, float *, long, int, int,

@@ -340,6 +340,139 @@ __global__ void __launch_bounds__(256, 4)
     }
 }
 
+// Range apply with the next projection fused (FP32). The Chebyshev filter projects each new
+// iterate right after the apply that finishes it, and that apply already holds the finished
+// values of its range's covered points in shared memory, with the range's Chi rows staged. So
+// per group of 64 columns this kernel: gathers the output tile, adds scale * sum_j Chi_j
+// alpha_j exactly as k_nl_apply_range does (lane l now owns columns 2l, 2l+1, the tile rows
+// are padded to 66 floats; the additions per element are the same IEEE operations in the same
+// item order, so the output is bit-identical), writes the tile back, and then, as
+// k_nl_project_range does on a gathered tile, accumulates dV * Gamma * Chi^T tile per work
+// item and adds it atomically into alpha_next (zeroed by the caller). Ranges partition the
+// covered points, so a range's tile is final once its own apply is done. The separate
+// projection of the next degree, and its read of every covered element, disappear.
+template <int MAXJ>
+__global__ void __launch_bounds__(256, MAXJ <= 9 ? 4 : 2)  // larger sets: registers, no spills
+    k_nl_apply_project_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
+                             const int *__restrict__ rng_item0, const int *__restrict__ item_e0,
+                             const int *__restrict__ item_wsplit, const int2 *__restrict__ item_row,
+                             const int *__restrict__ pe_lp, const float *__restrict__ pe_chi,
+                             const int *__restrict__ cov_pt, const float *__restrict__ gamma,
+                             int ncol, const float *__restrict__ alpha, long lda, float scale,
+                             float *__restrict__ out, long ldo, float *__restrict__ alpha_next,
+                             float dV)
+{
+    constexpr int NC = 64, OLD = NC + 2;             // columns per group, padded tile row
+    constexpr int MAXJP = (MAXJ + 3) / 4 * 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *cs = reinterpret_cast<float *>(smem_raw);  // [entries][MAXJP]
+    const int r = blockIdx.x;
+    const int p0 = rng_pt0[r], npt = rng_pt0[r + 1] - p0;
+    const int eb = rng_ent0[r], ne = rng_ent0[r + 1] - eb;
+    const int ib = rng_item0[r], ni = rng_item0[r + 1] - ib;
+    float *os = cs + (size_t)ne * MAXJP;                          // [kRangePts][OLD]
+    int *lps = reinterpret_cast<int *>(os + kRangePts * OLD);     // [entries]
+    int *gps = lps + ne;                                          // [kRangePts]
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+    for (int i = t; i < npt; i += 256) gps[i] = cov_pt[p0 + i];
+    for (int i = t; i < ne; i += 256) lps[i] = pe_lp[eb + i];
+    {
+        const float4 *src = reinterpret_cast<const float4 *>(pe_chi + (long)eb * MAXJP);
+        float4 *dst = reinterpret_cast<float4 *>(cs);
+        for (int i = t; i < ne * (MAXJP / 4); i += 256) dst[i] = __ldg(src + i);
+    }
+    const int ngroup = (ncol + NC - 1) / NC;
+    for (int gi = 0; gi < ngroup; gi++) {
+        const int n0 = ((gi + r) % ngroup) * NC;
+        const int c0 = n0 + 2 * lane;
+        __syncthreads();  // staging done / previous tile written back and projected
+        gather_tile<OLD, NC>(out, ldo, n0, ncol, gps, npt, os);
+        __syncthreads();
+        // apply: warp w owns the tile rows of points [w * kRangeWarpPts, (w + 1) * kRangeWarpPts)
+        for (int it = 0; it < ni; it++) {
+            const int *ws = item_wsplit + (long)(ib + it) * (kRangeWarps + 1);
+            const int e0 = ws[warp] - eb, e1 = ws[warp + 1] - eb;
+            if (e0 == e1) continue;
+            const int2 row = item_row[ib + it];
+            float2 a[MAXJ];  // scale * alpha of columns (2 lane, 2 lane + 1)
+#pragma unroll
+            for (int j = 0; j < MAXJ; j++) {
+                a[j] = make_float2(0.f, 0.f);
+                if (j < row.y) {
+                    const float *ar = alpha + (long)(row.x + j) * lda;
+                    if (c0 + 1 < ncol) {  // lda and c0 are even: an 8-byte aligned pair
+                        const float2 v = __ldg(reinterpret_cast<const float2 *>(ar + c0));
+                        a[j] = make_float2(scale * v.x, scale * v.y);
+                    } else if (c0 < ncol) {
+                        a[j].x = scale * __ldg(ar + c0);
+                    }
+                }
+            }
+#pragma unroll 4
+            for (int e = e0; e < e1; e++) {
+                const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
+                float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < MAXJP / 4; q++) {
+                    const float4 c4 = cv[q];
+                    const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                    for (int w = 0; w < 4; w++)
+                        if (q * 4 + w < MAXJ) s = __ffma2_rn(make_float2(ce[w], ce[w]), a[q * 4 + w], s);
+                }
+                float2 *o = reinterpret_cast<float2 *>(os + lps[e] * OLD + 2 * lane);
+                float2 ov = *o;
+                ov.x += s.x;
+                ov.y += s.y;
+                *o = ov;
+            }
+        }
+        __syncthreads();  // the tile holds the finished values of this range's points
+#pragma unroll 8
+        for (int u = 0; u < kRangePts * NC / 256; u++) {
+            const int idx = t + u * 256;
+            const int lp = idx % kRangePts, c = idx / kRangePts;
+            if (lp < npt && n0 + c < ncol) out[(long)(n0 + c) * ldo + gps[lp]] = os[lp * OLD + c];
+        }
+        if (!alpha_next) continue;
+        // projection of the finished tile for the next degree, as k_nl_project_range
+        for (int it = warp; it < ni; it += 8) {
+            const int2 row = item_row[ib + it];
+            const int e0 = item_e0[ib + it] - eb, e1 = item_e0[ib + it + 1] - eb;
+            float2 acc[MAXJ];
+#pragma unroll
+            for (int j = 0; j < MAXJ; j++) acc[j] = make_float2(0.f, 0.f);
+#pragma unroll 2
+            for (int e = e0; e < e1; e++) {
+                const float2 xv = *reinterpret_cast<const float2 *>(os + lps[e] * OLD + 2 * lane);
+                const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
+#pragma unroll
+                for (int q = 0; q < MAXJP / 4; q++) {
+                    const float4 c4 = cv[q];
+                    const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                    for (int w = 0; w < 4; w++)
+                        if (q * 4 + w < MAXJ)
+                            acc[q * 4 + w] = __ffma2_rn(make_float2(ce[w], ce[w]), xv, acc[q * 4 + w]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < MAXJ; j++) {
+                if (j < row.y) {
+                    const float sj = dV * gamma[row.x + j];
+                    float *dst = alpha_next + (long)(row.x + j) * lda + c0;
+                    if (c0 + 1 < ncol)
+                        atomicAdd(reinterpret_cast<float2 *>(dst),
+                                  make_float2(sj * acc[j].x, sj * acc[j].y));
+                    else if (c0 < ncol)
+                        atomicAdd(dst, sj * acc[j].x);
+                }
+            }
+        }
+    }
+}
+
 // Apply: one thread per covered grid point, looping over column blocks of CB; alpha rows are
 // read as vectors (VW elements per load, broadcast across the warp when neighbouring points
 // share an atom).
@@ -845,6 +978,42 @@ template int launch_nonlocal_project<double>(sgpu_ctx *, int, const double *, lo
                                              long, cudaStream_t);
 template int launch_nonlocal_project<float>(sgpu_ctx *, int, const float *, long, float *, long,
                                             cudaStream_t);
+int launch_nonlocal_apply_project(sgpu_ctx *ctx, int ncol, const float *alpha, long lda,
+                                  double scale, float *out, long ldo, float *alpha_next,
+                                  cudaStream_t st)
+{
+    const Nonlocal &nl = ctx->nl;
+    if (!ctx->has_nl || nl.ncov == 0 || ncol <= 0) return SGPU_OK;
+    if (nl.nrange == 0) {
+        set_error("nonlocal: the fused apply needs the range tables (none built)");
+        return SGPU_ERR_STATE;
+    }
+    const size_t rsm = sizeof(float) * ((size_t)nl.max_range_ent * nl.range_jp +
+                                        (size_t)kRangePts * 66) +
+                       sizeof(int) * ((size_t)nl.max_range_ent + kRangePts);
+    ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
+#define SGPU_FAPPLY(MJ)                                                                      \
+    {                                                                                        \
+        auto kern = k_nl_apply_project_range<MJ>;                                            \
+        SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                           (int)rsm));                                       \
+        kern<<<nl.nrange, 256, rsm, st>>>(nl.rng_pt0, nl.rng_ent0, nl.rng_item0, nl.item_e0, \
+                                          nl.item_wsplit, nl.item_row, nl.pe_lp, nl.pe_chi32, \
+                                          nl.cov_pt, nl.gamma32, ncol, alpha, lda,           \
+                                          (float)scale, out, ldo, alpha_next,                \
+                                          (float)ctx->dV);                                   \
+    }
+    if (nl.range_jp == 12)
+        SGPU_FAPPLY(9)
+    else if (nl.range_jp == 20)
+        SGPU_FAPPLY(18)
+    else
+        SGPU_FAPPLY(32)
+#undef SGPU_FAPPLY
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
 template int launch_nonlocal_apply<double>(sgpu_ctx *, int, const double *, long, double,
                                            double *, long, cudaStream_t);
 template int launch_nonlocal_apply<float>(sgpu_ctx *, int, const float *, long, double, float *,

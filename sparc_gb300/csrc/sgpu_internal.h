@@ -149,7 +149,7 @@ struct sgpu_ctx {
     bool has_nl = false;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
-    sgpu::Workspace ws[12];    // grow-only scratch slots (see enum WsSlot)
+    sgpu::Workspace ws[13];    // grow-only scratch slots (see enum WsSlot)
     sgpu::MixState *mix = nullptr;
     sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)
     sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
@@ -159,6 +159,9 @@ struct sgpu_ctx {
                                // 2 per point with the Chi values hoisted, 3 dense per chunk,
                                // 4 per range with the output tile in shared memory
     int nl_project_variant = 0;  // FP32 projection: 0 per image segment, 1 per point range
+    bool nl_fuse = false;  // FP32 filter: project each new iterate inside the range apply that
+                           // finishes it (one projection launch per filter, not per degree)
+    double tune_fused_ms = 0.0;  // last timing of the fused apply + projection
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int *kstatus = nullptr;    // device word: bits set by kernel waits that ran out
@@ -179,7 +182,7 @@ namespace sgpu {
 
 enum WsSlot {
     WS_STAGE_A = 0, WS_STAGE_B, WS_STAGE_C, WS_ALPHA, WS_MISC, WS_EIG, WS_POIS, WS_MIX,
-    WS_RED, WS_RHS, WS_SCF, WS_SCF2
+    WS_RED, WS_RHS, WS_SCF, WS_SCF2, WS_ALPHA2
 };
 
 // grow-only device scratch
@@ -230,6 +233,11 @@ int launch_gradient(sgpu_ctx *ctx, int ncol, const double *x, long ldx, double *
 template <typename T>
 int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, double scale,
                           T *out, long ldo, cudaStream_t st);
+// the range apply of alpha into out with the projection of the finished out fused:
+// alpha_next (zeroed by the caller; may be null) += dV * Gamma * Chi^T out
+int launch_nonlocal_apply_project(sgpu_ctx *ctx, int ncol, const float *alpha, long lda,
+                                  double scale, float *out, long ldo, float *alpha_next,
+                                  cudaStream_t st);
 int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double *gamma,
                     int nimg, const int *img_atom, const int *img_ndc, const int *grid_pos,
                     const double *chi);
@@ -238,7 +246,10 @@ void nonlocal_free(Nonlocal &nl);
 // ---- Hamiltonian and filter (chefsi.cu)
 template <typename T>
 int hamiltonian_dev(sgpu_ctx *ctx, int spin, int ncol, double c, const T *x, long ldx, T *hx,
-                    long ldh, double s1, double s2, const T *z, long ldz, cudaStream_t st);
+                    long ldh, double s1, double s2, const T *z, long ldz, cudaStream_t st,
+                    const T *alpha_in = nullptr, T *alpha_out = nullptr);
+// whether the FP32 filter carries the projections across degrees (fused range apply)
+bool filter_fuses_projection(sgpu_ctx *ctx);
 template <typename T>
 int chebyshev_dev(sgpu_ctx *ctx, int spin, T *X, long ldx, T *Y, long ldy, int ncol, int m,
                   double a, double b, double a0, cudaStream_t st);

@@ -273,3 +273,38 @@ def test_bounded_wait_reports_and_context_stays_usable(gpu_available):
         outs.append(Y)
     np.testing.assert_array_equal(outs[0], outs[1])
     assert ctx.kernel_status() == 0
+
+
+@pytest.mark.parametrize("lmax,m", [(2, 20), (3, 7), (2, 1), (2, 2)])
+def test_fp32_filter_with_carried_projections(gpu_available, lmax, m):
+    """Nonlocal projections carried across filter degrees (each degree's range apply also
+    projects the iterate it finishes): the FP32 filter matches the FP64 oracle within the FP32
+    filter tolerance, and the filter that launches the range apply and the range projection
+    separately to FP32 rounding (the two sum the projections in other atomic orders).
+    67 columns: two column groups, the second ragged, an odd last pair."""
+    shape = (40, 36, 30)
+    rng = np.random.default_rng(77 + lmax)
+    h = (0.41, 0.37, 0.45)
+    grid = dict(Nx=shape[0], Ny=shape[1], Nz=shape[2], FDn=6, cx=fd_d2_coeffs(6, h[0]),
+                cy=fd_d2_coeffs(6, h[1]), cz=fd_d2_coeffs(6, h[2]), dV=h[0] * h[1] * h[2])
+    Nd = shape[0] * shape[1] * shape[2]
+    veff = rng.normal(0.0, 1.0, Nd)
+    nl = synthetic_nonlocal(rng, shape, 0.4, natom=9, rc=2.4, lmax=lmax)
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    x = rng.uniform(-1, 1, (67, Nd))
+    ctx.set_nonlocal_apply_variant(4)
+    ctx.set_nonlocal_project_variant(1)
+    outs = {}
+    for fuse in (False, True):
+        ctx.set_nonlocal_fuse(fuse)
+        assert ctx.nonlocal_fuse()[0] == fuse
+        X = x.astype(np.float32); Y = np.zeros_like(X)
+        ctx.ChebyshevFiltering_f32(X, Y, m, 0.5, 50.0, -1.0)
+        outs[fuse] = (X.astype(np.float64), Y.astype(np.float64))
+    Xo, Yo = o.chebyshev(veff, m, 0.5, 50.0, -1.0, x)
+    for fuse in (False, True):
+        assert rel_err(outs[fuse][1], Yo) < TOL32_FILTER, fuse
+        assert rel_err(outs[fuse][0], Xo) < TOL32_FILTER, fuse
+    assert rel_err(outs[True][1], outs[False][1]) < 1e-5
+    assert rel_err(outs[True][0], outs[False][0]) < 1e-5

@@ -191,10 +191,18 @@ def test_lanczos_bounds(gpu_available):
     assert abs(lo2 - emin) < 1e-6 and abs(hi2 - emax) < 1e-6 * abs(emax)
 
 
-@pytest.mark.parametrize("precision", [64, 32])
-def test_scf_matches_reference_program(gpu_available, precision):
+@pytest.mark.parametrize("precision,carried", [(64, False), (32, False), (32, True)])
+def test_scf_matches_reference_program(gpu_available, precision, carried):
+    """The SCF against the reference program's run; (32, True): the FP32 filter degrees with
+    the nonlocal projections carried across degrees by the fused range apply."""
     d, grid, nl, ref = load_scf()
     ctx = make_ctx(grid, nl)
+    if carried:  # fixed forms: the SCF then skips its own tuning
+        ctx.set_stencil_variant(6)
+        ctx.set_nonlocal_apply_variant(4)
+        ctx.set_nonlocal_project_variant(1)
+        ctx.set_nonlocal_fuse(True)
+        assert ctx.nonlocal_fuse()[0]
     prm = scf_params(sg, d, ref, precision=precision, switch=1e-4)
     res, rho, lam, occ = ctx.scf(prm, d["b"], d["rho0"], d["rho_core"])
     n_atom = int(d["n_atom"])
