@@ -63,8 +63,9 @@ def parse():
                     help="use this FP32 stencil variant instead of the tuned one (profiling)")
     ap.add_argument("--nl-apply", type=int, default=None,
                     help="use this nonlocal apply form instead of the tuned one (profiling)")
-    ap.add_argument("--nl-fuse", type=int, default=None, choices=[0, 1],
-                    help="force the projections carried across filter degrees on or off")
+    ap.add_argument("--nl-fuse", type=int, default=None, choices=[0, 2, 4],
+                    help="force the projections carried across filter degrees off (0) or on "
+                         "with 2 or 4 columns per thread")
     ap.add_argument("--nl-project", type=int, default=None,
                     help="use this FP32 projection form instead of the tuned one (profiling)")
     return ap.parse_args()
@@ -474,9 +475,9 @@ def main():
     if args.nl_project is not None:
         ctx.set_nonlocal_project_variant(args.nl_project)
     if args.nl_fuse is not None:
-        ctx.set_nonlocal_fuse(args.nl_fuse)
+        ctx.set_nonlocal_fuse(args.nl_fuse != 0, args.nl_fuse or None)
     forms = ctx.variants()
-    fuse_on, fuse_ms = ctx.nonlocal_fuse()
+    fuse_on, fuse_cpl, fuse_ms = ctx.nonlocal_fuse()
     kernel_name = ["k_stencil_f32x2<32x16>", "k_stencil_f32_b22<32x16>",
                    "k_stencil_f32_b22<64x8>", "k_stencil_f32x2<64x8>",
                    "k_stencil_f32_b22<32x16, 3 blocks/SM>",
@@ -652,7 +653,8 @@ def main():
                            "autotune_ms": {k: [round(float(v), 4) for v in vs]
                                            for k, vs in ctx.tuning().items()},
                            "projection_carried": fuse_on,
-                           "fused_apply_project_ms": round(fuse_ms, 4)}},
+                           "fused_columns_per_thread": fuse_cpl,
+                           "fused_apply_project_ms": [round(v, 4) for v in fuse_ms]}},
             "roofline": {"bound": "hbm", "kernel": kernel_name,
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_src,

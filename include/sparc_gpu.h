@@ -484,19 +484,21 @@ int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
  * partial sums atomically), so results agree to FP32 rounding. */
 int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
 
-/* FP32 filter with the projections carried across degrees (1) or not (0). When on, every
- * degree's nonlocal apply is the range form with the projection of the iterate it finishes
- * fused in (alpha of the next degree is formed from the finished values while they are in
- * shared memory), so a filter of degree m launches one projection instead of m. The apply
- * results are bit-identical to form 4; the projections agree with the separate ones to FP32
- * rounding (atomic summation order). Needs the range tables of FP32 projector sets; off
- * otherwise. sgpu_autotune turns it on when the fused launch beats the fastest separate
- * apply plus projection. */
-int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int on);
+/* FP32 filter with the projections carried across degrees (mode 1, 2 or 4) or not (0). When
+ * on, every degree's nonlocal apply is the range form with the projection of the iterate it
+ * finishes fused in (alpha of the next degree is formed from the finished values while they
+ * are in shared memory), so a filter of degree m launches one projection instead of m. The
+ * fused kernel has two forms, 2 or 4 columns per thread (mode 2 or 4; mode 1 keeps the
+ * current one). The apply results are bit-identical to form 4 in both; the projections agree
+ * with the separate ones to FP32 rounding (atomic summation order). Needs the range tables of
+ * FP32 projector sets; off otherwise. sgpu_autotune times both forms and turns fusion on when
+ * the faster beats the fastest separate apply plus projection. */
+int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int mode);
 
-/* Whether the FP32 filter fuses the projections (*on) and the last tuned time of one fused
- * launch (*fused_ms, 0 before tuning); either pointer may be NULL. */
-int sgpu_get_nonlocal_fuse(sgpu_ctx *ctx, int *on, double *fused_ms);
+/* The fused form in use (*mode: 0 off, else 2 or 4 columns per thread) and the last tuned
+ * times of one fused launch of each form (fused_ms[2]: 2 and 4 columns, 0 before tuning);
+ * either pointer may be NULL. */
+int sgpu_get_nonlocal_fuse(sgpu_ctx *ctx, int *mode, double *fused_ms);
 
 /* The kernel forms in use (set by sgpu_autotune or the sgpu_set_*_variant calls); any
  * pointer may be NULL. */

@@ -563,16 +563,19 @@ class Context:
         _check(lib().sgpu_kernel_status(self._h, ctypes.byref(st)))
         return int(st.value)
 
-    def set_nonlocal_fuse(self, on):
-        """Carry the nonlocal projections across filter degrees (fused range apply) or not."""
-        _check(lib().sgpu_set_nonlocal_fuse(self._h, 1 if on else 0))
+    def set_nonlocal_fuse(self, on, cpl=None):
+        """Carry the nonlocal projections across filter degrees (fused range apply) or not;
+        cpl = 2 or 4 fixes the fused kernel's columns per thread."""
+        mode = 0 if not on else (int(cpl) if cpl else 1)
+        _check(lib().sgpu_set_nonlocal_fuse(self._h, mode))
 
     def nonlocal_fuse(self):
-        """(on, ms of one fused launch at the last tuning)."""
-        on = ctypes.c_int()
-        ms = ctypes.c_double()
-        _check(lib().sgpu_get_nonlocal_fuse(self._h, ctypes.byref(on), ctypes.byref(ms)))
-        return bool(on.value), float(ms.value)
+        """(on, columns per thread of the fused form or 0, [ms of one fused launch with 2 and
+        4 columns per thread at the last tuning])."""
+        mode = ctypes.c_int()
+        ms = (ctypes.c_double * 2)()
+        _check(lib().sgpu_get_nonlocal_fuse(self._h, ctypes.byref(mode), ms))
+        return mode.value != 0, int(mode.value), [float(ms[0]), float(ms[1])]
 
     def check_wait_bound(self):
         """Run the bounded-wait diagnostic; returns the status word it left (2 when a wait

@@ -129,28 +129,36 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
             const size_t abytes = sizeof(float) * (size_t)ctx->nl.ntot * lda;
             if (rc == SGPU_OK && ctx->nl.nrange > 0) {
                 if (cudaMallocAsync(&anext, abytes, st) != cudaSuccess) rc = SGPU_ERR_CUDA;
-                float t = 0.f, tmin = 1e30f;
-                for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
-                    if (cudaEventRecord(ctx->ev0, st) != cudaSuccess ||
-                        cudaMemsetAsync(anext, 0, abytes, st) != cudaSuccess) {
-                        rc = SGPU_ERR_CUDA;
-                        break;
+                float fbest = 1e30f;
+                int cbest = 2;
+                for (int cpl = 2; cpl <= 4 && rc == SGPU_OK; cpl += 2) {  // columns per lane
+                    ctx->nl_fuse_cpl = cpl;
+                    float t = 0.f, tmin = 1e30f;
+                    for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
+                        if (cudaEventRecord(ctx->ev0, st) != cudaSuccess ||
+                            cudaMemsetAsync(anext, 0, abytes, st) != cudaSuccess) {
+                            rc = SGPU_ERR_CUDA;
+                            break;
+                        }
+                        if ((rc = launch_nonlocal_apply_project(ctx, ncol, alpha, lda, 1.0, Y,
+                                                                Nd, anext, st)) != SGPU_OK)
+                            break;
+                        if (cudaEventRecord(ctx->ev1, st) != cudaSuccess ||
+                            cudaEventSynchronize(ctx->ev1) != cudaSuccess ||
+                            cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) != cudaSuccess) {
+                            rc = SGPU_ERR_CUDA;
+                            break;
+                        }
+                        if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
                     }
-                    if ((rc = launch_nonlocal_apply_project(ctx, ncol, alpha, lda, 1.0, Y, Nd,
-                                                            anext, st)) != SGPU_OK)
-                        break;
-                    if (cudaEventRecord(ctx->ev1, st) != cudaSuccess ||
-                        cudaEventSynchronize(ctx->ev1) != cudaSuccess ||
-                        cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) != cudaSuccess) {
-                        rc = SGPU_ERR_CUDA;
-                        break;
-                    }
-                    if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
+                    if (rc == SGPU_OK) ctx->tune_fused_cpl_ms[cpl / 2 - 1] = tmin;
+                    if (rc == SGPU_OK && tmin < fbest) { fbest = tmin; cbest = cpl; }
                 }
+                ctx->nl_fuse_cpl = cbest;
                 if (rc == SGPU_OK) {
-                    ctx->tune_fused_ms = tmin;
-                    ctx->nl_fuse = tmin < ctx->tune_apply_ms[ctx->nl_apply_variant] +
-                                              ctx->tune_project_ms[ctx->nl_project_variant];
+                    ctx->tune_fused_ms = fbest;
+                    ctx->nl_fuse = fbest < ctx->tune_apply_ms[ctx->nl_apply_variant] +
+                                               ctx->tune_project_ms[ctx->nl_project_variant];
                 }
                 if (anext) cudaFreeAsync(anext, st);
             }
@@ -202,24 +210,28 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant)
     return SGPU_OK;
 }
 
-int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int on)
+int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int mode)
 {
-    if (!ctx || (on != 0 && on != 1)) {
-        set_error("sgpu_set_nonlocal_fuse: need a context and on = 0 or 1");
+    if (!ctx || (mode != 0 && mode != 1 && mode != 2 && mode != 4)) {
+        set_error("sgpu_set_nonlocal_fuse: need a context and mode 0, 1, 2 or 4");
         return SGPU_ERR_ARG;
     }
-    ctx->nl_fuse = on == 1;
+    ctx->nl_fuse = mode != 0;
+    if (mode == 2 || mode == 4) ctx->nl_fuse_cpl = mode;
     return SGPU_OK;
 }
 
-int sgpu_get_nonlocal_fuse(sgpu_ctx *ctx, int *on, double *fused_ms)
+int sgpu_get_nonlocal_fuse(sgpu_ctx *ctx, int *mode, double *fused_ms)
 {
     if (!ctx) {
         set_error("sgpu_get_nonlocal_fuse: null context");
         return SGPU_ERR_ARG;
     }
-    if (on) *on = filter_fuses_projection(ctx) ? 1 : 0;
-    if (fused_ms) *fused_ms = ctx->tune_fused_ms;
+    if (mode) *mode = filter_fuses_projection(ctx) ? ctx->nl_fuse_cpl : 0;
+    if (fused_ms) {
+        fused_ms[0] = ctx->tune_fused_cpl_ms[0];
+        fused_ms[1] = ctx->tune_fused_cpl_ms[1];
+    }
     return SGPU_OK;
 }
 

@@ -343,16 +343,27 @@ __global__ void __launch_bounds__(256, 4)
 // Range apply with the next projection fused (FP32). The Chebyshev filter projects each new
 // iterate right after the apply that finishes it, and that apply already holds the finished
 // values of its range's covered points in shared memory, with the range's Chi rows staged. So
-// per group of 64 columns this kernel: gathers the output tile, adds scale * sum_j Chi_j
-// alpha_j exactly as k_nl_apply_range does (lane l now owns columns 2l, 2l+1, the tile rows
-// are padded to 66 floats; the additions per element are the same IEEE operations in the same
-// item order, so the output is bit-identical), writes the tile back, and then, as
-// k_nl_project_range does on a gathered tile, accumulates dV * Gamma * Chi^T tile per work
-// item and adds it atomically into alpha_next (zeroed by the caller). Ranges partition the
-// covered points, so a range's tile is final once its own apply is done. The separate
-// projection of the next degree, and its read of every covered element, disappear.
-template <int MAXJ>
-__global__ void __launch_bounds__(256, MAXJ <= 9 ? 4 : 2)  // larger sets: registers, no spills
+// per group of 64 columns this kernel gathers the output tile, adds scale * sum_j Chi_j
+// alpha_j, writes the tile back, and then accumulates dV * Gamma * Chi^T tile per work item
+// and adds it atomically into alpha_next (zeroed by the caller). Ranges partition the covered
+// points, so a range's tile is final once its own apply is done; the separate projection of
+// the next degree, and its read of every covered element, disappear.
+//   apply: warp w owns the tile rows of points [w kRangeWarpPts, (w + 1) kRangeWarpPts) as in
+//     k_nl_apply_range; per element the same IEEE operations in the same item order, so the
+//     output is bit-identical to k_nl_apply_range.
+//   projection: per work item the entries are summed in order as in k_nl_project_range (the
+//     same per-item partial sums), then added atomically.
+// CPL = columns per lane. CPL 2: lane l owns columns 2l, 2l+1 and a warp takes one entry at a
+// time (apply) or one work item (projection). CPL 4: lane l owns columns 4(l % 16) .. + 3, so
+// each staged Chi value serves four columns and the tile moves in 16-byte pieces; the two
+// half-warps take alternate entries of an item (distinct points of one image) in the apply and
+// separate work items in the projection. The tuner times both.
+// The range's work-item table (entry split by owning warp, projector rows, entry bounds) is
+// staged in shared memory once, so an item costs the warps no dependent global loads.
+constexpr int kItemFields = kRangeWarps + 5;  // wsplit[kRangeWarps + 1], row, count, e0, e1
+
+template <int MAXJ, int CPL>
+__global__ void __launch_bounds__(256, CPL == 2 ? (MAXJ <= 9 ? 4 : 2) : (MAXJ <= 9 ? 3 : 2))
     k_nl_apply_project_range(const int *__restrict__ rng_pt0, const int *__restrict__ rng_ent0,
                              const int *__restrict__ rng_item0, const int *__restrict__ item_e0,
                              const int *__restrict__ item_wsplit, const int2 *__restrict__ item_row,
@@ -362,7 +373,8 @@ __global__ void __launch_bounds__(256, MAXJ <= 9 ? 4 : 2)  // larger sets: regis
                              float *__restrict__ out, long ldo, float *__restrict__ alpha_next,
                              float dV)
 {
-    constexpr int NC = 64, OLD = NC + 2;             // columns per group, padded tile row
+    static_assert(CPL == 2 || CPL == 4, "two or four columns per lane");
+    constexpr int NC = 64, OLD = NC + CPL;  // tile row: 64 columns + padding
     constexpr int MAXJP = (MAXJ + 3) / 4 * 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *cs = reinterpret_cast<float *>(smem_raw);  // [entries][MAXJP]
@@ -373,10 +385,23 @@ __global__ void __launch_bounds__(256, MAXJ <= 9 ? 4 : 2)  // larger sets: regis
     float *os = cs + (size_t)ne * MAXJP;                          // [kRangePts][OLD]
     int *lps = reinterpret_cast<int *>(os + kRangePts * OLD);     // [entries]
     int *gps = lps + ne;                                          // [kRangePts]
+    int *its = gps + kRangePts;                                   // [items][kItemFields]
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // CPL 2: every lane on the entry, columns 2 lane, 2 lane + 1; CPL 4: half-warps
+    const int half = CPL == 4 ? lane >> 4 : 0;
+    const int q = CPL == 4 ? lane & 15 : lane;
 
     for (int i = t; i < npt; i += 256) gps[i] = cov_pt[p0 + i];
     for (int i = t; i < ne; i += 256) lps[i] = pe_lp[eb + i];
+    for (int i = t; i < ni * kItemFields; i += 256) {
+        const int it = i / kItemFields, f = i - it * kItemFields;
+        int v;
+        if (f <= kRangeWarps) v = item_wsplit[(long)(ib + it) * (kRangeWarps + 1) + f] - eb;
+        else if (f == kRangeWarps + 1) v = item_row[ib + it].x;
+        else if (f == kRangeWarps + 2) v = item_row[ib + it].y;
+        else v = item_e0[ib + it + (f - kRangeWarps - 3)] - eb;
+        its[i] = v;
+    }
     {
         const float4 *src = reinterpret_cast<const float4 *>(pe_chi + (long)eb * MAXJP);
         float4 *dst = reinterpret_cast<float4 *>(cs);
@@ -385,47 +410,67 @@ __global__ void __launch_bounds__(256, MAXJ <= 9 ? 4 : 2)  // larger sets: regis
     const int ngroup = (ncol + NC - 1) / NC;
     for (int gi = 0; gi < ngroup; gi++) {
         const int n0 = ((gi + r) % ngroup) * NC;
-        const int c0 = n0 + 2 * lane;
+        const int c0 = n0 + CPL * q;  // this lane's first column
         __syncthreads();  // staging done / previous tile written back and projected
         gather_tile<OLD, NC>(out, ldo, n0, ncol, gps, npt, os);
         __syncthreads();
-        // apply: warp w owns the tile rows of points [w * kRangeWarpPts, (w + 1) * kRangeWarpPts)
         for (int it = 0; it < ni; it++) {
-            const int *ws = item_wsplit + (long)(ib + it) * (kRangeWarps + 1);
-            const int e0 = ws[warp] - eb, e1 = ws[warp + 1] - eb;
+            const int *wi = its + it * kItemFields;
+            const int e0 = wi[warp], e1 = wi[warp + 1];
             if (e0 == e1) continue;
-            const int2 row = item_row[ib + it];
-            float2 a[MAXJ];  // scale * alpha of columns (2 lane, 2 lane + 1)
+            const int rx = wi[kRangeWarps + 1], ry = wi[kRangeWarps + 2];
+            float2 alo[MAXJ], ahi[MAXJ];  // scale * alpha: columns (c0, c0+1), (c0+2, c0+3)
 #pragma unroll
             for (int j = 0; j < MAXJ; j++) {
-                a[j] = make_float2(0.f, 0.f);
-                if (j < row.y) {
-                    const float *ar = alpha + (long)(row.x + j) * lda;
-                    if (c0 + 1 < ncol) {  // lda and c0 are even: an 8-byte aligned pair
-                        const float2 v = __ldg(reinterpret_cast<const float2 *>(ar + c0));
-                        a[j] = make_float2(scale * v.x, scale * v.y);
-                    } else if (c0 < ncol) {
-                        a[j].x = scale * __ldg(ar + c0);
+                alo[j] = ahi[j] = make_float2(0.f, 0.f);
+                if (j < ry) {
+                    const float *ar = alpha + (long)(rx + j) * lda + c0;
+                    if (c0 + CPL - 1 < ncol) {  // lda and c0 are multiples of CPL: aligned
+                        if constexpr (CPL == 4) {
+                            const float4 v = __ldg(reinterpret_cast<const float4 *>(ar));
+                            alo[j] = make_float2(scale * v.x, scale * v.y);
+                            ahi[j] = make_float2(scale * v.z, scale * v.w);
+                        } else {
+                            const float2 v = __ldg(reinterpret_cast<const float2 *>(ar));
+                            alo[j] = make_float2(scale * v.x, scale * v.y);
+                        }
+                    } else {
+                        if (c0 < ncol) alo[j].x = scale * __ldg(ar);
+                        if (c0 + 1 < ncol) alo[j].y = scale * __ldg(ar + 1);
+                        if (CPL == 4 && c0 + 2 < ncol) ahi[j].x = scale * __ldg(ar + 2);
                     }
                 }
             }
 #pragma unroll 4
-            for (int e = e0; e < e1; e++) {
+            for (int e = e0 + half; e < e1; e += CPL / 2) {
                 const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
-                float2 s = make_float2(0.f, 0.f);
+                float2 slo = make_float2(0.f, 0.f), shi = slo;
 #pragma unroll
-                for (int q = 0; q < MAXJP / 4; q++) {
-                    const float4 c4 = cv[q];
+                for (int u = 0; u < MAXJP / 4; u++) {
+                    const float4 c4 = cv[u];
                     const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
                     for (int w = 0; w < 4; w++)
-                        if (q * 4 + w < MAXJ) s = __ffma2_rn(make_float2(ce[w], ce[w]), a[q * 4 + w], s);
+                        if (u * 4 + w < MAXJ) {
+                            slo = __ffma2_rn(make_float2(ce[w], ce[w]), alo[u * 4 + w], slo);
+                            if constexpr (CPL == 4)
+                                shi = __ffma2_rn(make_float2(ce[w], ce[w]), ahi[u * 4 + w], shi);
+                        }
                 }
-                float2 *o = reinterpret_cast<float2 *>(os + lps[e] * OLD + 2 * lane);
-                float2 ov = *o;
-                ov.x += s.x;
-                ov.y += s.y;
-                *o = ov;
+                float *orow = os + lps[e] * OLD + CPL * q;
+                if constexpr (CPL == 4) {
+                    float4 ov = *reinterpret_cast<float4 *>(orow);
+                    ov.x += slo.x;
+                    ov.y += slo.y;
+                    ov.z += shi.x;
+                    ov.w += shi.y;
+                    *reinterpret_cast<float4 *>(orow) = ov;
+                } else {
+                    float2 ov = *reinterpret_cast<float2 *>(orow);
+                    ov.x += slo.x;
+                    ov.y += slo.y;
+                    *reinterpret_cast<float2 *>(orow) = ov;
+                }
             }
         }
         __syncthreads();  // the tile holds the finished values of this range's points
@@ -436,37 +481,57 @@ __global__ void __launch_bounds__(256, MAXJ <= 9 ? 4 : 2)  // larger sets: regis
             if (lp < npt && n0 + c < ncol) out[(long)(n0 + c) * ldo + gps[lp]] = os[lp * OLD + c];
         }
         if (!alpha_next) continue;
-        // projection of the finished tile for the next degree, as k_nl_project_range
-        for (int it = warp; it < ni; it += 8) {
-            const int2 row = item_row[ib + it];
-            const int e0 = item_e0[ib + it] - eb, e1 = item_e0[ib + it + 1] - eb;
-            float2 acc[MAXJ];
+        // work items in turn: one per warp (CPL 2) or one per half-warp (CPL 4)
+        for (int it = warp * (CPL / 2) + half; it < ni; it += kRangeWarps * (CPL / 2)) {
+            const int *wi = its + it * kItemFields;
+            const int rx = wi[kRangeWarps + 1], ry = wi[kRangeWarps + 2];
+            const int e0 = wi[kRangeWarps + 3], e1 = wi[kRangeWarps + 4];
+            float2 plo[MAXJ], phi[MAXJ];
 #pragma unroll
-            for (int j = 0; j < MAXJ; j++) acc[j] = make_float2(0.f, 0.f);
+            for (int j = 0; j < MAXJ; j++) plo[j] = phi[j] = make_float2(0.f, 0.f);
 #pragma unroll 2
             for (int e = e0; e < e1; e++) {
-                const float2 xv = *reinterpret_cast<const float2 *>(os + lps[e] * OLD + 2 * lane);
+                const float *xrow = os + lps[e] * OLD + CPL * q;
+                float2 xlo, xhi = make_float2(0.f, 0.f);
+                if constexpr (CPL == 4) {
+                    const float4 xv = *reinterpret_cast<const float4 *>(xrow);
+                    xlo = make_float2(xv.x, xv.y);
+                    xhi = make_float2(xv.z, xv.w);
+                } else {
+                    xlo = *reinterpret_cast<const float2 *>(xrow);
+                }
                 const float4 *cv = reinterpret_cast<const float4 *>(cs + (size_t)e * MAXJP);
 #pragma unroll
-                for (int q = 0; q < MAXJP / 4; q++) {
-                    const float4 c4 = cv[q];
+                for (int u = 0; u < MAXJP / 4; u++) {
+                    const float4 c4 = cv[u];
                     const float ce[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
                     for (int w = 0; w < 4; w++)
-                        if (q * 4 + w < MAXJ)
-                            acc[q * 4 + w] = __ffma2_rn(make_float2(ce[w], ce[w]), xv, acc[q * 4 + w]);
+                        if (u * 4 + w < MAXJ) {
+                            plo[u * 4 + w] = __ffma2_rn(make_float2(ce[w], ce[w]), xlo, plo[u * 4 + w]);
+                            if constexpr (CPL == 4)
+                                phi[u * 4 + w] = __ffma2_rn(make_float2(ce[w], ce[w]), xhi, phi[u * 4 + w]);
+                        }
                 }
             }
 #pragma unroll
             for (int j = 0; j < MAXJ; j++) {
-                if (j < row.y) {
-                    const float sj = dV * gamma[row.x + j];
-                    float *dst = alpha_next + (long)(row.x + j) * lda + c0;
-                    if (c0 + 1 < ncol)
-                        atomicAdd(reinterpret_cast<float2 *>(dst),
-                                  make_float2(sj * acc[j].x, sj * acc[j].y));
-                    else if (c0 < ncol)
-                        atomicAdd(dst, sj * acc[j].x);
+                if (j < ry) {
+                    const float sj = dV * gamma[rx + j];
+                    float *dst = alpha_next + (long)(rx + j) * lda + c0;
+                    if (c0 + CPL - 1 < ncol) {
+                        if constexpr (CPL == 4)
+                            atomicAdd(reinterpret_cast<float4 *>(dst),
+                                      make_float4(sj * plo[j].x, sj * plo[j].y, sj * phi[j].x,
+                                                  sj * phi[j].y));
+                        else
+                            atomicAdd(reinterpret_cast<float2 *>(dst),
+                                      make_float2(sj * plo[j].x, sj * plo[j].y));
+                    } else {
+                        if (c0 < ncol) atomicAdd(dst, sj * plo[j].x);
+                        if (c0 + 1 < ncol) atomicAdd(dst + 1, sj * plo[j].y);
+                        if (CPL == 4 && c0 + 2 < ncol) atomicAdd(dst + 2, sj * phi[j].x);
+                    }
                 }
             }
         }
@@ -988,13 +1053,15 @@ int launch_nonlocal_apply_project(sgpu_ctx *ctx, int ncol, const float *alpha, l
         set_error("nonlocal: the fused apply needs the range tables (none built)");
         return SGPU_ERR_STATE;
     }
+    const int cpl = ctx->nl_fuse_cpl == 4 ? 4 : 2;
     const size_t rsm = sizeof(float) * ((size_t)nl.max_range_ent * nl.range_jp +
-                                        (size_t)kRangePts * 66) +
-                       sizeof(int) * ((size_t)nl.max_range_ent + kRangePts);
+                                        (size_t)kRangePts * (64 + cpl)) +
+                       sizeof(int) * ((size_t)nl.max_range_ent + kRangePts +
+                                      (size_t)nl.max_range_items * kItemFields);
     ProfScope ps(ctx, SGPU_KERNEL_NL_APPLY, st);
-#define SGPU_FAPPLY(MJ)                                                                      \
+#define SGPU_FAPPLY(MJ, CPL)                                                                 \
     {                                                                                        \
-        auto kern = k_nl_apply_project_range<MJ>;                                            \
+        auto kern = k_nl_apply_project_range<MJ, CPL>;                                       \
         SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                            (int)rsm));                                       \
         kern<<<nl.nrange, 256, rsm, st>>>(nl.rng_pt0, nl.rng_ent0, nl.rng_item0, nl.item_e0, \
@@ -1003,12 +1070,21 @@ int launch_nonlocal_apply_project(sgpu_ctx *ctx, int ncol, const float *alpha, l
                                           (float)scale, out, ldo, alpha_next,                \
                                           (float)ctx->dV);                                   \
     }
-    if (nl.range_jp == 12)
-        SGPU_FAPPLY(9)
-    else if (nl.range_jp == 20)
-        SGPU_FAPPLY(18)
-    else
-        SGPU_FAPPLY(32)
+    if (cpl == 4) {
+        if (nl.range_jp == 12)
+            SGPU_FAPPLY(9, 4)
+        else if (nl.range_jp == 20)
+            SGPU_FAPPLY(18, 4)
+        else
+            SGPU_FAPPLY(32, 4)
+    } else {
+        if (nl.range_jp == 12)
+            SGPU_FAPPLY(9, 2)
+        else if (nl.range_jp == 20)
+            SGPU_FAPPLY(18, 2)
+        else
+            SGPU_FAPPLY(32, 2)
+    }
 #undef SGPU_FAPPLY
     SGPU_CUDA_TRY(cudaGetLastError());
     return SGPU_OK;
@@ -1198,6 +1274,8 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
             }
             rng_pt0.push_back(p);
             rng_ent0.push_back((int)pe_lp.size());
+            nl.max_range_items = std::max(nl.max_range_items,
+                                          (int)item_row.size() - rng_item0.back());
             rng_item0.push_back((int)item_row.size());
             nl.max_range_ent = std::max(nl.max_range_ent, ents);
         }

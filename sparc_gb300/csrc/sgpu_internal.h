@@ -86,7 +86,7 @@ struct Nonlocal {
     int *chunk_rows = nullptr;     // alpha rows staged per chunk
     // range projection (FP32): ranges of consecutive covered points, each with its entries
     // regrouped by image into work items of at most kRangeItemEnt entries
-    int nrange = 0, nitem = 0, max_range_ent = 0, range_jp = 0;
+    int nrange = 0, nitem = 0, max_range_ent = 0, range_jp = 0, max_range_items = 0;
     int *rng_pt0 = nullptr;     // nrange + 1: first covered point of each range
     int *rng_ent0 = nullptr;    // nrange + 1: first entry (range order) of each range
     int *rng_item0 = nullptr;   // nrange + 1: first work item of each range
@@ -161,7 +161,9 @@ struct sgpu_ctx {
     int nl_project_variant = 0;  // FP32 projection: 0 per image segment, 1 per point range
     bool nl_fuse = false;  // FP32 filter: project each new iterate inside the range apply that
                            // finishes it (one projection launch per filter, not per degree)
-    double tune_fused_ms = 0.0;  // last timing of the fused apply + projection
+    int nl_fuse_cpl = 2;   // fused apply: columns per lane (2 or 4), chosen by the tuner
+    double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
+    double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int *kstatus = nullptr;    // device word: bits set by kernel waits that ran out

@@ -275,8 +275,9 @@ def test_bounded_wait_reports_and_context_stays_usable(gpu_available):
     assert ctx.kernel_status() == 0
 
 
-@pytest.mark.parametrize("lmax,m", [(2, 20), (3, 7), (2, 1), (2, 2)])
-def test_fp32_filter_with_carried_projections(gpu_available, lmax, m):
+@pytest.mark.parametrize("lmax,m,cpl", [(2, 20, 2), (2, 20, 4), (3, 7, 2), (3, 7, 4), (2, 1, 4),
+                                        (2, 2, 2)])
+def test_fp32_filter_with_carried_projections(gpu_available, lmax, m, cpl):
     """Nonlocal projections carried across filter degrees (each degree's range apply also
     projects the iterate it finishes): the FP32 filter matches the FP64 oracle within the FP32
     filter tolerance, and the filter that launches the range apply and the range projection
@@ -297,8 +298,8 @@ def test_fp32_filter_with_carried_projections(gpu_available, lmax, m):
     ctx.set_nonlocal_project_variant(1)
     outs = {}
     for fuse in (False, True):
-        ctx.set_nonlocal_fuse(fuse)
-        assert ctx.nonlocal_fuse()[0] == fuse
+        ctx.set_nonlocal_fuse(fuse, cpl)
+        assert ctx.nonlocal_fuse()[:2] == (fuse, cpl if fuse else 0)
         X = x.astype(np.float32); Y = np.zeros_like(X)
         ctx.ChebyshevFiltering_f32(X, Y, m, 0.5, 50.0, -1.0)
         outs[fuse] = (X.astype(np.float64), Y.astype(np.float64))

@@ -201,7 +201,7 @@ def test_scf_matches_reference_program(gpu_available, precision, carried):
         ctx.set_stencil_variant(6)
         ctx.set_nonlocal_apply_variant(4)
         ctx.set_nonlocal_project_variant(1)
-        ctx.set_nonlocal_fuse(True)
+        ctx.set_nonlocal_fuse(True, 4)
         assert ctx.nonlocal_fuse()[0]
     prm = scf_params(sg, d, ref, precision=precision, switch=1e-4)
     res, rho, lam, occ = ctx.scf(prm, d["b"], d["rho0"], d["rho_core"])
