@@ -581,28 +581,28 @@ def main():
     mix_gbs = 3 * X.numel() * 4 / (ev_a.elapsed_time(ev_b) / 5 / 1e3) / 1e9
     del Zmix
 
-    # --- e2e: drop-in call with FP64 pinned host arrays (FP32 arithmetic inside)
-    Xh0 = X0[:, :].double().cpu().pin_memory()
-    Xh = torch.empty_like(Xh0).pin_memory()
-    Yh = torch.empty_like(Xh0).pin_memory()
-
-    def step_e2e():
-        Xh.copy_(Xh0)  # host-side reset of the pinned input (outside the device stream)
-        ctx.ChebyshevFiltering(Xh, Yh, M, a, b, a0, precision=sg.SGPU_PREC_FP32)
-
+    # --- e2e: drop-in call with FP64 pinned host arrays (FP32 arithmetic inside). The call
+    # overwrites X, so every step gets its own pinned copy of the input, made before the
+    # timed region: a step times exactly the call (copies in, filter, copies out).
     e2e_steps = max(1, min(args.steps, 3))
+    Xh0 = X0[:, :].double().cpu()
+    Xhs = [Xh0.clone().pin_memory() for _ in range(e2e_steps + 1)]
+    Yh = torch.empty_like(Xh0).pin_memory()
+    del Xh0
+
+    def step_e2e(i):
+        ctx.ChebyshevFiltering(Xhs[i], Yh, M, a, b, a0, precision=sg.SGPU_PREC_FP32)
+
+    barrier()
+    step_e2e(e2e_steps)  # warm-up
     barrier()
     t0 = time.perf_counter()
-    for _ in range(1):
-        step_e2e()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        step_e2e()
+    for i in range(e2e_steps):
+        step_e2e(i)
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_val = world * bytes32 / e2e_s / 1e9
-    del Xh0, Xh, Yh
+    del Xhs, Yh
 
     # --- plain FP64 filter (the FP64 drop-in), device-resident
     fp64 = None

@@ -1,5 +1,6 @@
 // C ABI entry points (include/sparc_gpu.h): context set-up and the reference-shaped hot-path
 // calls, with host-array staging so that the reference's own malloc'ed buffers can be passed.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -240,6 +241,13 @@ int sgpu_destroy(sgpu_ctx *ctx)
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->kstatus) cudaFree(ctx->kstatus);
+    if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in);
+    if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out);
+    for (auto &slot : ctx->pipe_ev)
+        for (auto &e : slot)
+            if (e) cudaEventDestroy(e);
+    if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
+    if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx->mix;
     kpoint_free(ctx);
@@ -356,6 +364,71 @@ int sgpu_Hamiltonian_vectors_mult(sgpu_ctx *ctx, int spin, int ncol, double c, c
     return SGPU_OK;
 }
 
+// Host-array filter, pipelined over column chunks. The filter acts on every column on its own,
+// so the block is cut into chunks that move through three device slots: while chunk i is
+// filtered on the context stream, chunk i+1 is copied in on one copy stream and chunk i-1
+// copied out on another. The host-device copies then hide behind the filter instead of
+// adding to it. Each column's arithmetic is the one of the unchunked call.
+static int filter_pipelined(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y, int ldo,
+                            int ncol, int nc, int m, double a, double b, double a0, bool f32)
+{
+    const long Nd = ctx->Nd;
+    if (!ctx->copy_in) {
+        SGPU_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+        SGPU_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+        for (auto &slot : ctx->pipe_ev)
+            for (auto &e : slot) SGPU_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    // per slot: FP64 X and Y of nc columns, and (FP32) their FP32 images
+    const size_t n64 = (size_t)Nd * nc, per = n64 * (2 * sizeof(double) + (f32 ? 2 * sizeof(float) : 0));
+    char *base = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_STAGE_A, 3 * per, (void **)&base));
+    // the previous call's copies out of these buffers are complete: every call ends synchronised
+    cudaStream_t cs = ctx->stream;
+    const int nchunk = (ncol + nc - 1) / nc;
+    for (int i = 0; i < nchunk; i++) {
+        const int s = i % 3, c0 = i * nc, w = std::min(nc, ncol - c0);
+        double *dX = reinterpret_cast<double *>(base + s * per), *dY = dX + n64;
+        float *fX = reinterpret_cast<float *>(dY + n64), *fY = fX + n64;
+        cudaEvent_t in_done = ctx->pipe_ev[s][0], filtered = ctx->pipe_ev[s][1],
+                    freed = ctx->pipe_ev[s][2];
+        if (i >= 3) SGPU_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_in, freed, 0));
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(dX, sizeof(double) * Nd, X + (long)c0 * ldi,
+                                        sizeof(double) * ldi, sizeof(double) * Nd, w,
+                                        cudaMemcpyHostToDevice, ctx->copy_in));
+        SGPU_CUDA_TRY(cudaEventRecord(in_done, ctx->copy_in));
+        SGPU_CUDA_TRY(cudaStreamWaitEvent(cs, in_done, 0));
+        if (i == 0) SGPU_CUDA_TRY(cudaEventRecord(ctx->ev0, cs));
+        if (f32) {
+            {
+                ProfScope ps(ctx, SGPU_KERNEL_OTHER, cs);
+                SGPU_TRY(convert_cols<double, float>(dX, Nd, fX, Nd, Nd, w, cs));
+            }
+            SGPU_TRY(chebyshev_dev<float>(ctx, spin, fX, Nd, fY, Nd, w, m, a, b, a0, cs));
+            ProfScope ps(ctx, SGPU_KERNEL_OTHER, cs);
+            SGPU_TRY(convert_cols<float, double>(fX, Nd, dX, Nd, Nd, w, cs));
+            SGPU_TRY(convert_cols<float, double>(fY, Nd, dY, Nd, Nd, w, cs));
+            ctx->launches++;
+        } else {
+            SGPU_TRY(chebyshev_dev<double>(ctx, spin, dX, Nd, dY, Nd, w, m, a, b, a0, cs));
+        }
+        if (i == nchunk - 1) SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, cs));
+        SGPU_CUDA_TRY(cudaEventRecord(filtered, cs));
+        SGPU_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_out, filtered, 0));
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(X + (long)c0 * ldi, sizeof(double) * ldi, dX,
+                                        sizeof(double) * Nd, sizeof(double) * Nd, w,
+                                        cudaMemcpyDeviceToHost, ctx->copy_out));
+        SGPU_CUDA_TRY(cudaMemcpy2DAsync(Y + (long)c0 * ldo, sizeof(double) * ldo, dY,
+                                        sizeof(double) * Nd, sizeof(double) * Nd, w,
+                                        cudaMemcpyDeviceToHost, ctx->copy_out));
+        SGPU_CUDA_TRY(cudaEventRecord(freed, ctx->copy_out));
+    }
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->copy_out));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(cs));
+    SGPU_CUDA_TRY(cudaEventElapsedTime(&ctx->last_filter_ms, ctx->ev0, ctx->ev1));
+    return kernel_status_check(ctx);
+}
+
 int sgpu_ChebyshevFiltering(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y, int ldo,
                             int ncol, int m, double a, double b, double a0, int precision)
 {
@@ -370,6 +443,13 @@ int sgpu_ChebyshevFiltering(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
         return SGPU_ERR_ARG;
     }
     if (ncol == 0) return SGPU_OK;
+    // host arrays: stream column chunks (a quarter of the block, at least 64 columns) through
+    // the device so the copies overlap the filter
+    if (ncol >= 128 && !is_device_ptr(X) && !is_device_ptr(Y)) {
+        const int nc = std::max(64, (ncol + 3) / 4);
+        return filter_pipelined(ctx, spin, X, ldi, Y, ldo, ncol, nc, m, a, b, a0,
+                                precision == SGPU_PREC_FP32);
+    }
     double *dX, *dY;
     long lX, lY;
     SGPU_TRY(stage_in(ctx, WS_STAGE_A, X, ldi, ncol, true, &dX, &lX));

@@ -167,6 +167,10 @@ struct sgpu_ctx {
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int *kstatus = nullptr;    // device word: bits set by kernel waits that ran out
+    // host-array filter pipeline (capi.cu): copy-in and copy-out streams, and per buffer slot
+    // the events "input landed", "filtered", "slot free again"
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t pipe_ev[3][3] = {};
     float last_filter_ms = 0.f;
     // optional per-kernel timing (sgpu_profile_enable): events recorded around launches on
     // the context stream, resolved by sgpu_profile_read

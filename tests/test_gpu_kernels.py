@@ -309,3 +309,37 @@ def test_fp32_filter_with_carried_projections(gpu_available, lmax, m, cpl):
         assert rel_err(outs[fuse][0], Xo) < TOL32_FILTER, fuse
     assert rel_err(outs[True][1], outs[False][1]) < 1e-5
     assert rel_err(outs[True][0], outs[False][0]) < 1e-5
+
+
+@pytest.mark.parametrize("precision", [sg.SGPU_PREC_FP64, sg.SGPU_PREC_FP32])
+def test_host_arrays_stream_through_column_chunks(gpu_available, precision):
+    """Host blocks of >= 128 columns are filtered in column chunks whose copies overlap the
+    filter (three device slots, copy-in / filter / copy-out streams). 150 columns: chunks of
+    64, 64 and 22, every slot used and the last chunk ragged; leading dimensions padded. The
+    result matches the same call on device arrays (one unchunked pass) and the FP64 oracle."""
+    import ctypes
+    import torch
+    grid, nl, veff, rng = _random_case((30, 26, 22), seed=31, natom=5)
+    Nd = 30 * 26 * 22
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    ncol, ld, m = 150, Nd + 5, 5
+    x = rng.uniform(-1, 1, (ncol, Nd))
+    Xb = np.full((ncol, ld), 3.0); Xb[:, :Nd] = x
+    Yb = np.full((ncol, ld), 4.0)
+    rc = sg.lib().sgpu_ChebyshevFiltering(ctx._h, 0, sg._ptr(Xb), ld, sg._ptr(Yb), ld, ncol, m,
+                                          ctypes.c_double(0.3), ctypes.c_double(25.0),
+                                          ctypes.c_double(-2.0), precision)
+    assert rc == 0, sg.lib().sgpu_last_error()
+    assert np.all(Xb[:, Nd:] == 3.0) and np.all(Yb[:, Nd:] == 4.0)  # padding untouched
+    Xd = torch.from_numpy(x.copy()).cuda(); Yd = torch.zeros_like(Xd)
+    ctx.ChebyshevFiltering(Xd, Yd, m, 0.3, 25.0, -2.0, precision=precision)
+    Yref, Xref = Yd.cpu().numpy(), Xd.cpu().numpy()
+    tol = 1e-13 if precision == sg.SGPU_PREC_FP64 else 1e-5
+    assert rel_err(Yb[:, :Nd], Yref) < tol
+    assert rel_err(Xb[:, :Nd], Xref) < tol
+    Xo, Yo = o.chebyshev(veff, m, 0.3, 25.0, -2.0, x)
+    tol_o = TOL64 if precision == sg.SGPU_PREC_FP64 else TOL32_FILTER
+    assert rel_err(Yb[:, :Nd], Yo) < tol_o
+    assert rel_err(Xb[:, :Nd], Xo) < tol_o
+    assert ctx.kernel_status() == 0
