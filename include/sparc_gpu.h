@@ -120,6 +120,15 @@ int sgpu_Hamiltonian_vectors_mult(sgpu_ctx *ctx, int spin, int ncol, double c, c
 int sgpu_ChebyshevFiltering(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y, int ldo,
                             int ncol, int m, double a, double b, double a0, int precision);
 
+/* The same filter with X as input only: Y receives the filtered block and the host array X is
+ * left as it was (no copy back). eigSolve_CheFSI never reads X after the filter:
+ * Project_Hamiltonian writes H*Y into Xorb next (src/eigenSolver.c:349-364, :1596), so a
+ * shim can bind ChebyshevFiltering here and save a third of the host-device copies. X must
+ * be a host array (for device blocks use sgpu_ChebyshevFiltering, which works in place). */
+int sgpu_ChebyshevFiltering_y(sgpu_ctx *ctx, int spin, const double *X, int ldi, double *Y,
+                              int ldo, int ncol, int m, double a, double b, double a0,
+                              int precision);
+
 /* The same filter on FP32 blocks (host or device), for callers that keep the orbital block in
  * FP32 between filter calls (the mixed-precision SCF). No counterpart in the reference, which
  * filters in FP64 only; the recurrence scalars are the reference's, computed in FP64. */

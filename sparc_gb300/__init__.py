@@ -40,7 +40,7 @@ EXPORTED = [
     "sgpu_get_tuning", "sgpu_Calculate_local_forces", "sgpu_Calculate_nonlocal_forces",
     "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
-    "sgpu_get_nonlocal_fuse",
+    "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y",
 ]
 
 
@@ -324,6 +324,15 @@ class Context:
                                              int(m), ctypes.c_double(a), ctypes.c_double(b),
                                              ctypes.c_double(a0), int(precision)))
         return X, Y
+
+    def ChebyshevFiltering_y(self, X, Y, m, a, b, a0, spin=0, precision=SGPU_PREC_FP64):
+        """The filter with the host block X as input only (left unchanged); Y gets the result."""
+        ncol, ld = self._ncol_ld(X)
+        _check(lib().sgpu_ChebyshevFiltering_y(self._h, int(spin), _ptr(X), ld, _ptr(Y), ld,
+                                               ncol, int(m), ctypes.c_double(a),
+                                               ctypes.c_double(b), ctypes.c_double(a0),
+                                               int(precision)))
+        return Y
 
     def ChebyshevFiltering_f32(self, X, Y, m, a, b, a0, spin=0):
         ncol, ld = self._ncol_ld(X)

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "sgpu_internal.h"
 
@@ -369,8 +370,10 @@ int sgpu_Hamiltonian_vectors_mult(sgpu_ctx *ctx, int spin, int ncol, double c, c
 // filtered on the context stream, chunk i+1 is copied in on one copy stream and chunk i-1
 // copied out on another. The host-device copies then hide behind the filter instead of
 // adding to it. Each column's arithmetic is the one of the unchunked call.
+// return_x false: X is input only (its chunks are not copied back).
 static int filter_pipelined(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y, int ldo,
-                            int ncol, int nc, int m, double a, double b, double a0, bool f32)
+                            int ncol, int nc, int m, double a, double b, double a0, bool f32,
+                            bool return_x)
 {
     const long Nd = ctx->Nd;
     if (!ctx->copy_in) {
@@ -385,9 +388,28 @@ static int filter_pipelined(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
     SGPU_TRY(ws_get(ctx, WS_STAGE_A, 3 * per, (void **)&base));
     // the previous call's copies out of these buffers are complete: every call ends synchronised
     cudaStream_t cs = ctx->stream;
-    const int nchunk = (ncol + nc - 1) / nc;
-    for (int i = 0; i < nchunk; i++) {
-        const int s = i % 3, c0 = i * nc, w = std::min(nc, ncol - c0);
+    // chunk widths: the first and last chunks, whose copies nothing overlaps, are small
+    // (nc/4, then 3nc/4 to get back in step), the ones between nc wide
+    std::vector<int> widths;
+    if (ncol >= 4 * nc && nc >= 16) {
+        const int q = nc / 4;
+        widths = {q, nc - q};
+        int left = ncol - nc;
+        while (left > nc) {
+            const int w = std::min(nc, left - nc);
+            if (w <= 0) break;
+            widths.push_back(w);
+            left -= w;
+        }
+        widths.push_back(left - q);
+        widths.push_back(q);
+    } else {
+        for (int c = 0; c < ncol; c += nc) widths.push_back(std::min(nc, ncol - c));
+    }
+    const int nchunk = (int)widths.size();
+    int c0 = 0;
+    for (int i = 0; i < nchunk; c0 += widths[i], i++) {
+        const int s = i % 3, w = widths[i];
         double *dX = reinterpret_cast<double *>(base + s * per), *dY = dX + n64;
         float *fX = reinterpret_cast<float *>(dY + n64), *fY = fX + n64;
         cudaEvent_t in_done = ctx->pipe_ev[s][0], filtered = ctx->pipe_ev[s][1],
@@ -406,7 +428,7 @@ static int filter_pipelined(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
             }
             SGPU_TRY(chebyshev_dev<float>(ctx, spin, fX, Nd, fY, Nd, w, m, a, b, a0, cs));
             ProfScope ps(ctx, SGPU_KERNEL_OTHER, cs);
-            SGPU_TRY(convert_cols<float, double>(fX, Nd, dX, Nd, Nd, w, cs));
+            if (return_x) SGPU_TRY(convert_cols<float, double>(fX, Nd, dX, Nd, Nd, w, cs));
             SGPU_TRY(convert_cols<float, double>(fY, Nd, dY, Nd, Nd, w, cs));
             ctx->launches++;
         } else {
@@ -415,9 +437,10 @@ static int filter_pipelined(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
         if (i == nchunk - 1) SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, cs));
         SGPU_CUDA_TRY(cudaEventRecord(filtered, cs));
         SGPU_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_out, filtered, 0));
-        SGPU_CUDA_TRY(cudaMemcpy2DAsync(X + (long)c0 * ldi, sizeof(double) * ldi, dX,
-                                        sizeof(double) * Nd, sizeof(double) * Nd, w,
-                                        cudaMemcpyDeviceToHost, ctx->copy_out));
+        if (return_x)
+            SGPU_CUDA_TRY(cudaMemcpy2DAsync(X + (long)c0 * ldi, sizeof(double) * ldi, dX,
+                                            sizeof(double) * Nd, sizeof(double) * Nd, w,
+                                            cudaMemcpyDeviceToHost, ctx->copy_out));
         SGPU_CUDA_TRY(cudaMemcpy2DAsync(Y + (long)c0 * ldo, sizeof(double) * ldo, dY,
                                         sizeof(double) * Nd, sizeof(double) * Nd, w,
                                         cudaMemcpyDeviceToHost, ctx->copy_out));
@@ -429,8 +452,32 @@ static int filter_pipelined(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
     return kernel_status_check(ctx);
 }
 
+static int filter_host_or_device(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y,
+                                 int ldo, int ncol, int m, double a, double b, double a0,
+                                 int precision, bool return_x);
+
 int sgpu_ChebyshevFiltering(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y, int ldo,
                             int ncol, int m, double a, double b, double a0, int precision)
+{
+    return filter_host_or_device(ctx, spin, X, ldi, Y, ldo, ncol, m, a, b, a0, precision, true);
+}
+
+int sgpu_ChebyshevFiltering_y(sgpu_ctx *ctx, int spin, const double *X, int ldi, double *Y,
+                              int ldo, int ncol, int m, double a, double b, double a0,
+                              int precision)
+{
+    if (X && is_device_ptr(X)) {
+        set_error("sgpu_ChebyshevFiltering_y: X must be a host array (device blocks: use "
+                  "sgpu_ChebyshevFiltering, which works in place)");
+        return SGPU_ERR_ARG;
+    }
+    return filter_host_or_device(ctx, spin, const_cast<double *>(X), ldi, Y, ldo, ncol, m, a, b,
+                                 a0, precision, false);
+}
+
+static int filter_host_or_device(sgpu_ctx *ctx, int spin, double *X, int ldi, double *Y,
+                                 int ldo, int ncol, int m, double a, double b, double a0,
+                                 int precision, bool return_x)
 {
     SGPU_TRY(check_ctx(ctx));
     SGPU_TRY(check_block(ctx, ncol, ldi, ldo));
@@ -448,7 +495,7 @@ int sgpu_ChebyshevFiltering(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
     if (ncol >= 128 && !is_device_ptr(X) && !is_device_ptr(Y)) {
         const int nc = std::max(64, (ncol + 3) / 4);
         return filter_pipelined(ctx, spin, X, ldi, Y, ldo, ncol, nc, m, a, b, a0,
-                                precision == SGPU_PREC_FP32);
+                                precision == SGPU_PREC_FP32, return_x);
     }
     double *dX, *dY;
     long lX, lY;
@@ -473,11 +520,12 @@ int sgpu_ChebyshevFiltering(sgpu_ctx *ctx, int spin, double *X, int ldi, double 
                                       ctx->stream));
         SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
         ProfScope ps(ctx, SGPU_KERNEL_OTHER, ctx->stream);
-        SGPU_TRY(convert_cols<float, double>(fX, ctx->Nd, dX, lX, ctx->Nd, ncol, ctx->stream));
+        if (return_x)
+            SGPU_TRY(convert_cols<float, double>(fX, ctx->Nd, dX, lX, ctx->Nd, ncol, ctx->stream));
         SGPU_TRY(convert_cols<float, double>(fY, ctx->Nd, dY, lY, ctx->Nd, ncol, ctx->stream));
         ctx->launches++;
     }
-    SGPU_TRY(stage_out(ctx, dX, lX, X, ldi, ncol));
+    if (return_x) SGPU_TRY(stage_out(ctx, dX, lX, X, ldi, ncol));
     SGPU_TRY(stage_out(ctx, dY, lY, Y, ldo, ncol));
     SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     SGPU_CUDA_TRY(cudaEventElapsedTime(&ctx->last_filter_ms, ctx->ev0, ctx->ev1));

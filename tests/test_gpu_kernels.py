@@ -311,19 +311,21 @@ def test_fp32_filter_with_carried_projections(gpu_available, lmax, m, cpl):
     assert rel_err(outs[True][0], outs[False][0]) < 1e-5
 
 
-@pytest.mark.parametrize("precision", [sg.SGPU_PREC_FP64, sg.SGPU_PREC_FP32])
-def test_host_arrays_stream_through_column_chunks(gpu_available, precision):
+@pytest.mark.parametrize("precision,ncol", [(sg.SGPU_PREC_FP64, 150), (sg.SGPU_PREC_FP32, 150),
+                                            (sg.SGPU_PREC_FP32, 256)])
+def test_host_arrays_stream_through_column_chunks(gpu_available, precision, ncol):
     """Host blocks of >= 128 columns are filtered in column chunks whose copies overlap the
     filter (three device slots, copy-in / filter / copy-out streams). 150 columns: chunks of
-    64, 64 and 22, every slot used and the last chunk ragged; leading dimensions padded. The
-    result matches the same call on device arrays (one unchunked pass) and the FP64 oracle."""
+    64, 64 and 22, every slot used and the last chunk ragged; 256 columns: the schedule with
+    small end chunks (16, 48, 64, 64, 48, 16); leading dimensions padded. The result matches
+    the same call on device arrays (one unchunked pass) and the FP64 oracle."""
     import ctypes
     import torch
     grid, nl, veff, rng = _random_case((30, 26, 22), seed=31, natom=5)
     Nd = 30 * 26 * 22
     ctx = make_ctx(grid, nl, veff)
     o = Oracle(grid, nl)
-    ncol, ld, m = 150, Nd + 5, 5
+    ld, m = Nd + 5, 5
     x = rng.uniform(-1, 1, (ncol, Nd))
     Xb = np.full((ncol, ld), 3.0); Xb[:, :Nd] = x
     Yb = np.full((ncol, ld), 4.0)
@@ -342,4 +344,11 @@ def test_host_arrays_stream_through_column_chunks(gpu_available, precision):
     tol_o = TOL64 if precision == sg.SGPU_PREC_FP64 else TOL32_FILTER
     assert rel_err(Yb[:, :Nd], Yo) < tol_o
     assert rel_err(Xb[:, :Nd], Xo) < tol_o
+    # X as input only: the same Y, X untouched
+    Xi = x.copy(); Yi = np.zeros_like(x)
+    ctx.ChebyshevFiltering_y(Xi, Yi, m, 0.3, 25.0, -2.0, precision=precision)
+    np.testing.assert_array_equal(Xi, x)
+    assert rel_err(Yi, Yref) < tol
+    with pytest.raises(sg.SgpuError):  # device X would be overwritten in place: refused
+        ctx.ChebyshevFiltering_y(Xd, Yd, m, 0.3, 25.0, -2.0, precision=precision)
     assert ctx.kernel_status() == 0
