@@ -352,3 +352,26 @@ def test_host_arrays_stream_through_column_chunks(gpu_available, precision, ncol
     with pytest.raises(sg.SgpuError):  # device X would be overwritten in place: refused
         ctx.ChebyshevFiltering_y(Xd, Yd, m, 0.3, 25.0, -2.0, precision=precision)
     assert ctx.kernel_status() == 0
+
+
+@pytest.mark.parametrize("ncol", [1, 2, 63, 64, 65, 128])
+@pytest.mark.parametrize("cpl", [2, 4])
+def test_carried_projections_column_edges(gpu_available, ncol, cpl):
+    """The fused range apply + projection at column counts that end a 64-column group
+    exactly, one short, one over, a single column and an odd last pair (each form), against
+    the oracle within the FP32 filter tolerance."""
+    grid, nl, veff, rng = _random_case((32, 26, 22), seed=41 + ncol, natom=6)
+    Nd = 32 * 26 * 22
+    ctx = make_ctx(grid, nl, veff)
+    o = Oracle(grid, nl)
+    ctx.set_stencil_variant(6)
+    ctx.set_nonlocal_apply_variant(4)
+    ctx.set_nonlocal_project_variant(1)
+    ctx.set_nonlocal_fuse(True, cpl)
+    x = rng.uniform(-1, 1, (ncol, Nd))
+    X = x.astype(np.float32); Y = np.zeros_like(X)
+    ctx.ChebyshevFiltering_f32(X, Y, 4, 0.5, 50.0, -1.0)
+    Xo, Yo = o.chebyshev(veff, 4, 0.5, 50.0, -1.0, x)
+    assert rel_err(Y.astype(np.float64), Yo) < TOL32_FILTER
+    assert rel_err(X.astype(np.float64), Xo) < TOL32_FILTER
+    assert ctx.kernel_status() == 0
