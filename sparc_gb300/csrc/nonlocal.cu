@@ -253,7 +253,8 @@ __global__ void __launch_bounds__(256)
 // Range apply (FP32): the projection's ranges and work items run in reverse. Block = one range;
 // for each group of 64 columns (rotated by the range index) it gathers the output tile of its
 // points (os[point][64], one coalesced read of every covered output element), then each warp
-// owns kRangeWarpPts consecutive points of the tile: it walks the work items in order and,
+// owns a run of consecutive points of the tile (runs with about equal entry counts, set at
+// upload): it walks the work items in order and,
 // for the item's entries on its points (item_wsplit gives their range per warp), lane l holds
 // scale * alpha[row j, columns l and l+32] of the item's atom in registers and adds
 // sum_j Chi_j alpha_j into its tile rows. The tile is then written back once: every covered
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(256, 4)
         gather_tile<OLD, NC>(out, ldo, n0, ncol, gps, npt, os);
         __syncthreads();
         const int ca = n0 + lane, cb = n0 + lane + 32;
-        // warp w owns the tile rows of points [w * kRangeWarpPts, (w + 1) * kRangeWarpPts):
+        // warp w owns the tile rows of its run of points (item_wsplit):
         // it walks every item but only the item's entries on its own points, so no two warps
         // write one tile row and the additions per point run in item order
         for (int it = 0; it < ni; it++) {
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(256, 4)
 // and adds it atomically into alpha_next (zeroed by the caller). Ranges partition the covered
 // points, so a range's tile is final once its own apply is done; the separate projection of
 // the next degree, and its read of every covered element, disappear.
-//   apply: warp w owns the tile rows of points [w kRangeWarpPts, (w + 1) kRangeWarpPts) as in
+//   apply: warp w owns the tile rows of its run of points (item_wsplit) as in
 //     k_nl_apply_range; per element the same IEEE operations in the same item order, so the
 //     output is bit-identical to k_nl_apply_range.
 //   projection: per work item the entries are summed in order as in k_nl_project_range (the
@@ -1237,6 +1238,20 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
                           " projector spheres overlap at one grid point");
                 return SGPU_ERR_ARG;
             }
+            // the apply's owner warps: contiguous runs of the range's points with about equal
+            // entry counts (a range cut by the entry cap holds fewer than kRangePts points)
+            int wb[kRangeWarps + 1];
+            {
+                const long tot = covptr[p] - covptr[q0];
+                int c = q0;
+                wb[0] = 0;
+                for (int w = 1; w < kRangeWarps; w++) {
+                    const long target = tot * w / kRangeWarps;
+                    while (c < p && covptr[c] - covptr[q0] < target) c++;
+                    wb[w] = c - q0;
+                }
+                wb[kRangeWarps] = p - q0;
+            }
             order.clear();
             for (int e = covptr[q0]; e < covptr[p]; e++) order.push_back({(long)ent_meta[e].w, e});
             // entries are already in point order; a stable sort by image keeps it per image
@@ -1267,7 +1282,7 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
                 item_e0.push_back((int)pe_lp.size());
                 // the item's entries by owning warp: points ascend within the item
                 for (int w = 0, e = first; w <= kRangeWarps; w++) {
-                    while (e < (int)pe_lp.size() && pe_lp[e] < w * kRangeWarpPts) e++;
+                    while (e < (int)pe_lp.size() && (w == kRangeWarps || pe_lp[e] < wb[w])) e++;
                     item_wsplit.push_back(e);
                 }
                 k = k1;

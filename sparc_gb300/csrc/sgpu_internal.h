@@ -20,7 +20,6 @@ constexpr int kRangePts = 128;       // covered points per range of the range pr
 constexpr int kRangeMaxEnt = 320;    // entries per range at most (bounds its staged Chi)
 constexpr int kRangeItemEnt = 96;    // entries per work item of the range projection at most
 constexpr int kRangeWarps = 8;       // warps per range block
-constexpr int kRangeWarpPts = kRangePts / kRangeWarps;  // tile rows owned by one warp (apply)
 static_assert(kRangePts % kRangeWarps == 0, "whole tile rows per warp");
 
 // thread-local error text, returned by sgpu_last_error()
