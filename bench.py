@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-scf", action="store_true", help="skip the SCF time-to-solution blocks")
     ap.add_argument("--no-c4", action="store_true", help="skip the 216-atom SCF block")
     ap.add_argument("--no-c3", action="store_true", help="skip the batched k-point/spin block")
+    ap.add_argument("--rr-gemm", action="store_true",
+                    help="only time the Rayleigh-Ritz products at the Si216 shapes")
     ap.add_argument("--c3-only", action="store_true",
                     help="print only the batched k-point/spin block (profiling)")
     ap.add_argument("--stencil-variant", type=int, default=None,
@@ -433,6 +435,65 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def rr_gemm_block(sg, torch, dev, device=0, steps=3):
+    """The Rayleigh-Ritz products at the Si216 shapes (77^3 grid at h = 0.40, 520 states):
+    the mixed SCF's FP32 forms (tensor cores, BF16x9-split products, FP32 accumulation) and
+    the FP64 forms (DGEMM/DSYRK), timed with CUDA events on the library's stream, with the
+    achieved TFLOP/s of the rotation (one GEMM, 2 Nd Ns^2 flops) and of the two products of
+    the projection (2 Nd Ns^2 each; its H Y apply timed and subtracted)."""
+    from sparc_gb300.synthetic import fd_d2_coeffs, gaussian_potential
+    N, h, ns = (77, 77, 77), 0.40, 520
+    c = fd_d2_coeffs(6, h)
+    rng = np.random.default_rng(7)
+    ctx = sg.Context(*N, 6, c, c, c, h ** 3, device=device)
+    ctx.set_veff(gaussian_potential(rng, N, h))
+    nd = N[0] * N[1] * N[2]
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    out = {"shape": f"Nd = {nd} (77^3), Ns = {ns}"}
+    for name, dt in (("fp32", torch.float32), ("fp32_eager", torch.float32),
+                     ("fp64", torch.float64)):
+        ctx.set_gemm_emulation(name == "fp32_eager")
+        Y = torch.rand((ns, nd), device=dev, dtype=dt) - 0.5
+        HY = torch.empty_like(Y)
+        X = torch.empty_like(Y)
+        Hp = torch.empty((ns, ns), device=dev, dtype=torch.float64)
+        Mp = torch.empty_like(Hp)
+        Q = (torch.rand((ns, ns), device=dev, dtype=torch.float64) - 0.5) / ns ** 0.5
+        f32 = name != "fp64"
+        proj = (lambda: ctx.Project_Hamiltonian_f32(Y, HY, Hp, Mp)) if f32 else \
+            (lambda: ctx.Project_Hamiltonian(Y, HY, Hp, Mp))
+        rot = (lambda: ctx.Subspace_Rotation_f32(Y, Q, X)) if f32 else \
+            (lambda: ctx.Subspace_Rotation(Y, Q, X))
+        ham = (lambda: ctx.Hamiltonian_vectors_mult(0.0, Y, HY)) if name == "fp64" else None
+
+        def timed_ms(fn):
+            for _ in range(2):
+                fn()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            for _ in range(steps):
+                fn()
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            return ev0.elapsed_time(ev1) / steps
+
+        t_rot = timed_ms(rot)
+        t_proj = timed_ms(proj)
+        gemm = 2.0 * nd * ns * ns
+        out[name] = {"rotation_ms": round(t_rot, 3),
+                     "rotation_tflops": round(gemm / (t_rot / 1e3) / 1e12, 2),
+                     "projection_ms_incl_HY": round(t_proj, 3)}
+        if ham is not None:
+            t_h = timed_ms(ham)
+            out[name]["projection_products_tflops"] = round(
+                2 * gemm / ((t_proj - t_h) / 1e3) / 1e12, 2)
+        del Y, HY, X
+    ctx.close()
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -450,6 +511,10 @@ def main():
     dev = torch.device("cuda", local)
     if args.c3_only:
         print(json.dumps({"batched_c3": batched_c3_block(sg, torch, dev, device=local,
+                                                         steps=args.steps)}), flush=True)
+        return
+    if args.rr_gemm:
+        print(json.dumps({"rayleigh_ritz": rr_gemm_block(sg, torch, dev, device=local,
                                                          steps=args.steps)}), flush=True)
         return
 

@@ -201,6 +201,17 @@ int sgpu_Solve_Generalized_EigenProblem(sgpu_ctx *ctx, int Ns, double *Hp, doubl
 int sgpu_Subspace_Rotation(sgpu_ctx *ctx, const double *Y, int ldi, const double *Q, int ncol,
                            double *X, int ldo);
 
+/* The Rayleigh-Ritz products of the mixed SCF's FP32 phase on device FP32 blocks (for callers
+ * that keep the orbitals in FP32, beside sgpu_ChebyshevFiltering_f32): HY = H Y in FP32, then
+ * Hp = Yᵀ HY and Mp = Yᵀ Y, and X = Y Q, as FP32 GEMMs with FP32 accumulation (cuBLAS, with
+ * the FP32-accurate BF16x9 tensor-core emulation requested; see sgpu_set_gemm_emulation);
+ * Hp, Mp and Q are FP64 (host or device). FP32-precision counterparts of the two calls
+ * above. */
+int sgpu_Project_Hamiltonian_f32(sgpu_ctx *ctx, int spin, const float *Y, int ldi, float *HY,
+                                 int ldo, int ncol, double *Hp, double *Mp);
+int sgpu_Subspace_Rotation_f32(sgpu_ctx *ctx, const float *Y, int ldi, const double *Q, int ncol,
+                               float *X, int ldo);
+
 /* Lanczos estimate of the smallest and largest eigenvalue of H (spin block spin) from start
  * vector x0 (Nd values), stopping when both change by less than tol between iterations.
  * Replaces Lanczos (src/eigenSolver.c:1920) as called by Chebyshevfilter_constants (:589). */
@@ -492,6 +503,13 @@ int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
  * sgpu_autotune times both. The two sum in different orders (and both add per-block
  * partial sums atomically), so results agree to FP32 rounding. */
 int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
+
+/* The FP32-block Rayleigh-Ritz products (mixed SCF, sgpu_Project_Hamiltonian_f32,
+ * sgpu_Subspace_Rotation_f32) ask cuBLAS for FP32-accurate BF16x9 emulation on the tensor
+ * cores. eager = 0: cuBLAS emulates only where its heuristics expect a gain (its default);
+ * eager = 1: whenever possible. (With cuBLAS of CUDA 13.0 on GB300 both keep the FP32 SIMT
+ * GEMM for these shapes.) */
+int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int eager);
 
 /* FP32 filter with the projections carried across degrees (mode 1, 2 or 4) or not (0). When
  * on, every degree's nonlocal apply is the range form with the projection of the iterate it

@@ -40,7 +40,8 @@ EXPORTED = [
     "sgpu_get_tuning", "sgpu_Calculate_local_forces", "sgpu_Calculate_nonlocal_forces",
     "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
-    "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y",
+    "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
+    "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation",
 ]
 
 
@@ -333,6 +334,24 @@ class Context:
                                                ctypes.c_double(b), ctypes.c_double(a0),
                                                int(precision)))
         return Y
+
+    def set_gemm_emulation(self, eager):
+        """FP32-block products: BF16x9 tensor-core emulation whenever possible (True) or
+        where cuBLAS expects a gain (False)."""
+        _check(lib().sgpu_set_gemm_emulation(self._h, 1 if eager else 0))
+
+    def Project_Hamiltonian_f32(self, Y, HY, Hp, Mp, spin=0):
+        """FP32 device blocks Y, HY (ncol, Nd); Hp, Mp (ncol, ncol) FP64."""
+        ncol, ld = self._ncol_ld(Y)
+        _check(lib().sgpu_Project_Hamiltonian_f32(self._h, int(spin), _ptr(Y), ld, _ptr(HY), ld,
+                                                  ncol, _ptr(Hp), _ptr(Mp)))
+        return Hp, Mp
+
+    def Subspace_Rotation_f32(self, Y, Q, X):
+        """X = Y Q on FP32 device blocks (ncol, Nd); Q (ncol, ncol) FP64."""
+        ncol, ld = self._ncol_ld(Y)
+        _check(lib().sgpu_Subspace_Rotation_f32(self._h, _ptr(Y), ld, _ptr(Q), ncol, _ptr(X), ld))
+        return X
 
     def ChebyshevFiltering_f32(self, X, Y, m, a, b, a0, spin=0):
         ncol, ld = self._ncol_ld(X)

@@ -210,6 +210,24 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant)
     return SGPU_OK;
 }
 
+int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int eager)
+{
+    if (!ctx || (eager != 0 && eager != 1)) {
+        set_error("sgpu_set_gemm_emulation: need a context and eager = 0 or 1");
+        return SGPU_ERR_ARG;
+    }
+    ctx->gemm_eager = eager == 1;
+    if (ctx->cublas &&
+        cublasSetEmulationStrategy(ctx->cublas, ctx->gemm_eager
+                                                    ? CUBLAS_EMULATION_STRATEGY_EAGER
+                                                    : CUBLAS_EMULATION_STRATEGY_PERFORMANT) !=
+            CUBLAS_STATUS_SUCCESS) {
+        set_error("sgpu_set_gemm_emulation: cublasSetEmulationStrategy failed");
+        return SGPU_ERR_CUDA;
+    }
+    return SGPU_OK;
+}
+
 int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int mode)
 {
     if (!ctx || (mode != 0 && mode != 1 && mode != 2 && mode != 4)) {

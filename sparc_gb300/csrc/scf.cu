@@ -11,8 +11,8 @@
 // scalars (energy terms, SCF error) and the m x m Anderson systems come back to the host.
 //
 // Mixed precision (SGPU_PREC_FP32): while the SCF error is above fp64_switch_error the orbital
-// block is FP32, the filter runs in FP32 and the projection / rotation products use cuBLAS's
-// BF16x9 FP32 emulation on the tensor cores; the eigenproblem, Poisson, XC, mixing and all
+// block is FP32, the filter runs in FP32 and the projection / rotation products are FP32
+// GEMMs (cuBLAS, BF16x9 emulation requested); the eigenproblem, Poisson, XC, mixing and all
 // energy reductions stay FP64. Below the threshold (or once the FP32 error stalls) the block
 // is widened to FP64 and the remaining iterations are either the plain FP64 path or, with
 // graded_tail, an FP32 filter whose last degrees run in FP64 followed by an FP64
@@ -410,6 +410,54 @@ int sgpu_Subspace_Rotation(sgpu_ctx *ctx, const double *Y, int ldi, const double
         SGPU_CUDA_TRY(cudaMemcpy2DAsync(X, sizeof(double) * ldo, dX, sizeof(double) * lx,
                                         sizeof(double) * ctx->Nd, ncol, cudaMemcpyDeviceToHost,
                                         ctx->stream));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+// FP32 orbital blocks (device): the Rayleigh-Ritz products of the mixed SCF's FP32 phase, Hp
+// and Mp (or Q) FP64 on the host or the device.
+int sgpu_Project_Hamiltonian_f32(sgpu_ctx *ctx, int spin, const float *Y, int ldi, float *HY,
+                                 int ldo, int ncol, double *Hp, double *Mp)
+{
+    SGPU_TRY(check(ctx));
+    if (ncol <= 0 || ldi < ctx->Nd || ldo < ctx->Nd || !Y || !HY || !Hp || !Mp) {
+        set_error("Project_Hamiltonian_f32: need ncol > 0, arrays and leading dimensions >= Nd");
+        return SGPU_ERR_ARG;
+    }
+    if (!is_device_ptr(Y) || !is_device_ptr(HY)) {
+        set_error("Project_Hamiltonian_f32: Y and HY must be device FP32 blocks");
+        return SGPU_ERR_ARG;
+    }
+    const long n2 = (long)ncol * ncol;
+    double *dHp, *dMp;
+    SGPU_TRY(stage_vec(ctx, WS_SCF, Hp, 2 * n2, &dHp));
+    dMp = is_device_ptr(Mp) ? Mp : dHp + n2;
+    if (is_device_ptr(Hp) && !is_device_ptr(Mp))
+        SGPU_TRY(ws_get(ctx, WS_SCF2, sizeof(double) * n2, (void **)&dMp));
+    SGPU_TRY(hamiltonian_dev<float>(ctx, spin, ncol, 0.0, Y, ldi, HY, ldo, 1.0, 0.0, nullptr, 0,
+                                    ctx->stream));
+    SGPU_TRY(project_f32(ctx, ncol, Y, ldi, HY, ldo, dHp, dMp, ctx->stream));
+    SGPU_TRY(unstage_vec(ctx, dHp, Hp, n2));
+    SGPU_TRY(unstage_vec(ctx, dMp, Mp, n2));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_Subspace_Rotation_f32(sgpu_ctx *ctx, const float *Y, int ldi, const double *Q, int ncol,
+                               float *X, int ldo)
+{
+    SGPU_TRY(check(ctx));
+    if (ncol <= 0 || ldi < ctx->Nd || ldo < ctx->Nd || !Y || !Q || !X) {
+        set_error("Subspace_Rotation_f32: need ncol > 0, arrays and leading dimensions >= Nd");
+        return SGPU_ERR_ARG;
+    }
+    if (!is_device_ptr(Y) || !is_device_ptr(X)) {
+        set_error("Subspace_Rotation_f32: Y and X must be device FP32 blocks");
+        return SGPU_ERR_ARG;
+    }
+    double *dQ;
+    SGPU_TRY(stage_vec(ctx, WS_SCF, Q, (long)ncol * ncol, &dQ));
+    SGPU_TRY(rotate_f32(ctx, ncol, Y, ldi, dQ, X, ldo, ctx->stream));
     SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return SGPU_OK;
 }

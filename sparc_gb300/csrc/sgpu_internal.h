@@ -161,6 +161,8 @@ struct sgpu_ctx {
     bool nl_fuse = false;  // FP32 filter: project each new iterate inside the range apply that
                            // finishes it (one projection launch per filter, not per degree)
     int nl_fuse_cpl = 2;   // fused apply: columns per lane (2 or 4), chosen by the tuner
+    bool gemm_eager = false;  // FP32 products: BF16x9 emulation whenever possible (else only
+                              // where cuBLAS expects a gain)
     double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
     double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings

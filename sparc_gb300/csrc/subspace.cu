@@ -9,9 +9,11 @@
 //       X = Y Q (cblas_dgemm :1415)
 //
 // GPU form: the products are plain GEMMs, so they go to cuBLAS: DSYRK/DGEMM in FP64 for the
-// drop-in, and for FP32 blocks (the mixed-precision filter) SGEMM with the BF16x9 FP32
-// emulation on the tensor cores (each FP32 operand split into three BF16 terms, FP32
-// accumulation). The Ns x Ns generalized eigenproblem stays FP64 on cuSOLVER (dsygvd).
+// drop-in, and for FP32 blocks (the mixed-precision filter) FP32 GEMMs with the BF16x9
+// emulated compute type requested (cuBLAS may then split each FP32 operand into three BF16
+// terms on the tensor cores; on this GB300 and cuBLAS it keeps its FP32 SIMT GEMM, measured at
+// 56 TFLOP/s at the Si216 shapes, either strategy). FP32 accumulation throughout. The Ns x Ns
+// generalized eigenproblem stays FP64 on cuSOLVER (dsygvd).
 #include <algorithm>
 
 #include "sgpu_internal.h"
@@ -23,6 +25,9 @@ static int ensure_handles(sgpu_ctx *ctx)
     if (!ctx->cublas) {
         SGPU_CUBLAS_TRY(cublasCreate(&ctx->cublas));
         SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, ctx->stream));
+        SGPU_CUBLAS_TRY(cublasSetEmulationStrategy(
+            ctx->cublas, ctx->gemm_eager ? CUBLAS_EMULATION_STRATEGY_EAGER
+                                         : CUBLAS_EMULATION_STRATEGY_PERFORMANT));
     }
     if (!ctx->cusolver) {
         if (cusolverDnCreate(&ctx->cusolver) != CUSOLVER_STATUS_SUCCESS) {
@@ -77,8 +82,8 @@ int project_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double
     return SGPU_OK;
 }
 
-// The same for FP32 blocks: products on the tensor cores with BF16x9 FP32 emulation,
-// accumulated in FP32, then widened to FP64 for the eigensolver.
+// The same for FP32 blocks: FP32 products (BF16x9 emulation requested), accumulated in FP32,
+// then widened to FP64 for the eigensolver.
 int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
                 double *Hp, double *Mp, cudaStream_t st)
 {
@@ -244,7 +249,7 @@ int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double 
     return SGPU_OK;
 }
 
-// X = Y Q with FP32 blocks: Q is narrowed to FP32, product with BF16x9 emulation
+// X = Y Q with FP32 blocks: Q is narrowed to FP32, FP32 product (BF16x9 emulation requested)
 int rotate_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const double *Q, float *X,
                long ldx, cudaStream_t st)
 {

@@ -375,3 +375,32 @@ def test_carried_projections_column_edges(gpu_available, ncol, cpl):
     assert rel_err(Y.astype(np.float64), Yo) < TOL32_FILTER
     assert rel_err(X.astype(np.float64), Xo) < TOL32_FILTER
     assert ctx.kernel_status() == 0
+
+
+@pytest.mark.parametrize("eager", [False, True])
+def test_fp32_rayleigh_ritz_products(gpu_available, eager):
+    """sgpu_Project_Hamiltonian_f32 / sgpu_Subspace_Rotation_f32 (tensor-core products with
+    FP32-accurate BF16x9 splitting) against FP64 products of the same FP32 inputs, with H
+    from the oracle: relative error within FP32 accumulation over Nd terms (1e-4)."""
+    import torch
+    grid, nl, veff, rng = _random_case((30, 26, 22), seed=51, natom=4)
+    Nd = 30 * 26 * 22
+    ctx = make_ctx(grid, nl, veff)
+    ctx.set_gemm_emulation(eager)
+    o = Oracle(grid, nl)
+    ncol = 40
+    y = rng.uniform(-1, 1, (ncol, Nd)).astype(np.float32)
+    Yd = torch.from_numpy(y).cuda(); HYd = torch.zeros_like(Yd)
+    Hp = np.zeros((ncol, ncol)); Mp = np.zeros((ncol, ncol))
+    ctx.Project_Hamiltonian_f32(Yd, HYd, Hp, Mp)
+    y64 = y.astype(np.float64)
+    hy = o.hamiltonian(veff, 0.0, y64)
+    assert rel_err(HYd.cpu().numpy().astype(np.float64), hy) < TOL32_H * 10
+    assert rel_err(Hp, y64 @ hy.T) < 1e-4
+    assert rel_err(Mp, y64 @ y64.T) < 1e-4
+    q = rng.normal(size=(ncol, ncol))
+    Xd = torch.zeros_like(Yd)
+    ctx.Subspace_Rotation_f32(Yd, q, Xd)
+    # X (column-major Nd x ncol) = Y Q with Q column-major: row n of q holds column n of Q,
+    # so row n of the (ncol, Nd) result is sum_k q[n, k] y[k]
+    assert rel_err(Xd.cpu().numpy().astype(np.float64), q @ y64) < 1e-4
