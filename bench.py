@@ -451,8 +451,8 @@ def rr_gemm_block(sg, torch, dev, device=0, steps=3):
     stream = torch.cuda.ExternalStream(ctx.stream())
     out = {"shape": f"Nd = {nd} (77^3), Ns = {ns}"}
     for name, dt in (("fp32", torch.float32), ("fp32_eager", torch.float32),
-                     ("fp64", torch.float64)):
-        ctx.set_gemm_emulation(name == "fp32_eager")
+                     ("fp32_bf16_split", torch.float32), ("fp64", torch.float64)):
+        ctx.set_gemm_emulation({"fp32_eager": 1, "fp32_bf16_split": 2}.get(name, 0))
         Y = torch.rand((ns, nd), device=dev, dtype=dt) - 0.5
         HY = torch.empty_like(Y)
         X = torch.empty_like(Y)

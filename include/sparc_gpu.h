@@ -203,8 +203,8 @@ int sgpu_Subspace_Rotation(sgpu_ctx *ctx, const double *Y, int ldi, const double
 
 /* The Rayleigh-Ritz products of the mixed SCF's FP32 phase on device FP32 blocks (for callers
  * that keep the orbitals in FP32, beside sgpu_ChebyshevFiltering_f32): HY = H Y in FP32, then
- * Hp = Yᵀ HY and Mp = Yᵀ Y, and X = Y Q, as FP32 GEMMs with FP32 accumulation (cuBLAS, with
- * the FP32-accurate BF16x9 tensor-core emulation requested; see sgpu_set_gemm_emulation);
+ * Hp = Yᵀ HY and Mp = Yᵀ Y, and X = Y Q, as FP32-accurate products with FP32 accumulation
+ * (cuBLAS FP32 GEMM or BF16 split products on the tensor cores: sgpu_set_gemm_emulation);
  * Hp, Mp and Q are FP64 (host or device). FP32-precision counterparts of the two calls
  * above. */
 int sgpu_Project_Hamiltonian_f32(sgpu_ctx *ctx, int spin, const float *Y, int ldi, float *HY,
@@ -504,12 +504,14 @@ int sgpu_set_nonlocal_apply_variant(sgpu_ctx *ctx, int variant);
  * partial sums atomically), so results agree to FP32 rounding. */
 int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
 
-/* The FP32-block Rayleigh-Ritz products (mixed SCF, sgpu_Project_Hamiltonian_f32,
- * sgpu_Subspace_Rotation_f32) ask cuBLAS for FP32-accurate BF16x9 emulation on the tensor
- * cores. eager = 0: cuBLAS emulates only where its heuristics expect a gain (its default);
- * eager = 1: whenever possible. (With cuBLAS of CUDA 13.0 on GB300 both keep the FP32 SIMT
- * GEMM for these shapes.) */
-int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int eager);
+/* How the FP32-block Rayleigh-Ritz products (mixed SCF, sgpu_Project_Hamiltonian_f32,
+ * sgpu_Subspace_Rotation_f32) are formed, all FP32-accurate with FP32 accumulation.
+ * mode 0: cuBLAS FP32 GEMM with the BF16x9 tensor-core emulation requested, used where cuBLAS
+ * expects a gain (its default strategy); mode 1: the same with the eager strategy (with
+ * cuBLAS of CUDA 13.0 on GB300 both keep the FP32 SIMT GEMM for these shapes); mode 2: each
+ * FP32 operand split into three BF16 parts and the product formed from six BF16 GEMMs on the
+ * tensor cores (the part products of order <= 2, smallest first). */
+int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode);
 
 /* FP32 filter with the projections carried across degrees (mode 1, 2 or 4) or not (0). When
  * on, every degree's nonlocal apply is the range form with the projection of the iterate it

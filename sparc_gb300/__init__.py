@@ -335,10 +335,10 @@ class Context:
                                                int(precision)))
         return Y
 
-    def set_gemm_emulation(self, eager):
-        """FP32-block products: BF16x9 tensor-core emulation whenever possible (True) or
-        where cuBLAS expects a gain (False)."""
-        _check(lib().sgpu_set_gemm_emulation(self._h, 1 if eager else 0))
+    def set_gemm_emulation(self, mode):
+        """FP32-block products: 0 cuBLAS FP32 GEMM (BF16x9 emulation where cuBLAS expects a
+        gain), 1 the same with eager emulation, 2 three-part BF16 split on the tensor cores."""
+        _check(lib().sgpu_set_gemm_emulation(self._h, int(mode)))
 
     def Project_Hamiltonian_f32(self, Y, HY, Hp, Mp, spin=0):
         """FP32 device blocks Y, HY (ncol, Nd); Hp, Mp (ncol, ncol) FP64."""

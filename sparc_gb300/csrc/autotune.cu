@@ -210,17 +210,16 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant)
     return SGPU_OK;
 }
 
-int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int eager)
+int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode)
 {
-    if (!ctx || (eager != 0 && eager != 1)) {
-        set_error("sgpu_set_gemm_emulation: need a context and eager = 0 or 1");
+    if (!ctx || mode < 0 || mode > 2) {
+        set_error("sgpu_set_gemm_emulation: need a context and mode 0, 1 or 2");
         return SGPU_ERR_ARG;
     }
-    ctx->gemm_eager = eager == 1;
+    ctx->gemm_mode = mode;
     if (ctx->cublas &&
-        cublasSetEmulationStrategy(ctx->cublas, ctx->gemm_eager
-                                                    ? CUBLAS_EMULATION_STRATEGY_EAGER
-                                                    : CUBLAS_EMULATION_STRATEGY_PERFORMANT) !=
+        cublasSetEmulationStrategy(ctx->cublas, mode == 1 ? CUBLAS_EMULATION_STRATEGY_EAGER
+                                                          : CUBLAS_EMULATION_STRATEGY_PERFORMANT) !=
             CUBLAS_STATUS_SUCCESS) {
         set_error("sgpu_set_gemm_emulation: cublasSetEmulationStrategy failed");
         return SGPU_ERR_CUDA;

@@ -148,7 +148,7 @@ struct sgpu_ctx {
     bool has_nl = false;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
-    sgpu::Workspace ws[13];    // grow-only scratch slots (see enum WsSlot)
+    sgpu::Workspace ws[15];    // grow-only scratch slots (see enum WsSlot)
     sgpu::MixState *mix = nullptr;
     sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)
     sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
@@ -161,8 +161,9 @@ struct sgpu_ctx {
     bool nl_fuse = false;  // FP32 filter: project each new iterate inside the range apply that
                            // finishes it (one projection launch per filter, not per degree)
     int nl_fuse_cpl = 2;   // fused apply: columns per lane (2 or 4), chosen by the tuner
-    bool gemm_eager = false;  // FP32 products: BF16x9 emulation whenever possible (else only
-                              // where cuBLAS expects a gain)
+    int gemm_mode = 0;  // FP32-block products: 0 cuBLAS FP32 GEMM (BF16x9 emulation where
+                        // cuBLAS expects a gain), 1 the same with eager emulation, 2 the
+                        // library's three-part BF16 split on the tensor cores
     double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
     double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
@@ -189,7 +190,7 @@ namespace sgpu {
 
 enum WsSlot {
     WS_STAGE_A = 0, WS_STAGE_B, WS_STAGE_C, WS_ALPHA, WS_MISC, WS_EIG, WS_POIS, WS_MIX,
-    WS_RED, WS_RHS, WS_SCF, WS_SCF2, WS_ALPHA2
+    WS_RED, WS_RHS, WS_SCF, WS_SCF2, WS_ALPHA2, WS_SPLIT_A, WS_SPLIT_B
 };
 
 // grow-only device scratch

@@ -16,6 +16,8 @@
 // generalized eigenproblem stays FP64 on cuSOLVER (dsygvd).
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "sgpu_internal.h"
 
 namespace sgpu {
@@ -26,8 +28,8 @@ static int ensure_handles(sgpu_ctx *ctx)
         SGPU_CUBLAS_TRY(cublasCreate(&ctx->cublas));
         SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, ctx->stream));
         SGPU_CUBLAS_TRY(cublasSetEmulationStrategy(
-            ctx->cublas, ctx->gemm_eager ? CUBLAS_EMULATION_STRATEGY_EAGER
-                                         : CUBLAS_EMULATION_STRATEGY_PERFORMANT));
+            ctx->cublas, ctx->gemm_mode == 1 ? CUBLAS_EMULATION_STRATEGY_EAGER
+                                             : CUBLAS_EMULATION_STRATEGY_PERFORMANT));
     }
     if (!ctx->cusolver) {
         if (cusolverDnCreate(&ctx->cusolver) != CUSOLVER_STATUS_SUCCESS) {
@@ -82,8 +84,65 @@ int project_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double
     return SGPU_OK;
 }
 
-// The same for FP32 blocks: FP32 products (BF16x9 emulation requested), accumulated in FP32,
-// then widened to FP64 for the eigensolver.
+// FP32-accurate products on the BF16 tensor cores (gemm_mode 2). Each FP32 operand x becomes
+// three BF16 parts, hi = bf16(x), mid = bf16(x - hi), lo = bf16(x - hi - mid) (both
+// differences are exact in FP32), which carry its 24-bit significand 8 bits at a time; a
+// product is then the sum of the six part products whose orders add up to at most 2 (the
+// dropped ones are below FP32 rounding), each a BF16 GEMM with FP32 accumulation, smallest
+// first. x: rows x cols, leading dimension ldx; parts: leading dimension rows.
+__global__ void k_split3_bf16(const float *__restrict__ x, long ldx, long rows,
+                              __nv_bfloat16 *__restrict__ p0, __nv_bfloat16 *__restrict__ p1,
+                              __nv_bfloat16 *__restrict__ p2)
+{
+    const long c = blockIdx.y;
+    const float *xc = x + c * ldx;
+    const long o = c * rows;
+    for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < rows;
+         r += (long)gridDim.x * blockDim.x) {
+        const float v = xc[r];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const float r1 = v - __bfloat162float(h);
+        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+        const float r2 = r1 - __bfloat162float(m);
+        p0[o + r] = h;
+        p1[o + r] = m;
+        p2[o + r] = __float2bfloat16_rn(r2);
+    }
+}
+
+static int split3(sgpu_ctx *ctx, const float *x, long ldx, long rows, int cols, int slot,
+                  __nv_bfloat16 **parts, cudaStream_t st)
+{
+    __nv_bfloat16 *base = nullptr;
+    SGPU_TRY(ws_get(ctx, slot, sizeof(__nv_bfloat16) * 3 * (size_t)rows * cols, (void **)&base));
+    for (int i = 0; i < 3; i++) parts[i] = base + (size_t)i * rows * cols;
+    const dim3 grid((unsigned)std::max<long>(1, std::min<long>((rows + 1023) / 1024, 64)), cols);
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    k_split3_bf16<<<grid, 256, 0, st>>>(x, ldx, rows, parts[0], parts[1], parts[2]);
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
+// C (m x n, FP32) = op(A) op(B) from the three parts of each operand
+static int gemm_split3(sgpu_ctx *ctx, cublasOperation_t ta, cublasOperation_t tb, int m, int n,
+                       int k, __nv_bfloat16 *const *A, int lda, __nv_bfloat16 *const *B, int ldb,
+                       float *C, int ldc, cudaStream_t st)
+{
+    static const int terms[6][2] = {{2, 0}, {0, 2}, {1, 1}, {1, 0}, {0, 1}, {0, 0}};
+    const float one = 1.f, zero = 0.f;
+    for (int t = 0; t < 6; t++) {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasGemmEx(ctx->cublas, ta, tb, m, n, k, &one, A[terms[t][0]],
+                                     CUDA_R_16BF, lda, B[terms[t][1]], CUDA_R_16BF, ldb,
+                                     t == 0 ? &zero : &one, C, CUDA_R_32F, ldc,
+                                     CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
+    }
+    return SGPU_OK;
+}
+
+// The same for FP32 blocks: FP32-accurate products, accumulated in FP32, then widened to FP64
+// for the eigensolver. gemm_mode 0 / 1: cuBLAS FP32 GEMM with the BF16x9 emulation requested
+// (performant / eager strategy); 2: the three-part BF16 split above on the tensor cores.
 int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
                 double *Hp, double *Mp, cudaStream_t st)
 {
@@ -92,7 +151,16 @@ int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *
     float *tmp = nullptr;
     SGPU_TRY(ws_get(ctx, WS_EIG, sizeof(float) * 2 * (size_t)ncol * ncol, (void **)&tmp));
     const float one = 1.f, zero = 0.f;
-    for (int w = 0; w < 2; w++) {
+    if (ctx->gemm_mode == 2) {
+        __nv_bfloat16 *ys[3], *hs[3];
+        SGPU_TRY(split3(ctx, Y, ldy, ctx->Nd, ncol, WS_SPLIT_A, ys, st));
+        SGPU_TRY(split3(ctx, HY, ldh, ctx->Nd, ncol, WS_SPLIT_B, hs, st));
+        SGPU_TRY(gemm_split3(ctx, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol, (int)ctx->Nd, ys,
+                             (int)ctx->Nd, ys, (int)ctx->Nd, tmp, ncol, st));
+        SGPU_TRY(gemm_split3(ctx, CUBLAS_OP_T, CUBLAS_OP_N, ncol, ncol, (int)ctx->Nd, ys,
+                             (int)ctx->Nd, hs, (int)ctx->Nd, tmp + (size_t)ncol * ncol, ncol, st));
+    }
+    for (int w = 0; w < 2 && ctx->gemm_mode != 2; w++) {
         const float *B = w == 0 ? Y : HY;
         const long ldb = w == 0 ? ldy : ldh;
         ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
@@ -260,6 +328,13 @@ int rotate_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const double *
     {
         ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
         SGPU_TRY(convert_cols<double, float>(Q, ncol, q32, ncol, ncol, ncol, st));
+    }
+    if (ctx->gemm_mode == 2) {
+        __nv_bfloat16 *ys[3], *qs[3];
+        SGPU_TRY(split3(ctx, Y, ldy, ctx->Nd, ncol, WS_SPLIT_A, ys, st));
+        SGPU_TRY(split3(ctx, q32, ncol, ncol, ncol, WS_SPLIT_B, qs, st));
+        return gemm_split3(ctx, CUBLAS_OP_N, CUBLAS_OP_N, (int)ctx->Nd, ncol, ncol, ys,
+                           (int)ctx->Nd, qs, ncol, X, (int)ldx, st);
     }
     const float one = 1.f, zero = 0.f;
     ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);

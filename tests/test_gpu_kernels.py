@@ -377,8 +377,8 @@ def test_carried_projections_column_edges(gpu_available, ncol, cpl):
     assert ctx.kernel_status() == 0
 
 
-@pytest.mark.parametrize("eager", [False, True])
-def test_fp32_rayleigh_ritz_products(gpu_available, eager):
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_fp32_rayleigh_ritz_products(gpu_available, mode):
     """sgpu_Project_Hamiltonian_f32 / sgpu_Subspace_Rotation_f32 (tensor-core products with
     FP32-accurate BF16x9 splitting) against FP64 products of the same FP32 inputs, with H
     from the oracle: relative error within FP32 accumulation over Nd terms (1e-4)."""
@@ -386,7 +386,7 @@ def test_fp32_rayleigh_ritz_products(gpu_available, eager):
     grid, nl, veff, rng = _random_case((30, 26, 22), seed=51, natom=4)
     Nd = 30 * 26 * 22
     ctx = make_ctx(grid, nl, veff)
-    ctx.set_gemm_emulation(eager)
+    ctx.set_gemm_emulation(mode)
     o = Oracle(grid, nl)
     ncol = 40
     y = rng.uniform(-1, 1, (ncol, Nd)).astype(np.float32)
