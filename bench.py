@@ -490,6 +490,27 @@ def rr_gemm_block(sg, torch, dev, device=0, steps=3):
             out[name]["projection_products_tflops"] = round(
                 2 * gemm / ((t_proj - t_h) / 1e3) / 1e12, 2)
         del Y, HY, X
+    # the FP64 generalized eigensolve of the subspace (cuSOLVER dsygvd), once per filter pass
+    A = torch.rand((ns, ns), device=dev, dtype=torch.float64) - 0.5
+    H0 = (A + A.T).contiguous()
+    B = torch.rand((ns, ns), device=dev, dtype=torch.float64) / ns
+    M0 = (B @ B.T + torch.eye(ns, device=dev, dtype=torch.float64)).contiguous()
+    Hp, Mp = H0.clone(), M0.clone()
+    lam = torch.empty(ns, device=dev, dtype=torch.float64)
+
+    def eig():
+        Hp.copy_(H0)
+        Mp.copy_(M0)
+        ctx.Solve_Generalized_EigenProblem(Hp, Mp, lam)
+
+    for _ in range(2):
+        eig()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        eig()
+    torch.cuda.synchronize()
+    out["generalized_eig_fp64_ms"] = round((time.perf_counter() - t0) / steps * 1e3, 3)
     ctx.close()
     return out
 
