@@ -4,7 +4,7 @@ References: the reference program's own outputs for the Si8 system (Calculate_Vx
 Calculate_elecstPotential on the initial density, the converged SCF energies and
 eigenvalues), numpy/LAPACK for the dense Rayleigh-Ritz step, and the CPU oracle.
 Tolerances: pointwise FP64 maps 1e-12 relative; iterative solves at their stopping tolerance;
-SCF energy 1e-5 Ha/atom and occupied eigenvalues 1e-5 Ha (the spec bars)."""
+SCF energy 1e-5 Ha/atom and occupied eigenvalues 1e-5 Ha (the parity bars of the SCF)."""
 import numpy as np
 import pytest
 
