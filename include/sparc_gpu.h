@@ -100,9 +100,10 @@ int sgpu_Vnl_vec_mult(sgpu_ctx *ctx, int ncol, const double *x, int ldi, double 
  * It allocates nothing: the projection coefficients live in a fixed 8 MiB scratch array
  * inside the library (held on every GPU that loads the library until exit), so
  * n_proj * round_up(ncol, 8) must not exceed 1048576 (larger requests return SGPU_ERR_ARG);
- * x and Hx must be device pointers. The first call on a device looks up the scratch
- * address on that device; make it before any stream capture. All calls share the scratch
- * (each clears it first): calls that overlap on the GPU race and must be serialised. */
+ * x and Hx must be device pointers. Each CUDA context holds its own copy of the array; the
+ * first call in a context looks up its address there, so make it before any stream capture.
+ * All calls in one context share that array (each clears it first): calls that overlap on
+ * the GPU race and must be serialised. */
 int sgpu_Vnl_vec_mult_noalloc(sgpu_ctx *ctx, int ncol, const double *x, int ldi, double *Hx,
                               int ldo);
 
@@ -441,6 +442,12 @@ int sgpu_kernel_status(sgpu_ctx *ctx, int *status);
  * the status word and the block exits; this call returns that word in *status (2 when the
  * bound works) and leaves it cleared. No copy is in flight and nothing faults. */
 int sgpu_check_wait_bound(sgpu_ctx *ctx, int *status);
+
+/* Measures this GPU's FP64 FMA rate (TFLOP/s, an FMA counted as two flops) with one
+ * arithmetic-only kernel timed by CUDA events on the context stream: the ceiling of the FP64
+ * stencil and nonlocal kernels, which on this part are bound by the FP64 pipe rather than by
+ * HBM. No counterpart in the reference (a measurement aid). */
+int sgpu_measure_fp64_rate(sgpu_ctx *ctx, double *tflops);
 
 /* ------------------------------------------------------ learned initial density */
 /* No counterpart in the reference, which starts each SCF from the superposition of atomic

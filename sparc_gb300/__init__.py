@@ -41,7 +41,7 @@ EXPORTED = [
     "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
     "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
-    "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation",
+    "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation", "sgpu_measure_fp64_rate",
 ]
 
 
@@ -604,6 +604,12 @@ class Context:
         ms = (ctypes.c_double * 2)()
         _check(lib().sgpu_get_nonlocal_fuse(self._h, ctypes.byref(mode), ms))
         return mode.value != 0, int(mode.value), [float(ms[0]), float(ms[1])]
+
+    def measure_fp64_rate(self):
+        """This GPU's FP64 FMA rate in TFLOP/s (sgpu_measure_fp64_rate)."""
+        t = ctypes.c_double()
+        _check(lib().sgpu_measure_fp64_rate(self._h, ctypes.byref(t)))
+        return float(t.value)
 
     def check_wait_bound(self):
         """Run the bounded-wait diagnostic; returns the status word it left (2 when a wait

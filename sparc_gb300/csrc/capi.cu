@@ -655,6 +655,17 @@ int sgpu_check_wait_bound(sgpu_ctx *ctx, int *status)
     return SGPU_ERR_STATE;
 }
 
+int sgpu_measure_fp64_rate(sgpu_ctx *ctx, double *tflops)
+{
+    SGPU_TRY(check_ctx(ctx));
+    if (!tflops) {
+        set_error("sgpu_measure_fp64_rate: null argument");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_CUDA_TRY(cudaSetDevice(ctx->device));
+    return fp64_fma_rate(ctx, tflops);
+}
+
 int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms)
 {
     if (!ctx || !ms) {

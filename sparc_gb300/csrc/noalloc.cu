@@ -13,12 +13,14 @@
 //  * scratch holds kNoallocScratchDoubles doubles (8 MiB): n_proj * round_up(ncol, 8) must fit,
 //    larger requests are rejected with SGPU_ERR_ARG before anything is launched;
 //  * x and Hx must be device pointers (staging host arrays would need device buffers);
-//  * the first call on a device looks up the scratch array's device address on that device
-//    (cudaGetSymbolAddress, with that device current) and caches it; make that first call
-//    before any stream capture;
-//  * all calls share the one array and each call clears it before use: calls whose work
-//    overlaps on the GPU (different streams, threads or contexts of the same device) race
-//    on it and must be serialised by the caller.
+//  * the first call in a CUDA context looks up the scratch array's device address in that
+//    context (cudaGetSymbolAddress, with the context's device current) and caches it under the
+//    context's unique id; make that first call before any stream capture. Each context holds
+//    its own copy of the array (a context loads its own copy of the library's device image),
+//    and a context created after cudaDeviceReset gets a new id, so no stale address is used;
+//  * all calls in one context share its array and each call clears it before use: calls whose
+//    work overlaps on the GPU (different streams or threads using the same context) race on
+//    it and must be serialised by the caller.
 #include <mutex>
 
 #include "sgpu_internal.h"
@@ -26,32 +28,75 @@
 namespace {
 
 constexpr long kNoallocScratchDoubles = 1L << 20;  // 8 MiB
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoallocScratchDoubles];
 
 std::mutex g_noalloc_mutex;
-double *g_noalloc_ptr[kMaxDevices] = {nullptr};
 
-// device address of the scratch array on the current device (looked up once per device)
-int noalloc_scratch(int device, double **out)
+// driver entry points, resolved through the runtime (the library does not link libcuda)
+typedef int (*ctx_get_current_fn)(void **ctx);
+typedef int (*ctx_get_id_fn)(void *ctx, unsigned long long *id);
+ctx_get_current_fn g_ctx_get_current = nullptr;
+ctx_get_id_fn g_ctx_get_id = nullptr;
+
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    double *ptr;
+};
+constexpr int kCacheSlots = 64;
+ScratchEntry g_noalloc_cache[kCacheSlots];
+int g_noalloc_cached = 0;
+int g_noalloc_next = 0;  // slot replaced next once the table is full
+
+// unique id of the CUDA context current on this thread (call with g_noalloc_mutex held)
+int current_context_id(unsigned long long *id)
 {
-    if (device < 0 || device >= kMaxDevices) {
-        sgpu::set_error("Vnl_vec_mult_noalloc: device ordinal out of range");
-        return SGPU_ERR_ARG;
-    }
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device]) {
-        double *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            sgpu::set_error(std::string("Vnl_vec_mult_noalloc: cudaGetSymbolAddress: ") +
-                            cudaGetErrorString(e));
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                          cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000,
+                                                          cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+            sgpu::set_error("Vnl_vec_mult_noalloc: cannot resolve cuCtxGetCurrent/cuCtxGetId");
             return SGPU_ERR_CUDA;
         }
-        g_noalloc_ptr[device] = p;
+        g_ctx_get_current = (ctx_get_current_fn)f1;
+        g_ctx_get_id = (ctx_get_id_fn)f2;
     }
-    *out = g_noalloc_ptr[device];
+    void *cu_ctx = nullptr;
+    if (g_ctx_get_current(&cu_ctx) != 0 || !cu_ctx || g_ctx_get_id(cu_ctx, id) != 0) {
+        sgpu::set_error("Vnl_vec_mult_noalloc: no current CUDA context");
+        return SGPU_ERR_CUDA;
+    }
+    return SGPU_OK;
+}
+
+// device address of the scratch array in the current context (looked up once per context)
+int noalloc_scratch(double **out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    unsigned long long id = 0;
+    SGPU_TRY(current_context_id(&id));
+    for (int i = 0; i < g_noalloc_cached; ++i)
+        if (g_noalloc_cache[i].ctx_id == id) {
+            *out = g_noalloc_cache[i].ptr;
+            return SGPU_OK;
+        }
+    double *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        sgpu::set_error(std::string("Vnl_vec_mult_noalloc: cudaGetSymbolAddress: ") +
+                        cudaGetErrorString(e));
+        return SGPU_ERR_CUDA;
+    }
+    int slot = g_noalloc_cached < kCacheSlots ? g_noalloc_cached++ : g_noalloc_next;
+    if (slot == g_noalloc_next && g_noalloc_cached == kCacheSlots)
+        g_noalloc_next = (g_noalloc_next + 1) % kCacheSlots;
+    g_noalloc_cache[slot] = {id, p};
+    *out = p;
     return SGPU_OK;
 }
 
@@ -85,7 +130,7 @@ extern "C" int sgpu_Vnl_vec_mult_noalloc(sgpu_ctx *ctx, int ncol, const double *
         return SGPU_ERR_ARG;
     }
     double *alpha = nullptr;
-    SGPU_TRY(noalloc_scratch(ctx->device, &alpha));
+    SGPU_TRY(noalloc_scratch(&alpha));
     // the array keeps the previous call's contents: clear the part this call accumulates into
     SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, sizeof(double) * (size_t)need, ctx->stream));
     SGPU_TRY(launch_nonlocal_project<double>(ctx, ncol, x, ldi, alpha, lda, ctx->stream));

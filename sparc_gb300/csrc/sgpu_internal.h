@@ -195,6 +195,7 @@ enum WsSlot {
 
 // grow-only device scratch
 int ws_get(sgpu_ctx *ctx, int slot, size_t bytes, void **out);
+int fp64_fma_rate(sgpu_ctx *ctx, double *tflops);
 
 // profiling: returns an event pair recorded around a launch of `kind` (or nulls when off)
 struct ProfScope {

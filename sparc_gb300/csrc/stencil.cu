@@ -892,7 +892,8 @@ struct BulkShape {
     static constexpr size_t data_bytes = sizeof(float) * ((size_t)NR * SLOT + (size_t)NV * BX * BY);
     static constexpr size_t bar_bytes = (8 * (2 * NR + NV) + 15) / 16 * 16;
     static constexpr int NDESC = 32 + BY;       // row descriptors: ring rows 0.., z rows 32..
-    static constexpr size_t smem_bytes = data_bytes + bar_bytes + 16 * NDESC;
+    // + one 16-byte word after the descriptors: the block's abort flag
+    static constexpr size_t smem_bytes = data_bytes + bar_bytes + 16 * (NDESC + 1);
     static_assert(H <= 32 && BY <= 32 && NR + NV <= 32 && NT >= 64, "one lane per tile row");
     static_assert(data_bytes % 16 == 0 && (SLOT * sizeof(float)) % 16 == 0, "16-byte slots");
 };
@@ -926,7 +927,10 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     int4 *const desc = reinterpret_cast<int4 *>(reinterpret_cast<char *>(ring) + S::data_bytes +
                                                 S::bar_bytes);
     constexpr int NW = S::NT / 32;
+    // set once any wait of the block has run out: from then on no copy is issued
+    volatile int *const abort_flag = reinterpret_cast<volatile int *>(desc + S::NDESC);
     if (tid == 0) {
+        *abort_flag = 0;
         for (int s = 0; s < NR; s++) {
             mbar_init(bfull + 8u * s, 1);
             mbar_init(bempty + 8u * s, NW);
@@ -966,13 +970,19 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     bool alive = true;    // false once one of this thread's waits has run out
     unsigned ph = 0;      // parity of the next wait: bits 0..NR-1 full, NR.. zfull
     unsigned phe = 0;     // parity of the next wait on empty (issuing warps)
+    int ring_end = zs;    // ring planes zs .. ring_end-1 issued (warp 0)
+    int z_end = zs;       // recurrence-term planes zs .. z_end-1 issued (warp 1)
     auto wait = [&](unsigned bar, int bit, unsigned &bits) {
         if (alive && !mbar_wait_bounded(bar, (bits >> bit) & 1u)) {
             alive = false;
+            *abort_flag = 1;  // visible to an issuing warp through its next empty wait
             if (p.status) atomicOr(p.status, 1);
         }
         bits ^= 1u << bit;
     };
+    // an issuing warp stops for good once its own wait or any other warp's has run out: a
+    // copy into a slot whose release was not seen could overwrite data still being read
+    auto may_issue = [&]() { return alive && *abort_flag == 0; };
     // one row per lane: ring rows from warp 0 (descriptors 0..H-1), recurrence-term rows from
     // warp 1 (32..32+BY-1); pb = the plane's first element, sbase = the slot's shared address
     auto issue_row = [&](const int4 d, const float *pb, unsigned sbase, unsigned bar, int xs) {
@@ -986,6 +996,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     };
     // ring plane pl (zs <= pl < 2 Nz) into ring slot s
     auto issue_ring = [&](int pl, int s) {
+        ring_end = pl + 1;
         const unsigned bar = bfull + 8u * s;
         if (lane == 0) mbar_arrive_tx(bar, S::plane_bytes);
         __syncwarp();
@@ -997,6 +1008,7 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
     };
     // recurrence-term plane pl (zs <= pl < Nz) into its slot s
     auto issue_z = [&](int pl, int s) {
+        z_end = pl + 1;
         const unsigned bar = bzfull + 8u * s;
         if (lane == 0) mbar_arrive_tx(bar, S::zplane_bytes);
         __syncwarp();
@@ -1031,8 +1043,9 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
             if (k + D < ze && (warp == 0 || (warp == 1 && zc))) {                                \
                 const int se = sk == 0 ? NR - 1 : sk - 1;                                        \
                 if (k > zs) wait(bempty + 8u * se, se, phe);                                     \
-                if (warp == 0) issue_ring(k + R + D, se);                                        \
-                else issue_z(k + D, svk == 0 ? NV - 1 : svk - 1);                                \
+                const bool go = __all_sync(0xffffffffu, may_issue());                            \
+                if (go && warp == 0) issue_ring(k + R + D, se);                                  \
+                else if (go) issue_z(k + D, svk == 0 ? NV - 1 : svk - 1);                       \
             }                                                                                    \
             const int skr = sk + R >= NR ? sk + R - NR : sk + R;                                 \
             if (k < zs + R) wait(bfull + 8u * sk, sk, ph);                                       \
@@ -1075,19 +1088,19 @@ __global__ void __launch_bounds__(BX / 2 * (BY / 2), MINB)
         SGPU_BULK_STEP(12)
     }
 #undef SGPU_BULK_STEP
-    // no copy may land after the block exits: wait for the last fill of every slot (planes
-    // zs .. ze+R-1 of the ring, zs .. ze-1 of the recurrence term were issued)
-    if (tid == 0) {
+    // no copy may land after the block exits: each issuing warp waits for the last fill it
+    // issued into each of its slots (ring planes zs .. ring_end-1 from warp 0, recurrence-term
+    // planes zs .. z_end-1 from warp 1; fewer than planned if a wait ran out)
+    if ((warp == 0 || (warp == 1 && zc)) && lane == 0) {
         bool ok = true;
-        for (int s = 0; s < NR; s++) {
-            const int last = ze + R - 1 - ((ze + R - 1 - s) % NR + NR) % NR;
-            if (last >= zs && !mbar_wait_bounded(bfull + 8u * s, ((last - zs) / NR) & 1)) ok = false;
+        const int nslot = warp == 0 ? NR : NV;
+        const int end = warp == 0 ? ring_end : z_end;
+        const unsigned base = warp == 0 ? bfull : bzfull;
+        for (int s = 0; s < nslot; s++) {
+            const int last = end - 1 - ((end - 1 - s) % nslot + nslot) % nslot;
+            if (last >= zs && !mbar_wait_bounded(base + 8u * s, ((last - zs) / nslot) & 1))
+                ok = false;
         }
-        if (zc)
-            for (int s = 0; s < NV; s++) {
-                const int last = ze - 1 - ((ze - 1 - s) % NV + NV) % NV;
-                if (last >= zs && !mbar_wait_bounded(bzfull + 8u * s, ((last - zs) / NV) & 1)) ok = false;
-            }
         if (!ok && p.status) atomicOr(p.status, 1);
     }
 }

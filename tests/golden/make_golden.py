@@ -1,6 +1,6 @@
 """Generate the committed golden fixtures from the reference SPARC program.
 
-Needs the reference sources (default /root/reference) and the oracle build
+Needs the reference sources ($SPARC_REFERENCE, default /root/reference) and the oracle build
 (`make -C oracle/ref REF=...`). For each system in systems.py it runs the reference's own
 set-up, records grid, FD weights and nonlocal projectors, then calls the reference kernels
 (Lap_plus_diag_vec_mult_orth, Vnl_vec_mult, Hamiltonian_vectors_mult, ChebyshevFiltering,
@@ -20,6 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 import systems  # noqa: E402
+
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+from oracle.refpath import reference_root  # noqa: E402
 
 
 def flatten_nonlocal(types, images, n_atom):
@@ -151,6 +154,28 @@ def capture_scf(sysd, psp_dir, out_npz, out_json, sparc_bin):
         json.dump(ref, fh, indent=1)
 
 
+def capture_scf_result(sysd, psp_dir, out_json, sparc_bin):
+    """Reference SCF result only (energies, eigenvalues, occupations, forces, wall time), for
+    systems too large to store their set-up as a fixture (Si216: the GPU side builds its own
+    set-up, which is pinned on the smaller systems)."""
+    import json
+    import subprocess
+    from ref_capture import parse_reference_outputs
+
+    tmp = tempfile.mkdtemp(prefix="sparc_scf_")
+    base = systems.write_system(sysd, tmp, psp_dir)
+    nthr = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(nthr), OPENBLAS_NUM_THREADS=str(nthr))
+    subprocess.run([sparc_bin, "-name", os.path.basename(base)], cwd=tmp, env=env, check=True,
+                   stdout=subprocess.DEVNULL)
+    ref = parse_reference_outputs(base)
+    ref["system"] = sysd["name"]
+    ref["where"] = (f"reference program, single rank (MPI stub) + {nthr}-thread OpenBLAS, "
+                    "x86 build host")
+    with open(out_json, "w") as fh:
+        json.dump(ref, fh, indent=1)
+
+
 def capture_setup(sysd, psp_dir, out_npz):
     """Inputs and outputs of the reference's per-geometry set-up: parsed pseudopotential
     tables, atom positions as read, pseudocharge cut-offs, pseudocharge densities, initial and
@@ -185,12 +210,20 @@ def capture_setup(sysd, psp_dir, out_npz):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "setup"], default=None,
+    ap.add_argument("--ref", default=reference_root(),
+                    help="reference tree (default: $SPARC_REFERENCE, else /root/reference)")
+    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "setup", "si216"], default=None,
                     help="regenerate one group of fixtures only")
     args = ap.parse_args()
     psp_dir = os.path.join(args.ref, "psps")
     ctx = mp.get_context("spawn")
+    if args.only == "si216":
+        # about half an hour on 8 x86 threads; not part of the default run
+        sparc_bin = os.path.join(HERE, "..", "..", "oracle", "_ref", "sparc")
+        js = os.path.join(HERE, "Si216_c4_scf_ref.json")
+        capture_scf_result(systems.si216_c4(), psp_dir, js, sparc_bin)
+        print("wrote", js)
+        return
     if args.only in (None, "setup"):
         for sysd in (systems.si2_small(), systems.si8_c1(), systems.al4_small()):
             path = os.path.join(HERE, f"{sysd['name']}_setup.npz")

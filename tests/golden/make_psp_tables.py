@@ -11,6 +11,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 
+from oracle.refpath import reference_root  # noqa: E402
 from sparc_gb300.psp8 import read_psp8, save_tables  # noqa: E402
 
 FILES = {"Si": "14_Si_4_1.9_1.9_pbe_n_v1.0.psp8", "Al": "13_Al_3_1.9_1.9_pbe_n_v1.0.psp8"}
@@ -18,7 +19,8 @@ FILES = {"Si": "14_Si_4_1.9_1.9_pbe_n_v1.0.psp8", "Al": "13_Al_3_1.9_1.9_pbe_n_v
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=reference_root(),
+                    help="reference tree (default: $SPARC_REFERENCE, else /root/reference)")
     args = ap.parse_args()
     for el, fn in FILES.items():
         tab = read_psp8(os.path.join(args.ref, "psps", fn), el)

@@ -9,12 +9,13 @@ import os
 import numpy as np
 import pytest
 
+from oracle.refpath import psps_dir
 from sparc_gb300.psp8 import Psp8Error, load_tables, read_psp8
 from sparc_gb300.setup import grid_from_mesh, ion_coordinates
 from sparc_gb300.synthetic import fd_d2_coeffs
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_PSPS = "/root/reference/psps"
+REF_PSPS = psps_dir()
 FIELDS = ("RadialGrid", "UdV", "rVloc", "rhoIsoAtom", "rho_c_table", "Gamma", "rc", "ppl")
 CASES = [("Si2_small", "Si"), ("Si8_c1", "Si"), ("Al4_small", "Al")]
 

@@ -8,9 +8,11 @@ import os
 import numpy as np
 import pytest
 
+from oracle.refpath import psps_dir
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libsparc_ref.so")
-PSPS = "/root/reference/psps"
+PSPS = psps_dir()
 
 pytestmark = pytest.mark.skipif(not (os.path.exists(REF_LIB) and os.path.isdir(PSPS)),
                                 reason="reference build not present")
