@@ -339,6 +339,9 @@ def scf_c4_block(sg, torch=None, device=0):
             lr, orr = np.array(ref["lambda"]), np.array(ref["occ"])
             occd = orr > 1e-3
             rec["max_occ_eig_err_vs_ref"] = float(np.abs(lam[occd] - lr[occd]).max())
+            if ref.get("forces"):
+                rec["max_force_err_vs_ref_Ha_per_Bohr"] = float(
+                    np.abs(F - np.array(ref["forces"])).max())
         out[name] = rec
     out["speedup_mixed_vs_fp64"] = round(out["fp64"]["time_s"] / out["mixed"]["time_s"], 3)
     t64 = out["fp64"]["time_to_1e-5_Ha_per_atom_s"]
@@ -465,8 +468,9 @@ def run_reference(args):
 
 def rr_gemm_block(sg, torch, dev, device=0, steps=3):
     """The Rayleigh-Ritz products at the Si216 shapes (77^3 grid at h = 0.40, 520 states):
-    the mixed SCF's FP32 forms (tensor cores, BF16x9-split products, FP32 accumulation) and
-    the FP64 forms (DGEMM/DSYRK), timed with CUDA events on the library's stream, with the
+    the library's tcgen05 split-slice products (FP32-accurate on FP32 blocks, FP64-accurate on
+    FP64 blocks), cuBLAS's FP32 forms (BF16x9 emulation requested, eager, three-part BF16
+    split) and cuBLAS DGEMM/DSYRK, timed with CUDA events on the library's stream, with the
     achieved TFLOP/s of the rotation (one GEMM, 2 Nd Ns^2 flops) and of the two products of
     the projection (2 Nd Ns^2 each; its H Y apply timed and subtracted)."""
     from sparc_gb300.synthetic import fd_d2_coeffs, gaussian_potential
@@ -478,8 +482,12 @@ def rr_gemm_block(sg, torch, dev, device=0, steps=3):
     nd = N[0] * N[1] * N[2]
     stream = torch.cuda.ExternalStream(ctx.stream())
     out = {"shape": f"Nd = {nd} (77^3), Ns = {ns}"}
-    for name, dt in (("fp32", torch.float32), ("fp32_eager", torch.float32),
+    for name, dt in (("fp32_tc", torch.float32), ("fp64_tc", torch.float64),
+                     ("fp32", torch.float32), ("fp32_eager", torch.float32),
                      ("fp32_bf16_split", torch.float32), ("fp64", torch.float64)):
+        # *_tc: the library's tcgen05 split-slice products (FP32-accurate on FP32 blocks,
+        # FP64-accurate on FP64 blocks); the others: cuBLAS
+        ctx.set_rr_products({"fp32_tc": 1, "fp64_tc": 2}.get(name, 0))
         ctx.set_gemm_emulation({"fp32_eager": 1, "fp32_bf16_split": 2}.get(name, 0))
         Y = torch.rand((ns, nd), device=dev, dtype=dt) - 0.5
         HY = torch.empty_like(Y)
@@ -487,12 +495,12 @@ def rr_gemm_block(sg, torch, dev, device=0, steps=3):
         Hp = torch.empty((ns, ns), device=dev, dtype=torch.float64)
         Mp = torch.empty_like(Hp)
         Q = (torch.rand((ns, ns), device=dev, dtype=torch.float64) - 0.5) / ns ** 0.5
-        f32 = name != "fp64"
+        f32 = dt == torch.float32
         proj = (lambda: ctx.Project_Hamiltonian_f32(Y, HY, Hp, Mp)) if f32 else \
             (lambda: ctx.Project_Hamiltonian(Y, HY, Hp, Mp))
         rot = (lambda: ctx.Subspace_Rotation_f32(Y, Q, X)) if f32 else \
             (lambda: ctx.Subspace_Rotation(Y, Q, X))
-        ham = (lambda: ctx.Hamiltonian_vectors_mult(0.0, Y, HY)) if name == "fp64" else None
+        ham = (lambda: ctx.Hamiltonian_vectors_mult(0.0, Y, HY)) if not f32 else None
 
         def timed_ms(fn):
             for _ in range(2):

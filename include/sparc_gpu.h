@@ -205,7 +205,8 @@ int sgpu_Subspace_Rotation(sgpu_ctx *ctx, const double *Y, int ldi, const double
 /* The Rayleigh-Ritz products of the mixed SCF's FP32 phase on device FP32 blocks (for callers
  * that keep the orbitals in FP32, beside sgpu_ChebyshevFiltering_f32): HY = H Y in FP32, then
  * Hp = Yᵀ HY and Mp = Yᵀ Y, and X = Y Q, as FP32-accurate products with FP32 accumulation
- * (cuBLAS FP32 GEMM or BF16 split products on the tensor cores: sgpu_set_gemm_emulation);
+ * (the library's tcgen05 split-slice kernels, sgpu_set_rr_products; or cuBLAS,
+ * sgpu_set_gemm_emulation);
  * Hp, Mp and Q are FP64 (host or device). FP32-precision counterparts of the two calls
  * above. */
 int sgpu_Project_Hamiltonian_f32(sgpu_ctx *ctx, int spin, const float *Y, int ldi, float *HY,
@@ -519,6 +520,21 @@ int sgpu_set_nonlocal_project_variant(sgpu_ctx *ctx, int variant);
  * FP32 operand split into three BF16 parts and the product formed from six BF16 GEMMs on the
  * tensor cores (the part products of order <= 2, smallest first). */
 int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode);
+
+/* Where the Rayleigh-Ritz products Mp = Yᵀ Y, Hp = Yᵀ HY (DP_Project_Hamiltonian,
+ * src/eigenSolver.c:1022-1033) and X = Y Q (DP_Subspace_Rotation, :1415) run.
+ * mode 1: on the library's own tcgen05 kernels, every operand row scaled by a power of two
+ * and cut into 7-bit BF16 slices whose products accumulate exactly in tensor memory (chunks
+ * of 512) and are then summed in compensated arithmetic: FP32-accurate (3 slices, 6 slice
+ * products) for FP32 blocks (sgpu_Project_Hamiltonian_f32, sgpu_Subspace_Rotation_f32, the
+ * mixed SCF's FP32 phase) and FP64-accurate (6 slices, 21 products) for the mixed SCF's FP64
+ * phase after the switch; plain FP64 calls (sgpu_Project_Hamiltonian,
+ * sgpu_Subspace_Rotation, the plain FP64 SCF) keep cuBLAS DSYRK/DGEMM, the drop-in.
+ * mode 2: the FP64-accurate tensor-core products for the plain FP64 calls too.
+ * mode 0: cuBLAS everywhere (sgpu_set_gemm_emulation then picks the FP32-block form).
+ * The Gram products compute the upper triangle and mirror it. No counterpart in the
+ * reference (which calls cblas_dgemm). */
+int sgpu_set_rr_products(sgpu_ctx *ctx, int mode);
 
 /* FP32 filter with the projections carried across degrees (mode 1, 2 or 4) or not (0). When
  * on, every degree's nonlocal apply is the range form with the projection of the iterate it

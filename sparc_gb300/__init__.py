@@ -42,6 +42,7 @@ EXPORTED = [
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
     "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
     "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation", "sgpu_measure_fp64_rate",
+    "sgpu_set_rr_products",
 ]
 
 
@@ -604,6 +605,11 @@ class Context:
         ms = (ctypes.c_double * 2)()
         _check(lib().sgpu_get_nonlocal_fuse(self._h, ctypes.byref(mode), ms))
         return mode.value != 0, int(mode.value), [float(ms[0]), float(ms[1])]
+
+    def set_rr_products(self, mode):
+        """Rayleigh-Ritz products: 1 tensor-core split slices for FP32 blocks and the mixed
+        SCF's FP64 phase, 2 also for plain FP64 calls, 0 cuBLAS (sgpu_set_rr_products)."""
+        _check(lib().sgpu_set_rr_products(self._h, int(mode)))
 
     def measure_fp64_rate(self):
         """This GPU's FP64 FMA rate in TFLOP/s (sgpu_measure_fp64_rate)."""

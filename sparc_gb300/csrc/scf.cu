@@ -720,7 +720,10 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 SGPU_TRY(chebyshev_graded(ctx, 0, X32, Y32, X64, Y64, Ns, m,
                                           prm->tail_fp64_degrees, cutoff, eigmax, eigmin, st));
                 SGPU_TRY(hamiltonian_dev<double>(ctx, 0, Ns, 0.0, Y64, N, X64, N, 1.0, 0.0, nullptr, 0, st));
-                SGPU_TRY(project_f64(ctx, Ns, Y64, N, X64, N, d_Hp, d_Mp, st));
+                if (ctx->rr_tc)  // FP64-accurate split products on the tensor cores
+                    SGPU_TRY(tc_project<double>(ctx, Ns, Y64, N, X64, N, d_Hp, d_Mp, true, st));
+                else
+                    SGPU_TRY(project_f64(ctx, Ns, Y64, N, X64, N, d_Hp, d_Mp, st));
             } else {
                 SGPU_TRY(chebyshev_dev<double>(ctx, 0, X64, N, Y64, N, Ns, m, cutoff, eigmax, eigmin, st));
                 SGPU_TRY(hamiltonian_dev<double>(ctx, 0, Ns, 0.0, Y64, N, X64, N, 1.0, 0.0, nullptr, 0, st));
@@ -733,6 +736,9 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
             filter_ms += ms;
             if (mixed) {
                 SGPU_TRY(rotate_f32(ctx, Ns, Y32, N, d_Hp, X32, N, st));
+            } else if (graded && ctx->rr_tc) {
+                SGPU_TRY(tc_rotate<double>(ctx, Ns, Y64, N, d_Hp, Ns, X64, N, true, st));
+                SGPU_TRY(convert_cols<double, float>(X64, nb, X32, nb, nb, 1, st));
             } else {
                 SGPU_TRY(rotate_f64(ctx, Ns, Y64, N, d_Hp, X64, N, st));
                 // the graded filter starts from an FP32 copy of the rotated orbitals

@@ -148,7 +148,7 @@ struct sgpu_ctx {
     bool has_nl = false;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
-    sgpu::Workspace ws[15];    // grow-only scratch slots (see enum WsSlot)
+    sgpu::Workspace ws[16];    // grow-only scratch slots (see enum WsSlot)
     sgpu::MixState *mix = nullptr;
     sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)
     sgpu::SetupState *setup = nullptr;  // pseudopotential tables (set-up calls)
@@ -163,7 +163,11 @@ struct sgpu_ctx {
     int nl_fuse_cpl = 2;   // fused apply: columns per lane (2 or 4), chosen by the tuner
     int gemm_mode = 0;  // FP32-block products: 0 cuBLAS FP32 GEMM (BF16x9 emulation where
                         // cuBLAS expects a gain), 1 the same with eager emulation, 2 the
-                        // library's three-part BF16 split on the tensor cores
+                        // library's three-part BF16 split on the tensor cores (cuBLAS GEMMs)
+    int rr_tc = 0;      // Rayleigh-Ritz products on the library's own tcgen05 split-slice
+                        // kernels (rr_tc.cu): 1 for FP32 blocks (FP32-accurate) and the mixed
+                        // SCF's FP64 phase (FP64-accurate), 2 also for plain FP64 calls;
+                        // 0 cuBLAS
     double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
     double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
@@ -190,7 +194,8 @@ namespace sgpu {
 
 enum WsSlot {
     WS_STAGE_A = 0, WS_STAGE_B, WS_STAGE_C, WS_ALPHA, WS_MISC, WS_EIG, WS_POIS, WS_MIX,
-    WS_RED, WS_RHS, WS_SCF, WS_SCF2, WS_ALPHA2, WS_SPLIT_A, WS_SPLIT_B
+    WS_RED, WS_RHS, WS_SCF, WS_SCF2, WS_ALPHA2, WS_SPLIT_A, WS_SPLIT_B, WS_TC_PART,
+    WS_COUNT
 };
 
 // grow-only device scratch
@@ -274,6 +279,12 @@ int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *
                 double *Hp, double *Mp, cudaStream_t st);
 int generalized_eig(sgpu_ctx *ctx, int n, double *Hp, double *Mp, double *lambda_dev,
                     cudaStream_t st);
+template <typename T>
+int tc_project(sgpu_ctx *ctx, int ncol, const T *Y, long ldy, const T *HY, long ldh, double *Hp,
+               double *Mp, bool fp64_accurate, cudaStream_t st);
+template <typename T>
+int tc_rotate(sgpu_ctx *ctx, int ncol, const T *Y, long ldy, const double *Q, int ldq, T *X,
+              long ldx, bool fp64_accurate, cudaStream_t st);
 int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *Q, double *X,
                long ldx, cudaStream_t st);
 int cholqr_f64(sgpu_ctx *ctx, int ncol, double *Y, long ldy, cudaStream_t st);

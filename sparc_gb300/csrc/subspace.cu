@@ -8,12 +8,13 @@
 //   DP_Subspace_Rotation              src/eigenSolver.c:1386-1439
 //       X = Y Q (cblas_dgemm :1415)
 //
-// GPU form: the products are plain GEMMs, so they go to cuBLAS: DSYRK/DGEMM in FP64 for the
-// drop-in, and for FP32 blocks (the mixed-precision filter) FP32 GEMMs with the BF16x9
-// emulated compute type requested (cuBLAS may then split each FP32 operand into three BF16
-// terms on the tensor cores; on this GB300 and cuBLAS it keeps its FP32 SIMT GEMM, measured at
-// 56 TFLOP/s at the Si216 shapes, either strategy). FP32 accumulation throughout. The Ns x Ns
-// generalized eigenproblem stays FP64 on cuSOLVER (dsygvd).
+// GPU form: with rr_tc set (sgpu_set_rr_products), FP32 blocks (the mixed-precision filter)
+// and the mixed-precision SCF's FP64 phase use the library's own tcgen05 kernels (rr_tc.cu:
+// split-slice BF16 products with exact chunk accumulation, FP32- or FP64-accurate); the plain
+// FP64 drop-in keeps cuBLAS DSYRK/DGEMM, and with rr_tc = 0 FP32 blocks go to cuBLAS FP32
+// GEMMs (BF16x9 emulation requested; on this GB300 cuBLAS keeps its FP32 SIMT GEMM, 56
+// TFLOP/s at the Si216 shapes). The Ns x Ns generalized eigenproblem stays FP64 on cuSOLVER
+// (dsygvd).
 #include <algorithm>
 
 #include <cuda_bf16.h>
@@ -63,6 +64,7 @@ __global__ void k_f32_to_f64(const float *__restrict__ a, double *__restrict__ b
 int project_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *HY,
                 long ldh, double *Hp, double *Mp, cudaStream_t st)
 {
+    if (ctx->rr_tc == 2) return tc_project<double>(ctx, ncol, Y, ldy, HY, ldh, Hp, Mp, true, st);
     SGPU_TRY(ensure_handles(ctx));
     SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
     const double one = 1.0, zero = 0.0;
@@ -146,6 +148,7 @@ static int gemm_split3(sgpu_ctx *ctx, cublasOperation_t ta, cublasOperation_t tb
 int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *HY, long ldh,
                 double *Hp, double *Mp, cudaStream_t st)
 {
+    if (ctx->rr_tc) return tc_project<float>(ctx, ncol, Y, ldy, HY, ldh, Hp, Mp, false, st);
     SGPU_TRY(ensure_handles(ctx));
     SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
     float *tmp = nullptr;
@@ -308,6 +311,7 @@ int standard_eig(sgpu_ctx *ctx, int n, double *Hp, double *lambda_dev, cudaStrea
 int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double *Q, double *X,
                long ldx, cudaStream_t st)
 {
+    if (ctx->rr_tc == 2) return tc_rotate<double>(ctx, ncol, Y, ldy, Q, ncol, X, ldx, true, st);
     SGPU_TRY(ensure_handles(ctx));
     SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
     const double one = 1.0, zero = 0.0;
@@ -321,6 +325,7 @@ int rotate_f64(sgpu_ctx *ctx, int ncol, const double *Y, long ldy, const double 
 int rotate_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const double *Q, float *X,
                long ldx, cudaStream_t st)
 {
+    if (ctx->rr_tc) return tc_rotate<float>(ctx, ncol, Y, ldy, Q, ncol, X, ldx, false, st);
     SGPU_TRY(ensure_handles(ctx));
     SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
     float *q32 = nullptr;

@@ -377,16 +377,21 @@ def test_carried_projections_column_edges(gpu_available, ncol, cpl):
     assert ctx.kernel_status() == 0
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode", ["tc", 0, 1, 2])
 def test_fp32_rayleigh_ritz_products(gpu_available, mode):
-    """sgpu_Project_Hamiltonian_f32 / sgpu_Subspace_Rotation_f32 (tensor-core products with
-    FP32-accurate BF16x9 splitting) against FP64 products of the same FP32 inputs, with H
-    from the oracle: relative error within FP32 accumulation over Nd terms (1e-4)."""
+    """sgpu_Project_Hamiltonian_f32 / sgpu_Subspace_Rotation_f32 against FP64 products of the
+    same FP32 inputs, with H from the oracle: the library's tcgen05 split-slice products
+    (sgpu_set_rr_products 1) and the cuBLAS forms (sgpu_set_gemm_emulation 0-2); relative
+    error within FP32 accumulation over Nd terms (1e-4)."""
     import torch
     grid, nl, veff, rng = _random_case((30, 26, 22), seed=51, natom=4)
     Nd = 30 * 26 * 22
     ctx = make_ctx(grid, nl, veff)
-    ctx.set_gemm_emulation(mode)
+    if mode == "tc":
+        ctx.set_rr_products(1)
+    else:
+        ctx.set_rr_products(0)
+        ctx.set_gemm_emulation(mode)
     o = Oracle(grid, nl)
     ncol = 40
     y = rng.uniform(-1, 1, (ncol, Nd)).astype(np.float32)
