@@ -369,16 +369,65 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(const TcParams p)
 
 // ---------------- operand splitting
 
-// slices of u (|u| < 1): S_i 2^(-7(i+1)) for i < NS, as exact BF16 numbers
-template <int NS>
-__device__ __forceinline__ void split7(double u, __nv_bfloat16 *out)
+// The split runs in integer arithmetic (this part's FP64 pipe is slow): an entry x = m 2^p
+// (m the signed integer significand) becomes the fixed-point integer U = round(x 2^(7 NS - e))
+// of its row, |U| <= 2^(7 NS), cut into signed 7-bit digits S_i (each rounded to nearest, so
+// |S_0| <= 128 and |S_i| <= 64 after it); slice i is S_i 2^(-7(i+1)), an exact BF16 number.
+struct Bits {
+    long long m;  // signed significand
+    int p;        // power of two: x = m 2^p
+    int fe;       // frexp exponent (|x| < 2^fe), or a large negative number for x = 0
+};
+__device__ __forceinline__ Bits bits_of(double x)
 {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7ff);
+    long long m = (long long)(b & ((1ull << 52) - 1));
+    Bits r;
+    if (be == 0) {
+        r.p = -1074;
+        r.fe = m ? -1022 : -(1 << 28);
+    } else {
+        m |= 1ll << 52;
+        r.p = be - 1075;
+        r.fe = be - 1022;
+    }
+    r.m = (b >> 63) ? -m : m;
+    return r;
+}
+__device__ __forceinline__ Bits bits_of(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const int be = (int)((b >> 23) & 0xff);
+    long long m = (long long)(b & ((1u << 23) - 1));
+    Bits r;
+    if (be == 0) {
+        r.p = -149;
+        r.fe = m ? -126 : -(1 << 28);
+    } else {
+        m |= 1ll << 23;
+        r.p = be - 150;
+        r.fe = be - 126;
+    }
+    r.m = (b >> 31) ? -m : m;
+    return r;
+}
+
+// slices of x 2^(-e) (|x 2^-e| < 1) as exact BF16 numbers S_i 2^(-7(i+1)), i < NS
+template <int NS>
+__device__ __forceinline__ void split7(Bits x, int e, __nv_bfloat16 *out)
+{
+    const int sh = x.p - e + 7 * NS;  // U = round(m 2^sh)
+    long long V;
+    if (sh >= 0) V = x.m << min(sh, 62);
+    else if (sh > -62) V = (x.m + (1ll << (-sh - 1))) >> (-sh);
+    else V = 0;
 #pragma unroll
     for (int i = 0; i < NS; i++) {
-        const double t = u * 128.0;
-        const double s = rint(t);
-        u = t - s;
-        out[i] = __double2bfloat16(ldexp(s, -7 * (i + 1)));
+        const int d = 7 * (NS - 1 - i);
+        const long long S = d ? (V + (1ll << (d - 1))) >> d : V;
+        V -= S << d;
+        out[i] = __float2bfloat16_rn(__ll2float_rn(S) * __int_as_float((127 - 7 * (i + 1)) << 23));
     }
 }
 
@@ -389,49 +438,42 @@ __device__ __forceinline__ int tile_off(int r, int k)
     return ((r >> 3) * 4 + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
 }
 
-// power-of-two scale e of a row or column from its largest magnitude: max < 2^e
-__device__ __forceinline__ int scale_exp(double mx)
-{
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);
-    return e;
-}
+// power-of-two scale e of a row or column from the largest frexp exponent of its entries
+// (max |x| < 2^e); 0 for a zero row
+__device__ __forceinline__ int scale_of(int fe_max) { return fe_max < -(1 << 27) ? 0 : fe_max; }
 
-// largest magnitude of each column of X (rows x cols, column-major), the entries of row r
-// first scaled by 2^(ksign * ek[r]) when ek is given: one block per column
+// scale of each column of X (rows x cols, column-major), the entries of row r first scaled by
+// 2^(ksign * ek[r]) when ek is given: one block per column
 template <typename T>
 __global__ void k_colmax_exp(const T *__restrict__ X, long ld, long rows, const int *ek,
                              int ksign, int *e)
 {
     const T *x = X + (long)blockIdx.x * ld;
-    double mx = 0.0;
-    for (long r = threadIdx.x; r < rows; r += blockDim.x) {
-        const double v = ek ? ldexp((double)x[r], ksign * ek[r]) : (double)x[r];
-        mx = fmax(mx, fabs(v));
-    }
-    __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int mx = -(1 << 28);
+    for (long r = threadIdx.x; r < rows; r += blockDim.x)
+        mx = max(mx, bits_of(x[r]).fe + (ek ? ksign * ek[r] : 0));
+    __shared__ int red[32];
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x < 32) {
-        mx = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (threadIdx.x == 0) e[blockIdx.x] = scale_exp(mx);
+        mx = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : -(1 << 28);
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (threadIdx.x == 0) e[blockIdx.x] = scale_of(mx);
     }
 }
 
-// largest magnitude of each row of X (rows x cols, column-major), column c first scaled by
-// 2^(-ec[c]): one thread per row
+// scale of each row of X (rows x cols, column-major), column c first scaled by 2^(-ec[c]):
+// one thread per row
 template <typename T>
 __global__ void k_rowmax_exp(const T *__restrict__ X, long ld, long rows, int cols,
                              const int *__restrict__ ec, int *e)
 {
     for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < rows;
          r += (long)gridDim.x * blockDim.x) {
-        double mx = 0.0;
-        for (int c = 0; c < cols; c++)
-            mx = fmax(mx, fabs(ldexp((double)X[(long)c * ld + r], -ec[c])));
-        e[r] = scale_exp(mx);
+        int mx = -(1 << 28);
+        for (int c = 0; c < cols; c++) mx = max(mx, bits_of(X[(long)c * ld + r]).fe - ec[c]);
+        e[r] = scale_of(mx);
     }
 }
 
@@ -457,8 +499,8 @@ __global__ void __launch_bounds__(256) k_split_cols(const T *__restrict__ X, lon
         for (int t = 0; t < 8; t++) {
             const long k = k0 + t;
             const bool in = n < ncols && k < krows;
-            const double v = in ? (double)X[(long)n * ld + k] : 0.0;
-            split7<NS>(ldexp(v, (ek && in ? ksign * ek[k] : 0) - en), sl[t]);
+            const Bits v = bits_of(in ? X[(long)n * ld + k] : T(0));
+            split7<NS>(v, en - (ek && in ? ksign * ek[k] : 0), sl[t]);
         }
 #pragma unroll
         for (int i = 0; i < NS; i++) {
@@ -491,8 +533,8 @@ __global__ void __launch_bounds__(256) k_split_rows(const T *__restrict__ X, lon
         for (int t = 0; t < 8; t++) {
             const int k = s * TK + g * 8 + t;
             const bool in = m < rows && k < kcols;
-            const double v = in ? (double)X[(long)k * ld + m] : 0.0;
-            split7<NS>(ldexp(v, (in ? -ec[k] : 0) - em), sl[t]);
+            const Bits v = bits_of(in ? X[(long)k * ld + m] : T(0));
+            split7<NS>(v, em + (in ? ec[k] : 0), sl[t]);
         }
 #pragma unroll
         for (int i = 0; i < NS; i++) {
