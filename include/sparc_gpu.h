@@ -523,7 +523,7 @@ int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode);
 
 /* Where the Rayleigh-Ritz products Mp = Yᵀ Y, Hp = Yᵀ HY (DP_Project_Hamiltonian,
  * src/eigenSolver.c:1022-1033) and X = Y Q (DP_Subspace_Rotation, :1415) run.
- * mode 1: on the library's own tcgen05 kernels, every operand row scaled by a power of two
+ * mode 1 (default): on the library's own tcgen05 kernels, every operand row scaled by a power of two
  * and cut into 7-bit BF16 slices whose products accumulate exactly in tensor memory (chunks
  * of 512) and are then summed in compensated arithmetic: FP32-accurate (3 slices, 6 slice
  * products) for FP32 blocks (sgpu_Project_Hamiltonian_f32, sgpu_Subspace_Rotation_f32, the

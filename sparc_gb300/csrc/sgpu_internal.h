@@ -164,10 +164,10 @@ struct sgpu_ctx {
     int gemm_mode = 0;  // FP32-block products: 0 cuBLAS FP32 GEMM (BF16x9 emulation where
                         // cuBLAS expects a gain), 1 the same with eager emulation, 2 the
                         // library's three-part BF16 split on the tensor cores (cuBLAS GEMMs)
-    int rr_tc = 0;      // Rayleigh-Ritz products on the library's own tcgen05 split-slice
-                        // kernels (rr_tc.cu): 1 for FP32 blocks (FP32-accurate) and the mixed
-                        // SCF's FP64 phase (FP64-accurate), 2 also for plain FP64 calls;
-                        // 0 cuBLAS
+    int rr_tc = 1;      // Rayleigh-Ritz products on the library's own tcgen05 split-slice
+                        // kernels (rr_tc.cu): 1 (default) for FP32 blocks (FP32-accurate) and
+                        // the mixed SCF's FP64 phase (FP64-accurate), 2 also for plain FP64
+                        // calls; 0 cuBLAS
     double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
     double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
