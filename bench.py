@@ -65,6 +65,14 @@ def parse():
     ap.add_argument("--no-c3", action="store_true", help="skip the batched k-point/spin block")
     ap.add_argument("--rr-gemm", action="store_true",
                     help="only time the Rayleigh-Ritz products at the Si216 shapes")
+    ap.add_argument("--rr-grid", type=int, default=77,
+                    help="grid edge of the --rr-gemm case (77: Si216; smaller for profiling)")
+    ap.add_argument("--rr-ns", type=int, default=520, help="states of the --rr-gemm case")
+    ap.add_argument("--rr-only", default=None,
+                    help="comma-separated --rr-gemm modes to run (fp32_tc, fp64_tc, fp32, "
+                         "fp32_eager, fp32_bf16_split, fp64)")
+    ap.add_argument("--fp64-only", action="store_true",
+                    help="only the FP64 filter steps, no tuning or side blocks (profiling)")
     ap.add_argument("--c3-only", action="store_true",
                     help="print only the batched k-point/spin block (profiling)")
     ap.add_argument("--stencil-variant", type=int, default=None,
@@ -466,7 +474,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def rr_gemm_block(sg, torch, dev, device=0, steps=3):
+def rr_gemm_block(sg, torch, dev, device=0, steps=3, grid=77, ns=520, only=None):
     """The Rayleigh-Ritz products at the Si216 shapes (77^3 grid at h = 0.40, 520 states):
     the library's tcgen05 split-slice products (FP32-accurate on FP32 blocks, FP64-accurate on
     FP64 blocks), cuBLAS's FP32 forms (BF16x9 emulation requested, eager, three-part BF16
@@ -474,19 +482,21 @@ def rr_gemm_block(sg, torch, dev, device=0, steps=3):
     achieved TFLOP/s of the rotation (one GEMM, 2 Nd Ns^2 flops) and of the two products of
     the projection (2 Nd Ns^2 each; its H Y apply timed and subtracted)."""
     from sparc_gb300.synthetic import fd_d2_coeffs, gaussian_potential
-    N, h, ns = (77, 77, 77), 0.40, 520
+    N, h = (grid, grid, grid), 0.40
     c = fd_d2_coeffs(6, h)
     rng = np.random.default_rng(7)
     ctx = sg.Context(*N, 6, c, c, c, h ** 3, device=device)
     ctx.set_veff(gaussian_potential(rng, N, h))
     nd = N[0] * N[1] * N[2]
     stream = torch.cuda.ExternalStream(ctx.stream())
-    out = {"shape": f"Nd = {nd} (77^3), Ns = {ns}"}
+    out = {"shape": f"Nd = {nd} ({grid}^3), Ns = {ns}"}
     for name, dt in (("fp32_tc", torch.float32), ("fp64_tc", torch.float64),
                      ("fp32", torch.float32), ("fp32_eager", torch.float32),
                      ("fp32_bf16_split", torch.float32), ("fp64", torch.float64)):
         # *_tc: the library's tcgen05 split-slice products (FP32-accurate on FP32 blocks,
         # FP64-accurate on FP64 blocks); the others: cuBLAS
+        if only and name not in only:
+            continue
         ctx.set_rr_products({"fp32_tc": 1, "fp64_tc": 2}.get(name, 0))
         ctx.set_gemm_emulation({"fp32_eager": 1, "fp32_bf16_split": 2}.get(name, 0))
         Y = torch.rand((ns, nd), device=dev, dtype=dt) - 0.5
@@ -571,8 +581,11 @@ def main():
                                                          steps=args.steps)}), flush=True)
         return
     if args.rr_gemm:
+        only = args.rr_only.split(",") if args.rr_only else None
         print(json.dumps({"rayleigh_ritz": rr_gemm_block(sg, torch, dev, device=local,
-                                                         steps=args.steps)}), flush=True)
+                                                         steps=args.steps, grid=args.rr_grid,
+                                                         ns=args.rr_ns, only=only)}),
+              flush=True)
         return
 
     wl = microbench_workload(N=N3, ncol=args.ncol, with_vectors=False)
@@ -586,6 +599,17 @@ def main():
     ctx.set_nonlocal(nl["ip_displ"], nl["gamma"], nl["img_atom"], nl["img_ndc"],
                      nl["grid_pos"], nl["chi"])
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    if args.fp64_only:  # the FP64 filter steps alone, for a launch list under a profiler
+        Xp0 = torch.rand((ncol, Nd), device=dev, dtype=torch.float64) * 2 - 1
+        Xp, Yp = Xp0.clone(), torch.empty_like(Xp0)
+        for _ in range(args.warmup + args.steps):
+            with torch.cuda.stream(stream):
+                Xp.copy_(Xp0)
+            ctx.ChebyshevFiltering(Xp, Yp, M, wl["a"], wl["b"], wl["a0"],
+                                   precision=sg.SGPU_PREC_FP64)
+        torch.cuda.synchronize()
+        print(json.dumps({"fp64_only": True, "steps": args.steps}), flush=True)
+        return
     # pick the FP32 kernel forms for this grid and block width (stencil variants give
     # identical results)
     variant, variant_ms = ctx.autotune(ncol=ncol)
