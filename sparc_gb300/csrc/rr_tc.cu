@@ -26,8 +26,8 @@
 // rotation, Y's columns are first balanced by powers of two (and Q's rows by the inverse), so
 // that a grid point's fixed-point row does not lose small columns to large ones.
 //
-// GEMM kernel (one CTA per SM, 320 threads): warp 0 issues the bulk copies into a two-stage
-// ring, one thread of warp 1 issues tcgen05.mma (M = 128, N = 128, K = 16, BF16 inputs, FP32
+// GEMM kernel (persistent, one CTA per SM looping over output tiles, 320 threads): warp 0
+// issues the bulk copies into a ring of stages (four for 3 slices, two for 6), one thread of warp 1 issues tcgen05.mma (M = 128, N = 128, K = 16, BF16 inputs, FP32
 // accumulators in four TMEM regions of 128 columns), warps 2-9 read the accumulators after
 // each chunk (tcgen05.ld) and keep the compensated sums. Every barrier wait is bounded; a wait
 // that runs out sets bit 4 of the status word and the kernel winds down (no copy left in
@@ -48,7 +48,6 @@ constexpr int TK = 32;                          // K per pipeline step
 constexpr int TILE_ELEMS = TM * TK;             // one 128 x 32 BF16 slice tile
 constexpr unsigned TILE_BYTES = TILE_ELEMS * 2; // 8 KB
 constexpr int CHUNK_STEPS = 16;                 // K steps per exact chunk (512 K values)
-constexpr int NSTAGE = 2;
 constexpr int EPI_WARPS = 8;
 constexpr int NTHREADS = 64 + 32 * EPI_WARPS;
 constexpr int STATUS_TC_WAIT = 4;
@@ -56,10 +55,11 @@ constexpr int STATUS_TC_WAIT = 4;
 template <int NS>
 struct TcShape {
     static constexpr unsigned stage_bytes = 2u * NS * TILE_BYTES;  // A slices then B slices
-    static constexpr unsigned bar_off = NSTAGE * stage_bytes;
-    // full[2], empty[2], acc_full, acc_empty, done, TMEM address, abort flag; at least 120 KB
-    // so that one CTA holds an SM (each CTA allocates all 512 TMEM columns)
-    static constexpr unsigned need = bar_off + 8 * 8 + 1024;
+    static constexpr int nstage = NS <= 3 ? 4 : 2;                 // ring depth
+    static constexpr unsigned bar_off = nstage * stage_bytes;
+    // full[nstage], empty[nstage], acc_full, acc_empty, done, TMEM address, abort flag; at
+    // least 120 KB so that one CTA holds an SM (each CTA allocates all 512 TMEM columns)
+    static constexpr unsigned need = bar_off + 16 * nstage + 32 + 1024;
     static constexpr unsigned smem_bytes = need > 120u * 1024 ? need : 120u * 1024;
 };
 
@@ -149,6 +149,33 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// exact float -> double through the bits (normal numbers; zero and the rest by conversion),
+// so the epilogue spends no FP64-pipe instruction on it
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned be = (b >> 23) & 0xffu;
+    if (be == 0u || be == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
+                                            ((unsigned long long)(be + 896u) << 52) |
+                                            ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// x 2^s by the exponent bits while the result stays a normal number (ldexp otherwise)
+__device__ __forceinline__ double scale2(double x, int s)
+{
+    const long long b = __double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7ff);
+    if (be == 0 || be + s <= 0 || be + s >= 0x7ff) return ldexp(x, s);
+    return __longlong_as_double(b + ((long long)s << 52));
+}
+__device__ __forceinline__ float scale2f(float x, int s)
+{
+    const int b = __float_as_int(x);
+    const int be = (b >> 23) & 0xff;
+    if (be == 0 || be + s <= 0 || be + s >= 0xff) return ldexpf(x, s);
+    return __int_as_float(b + (s << 23));
+}
+
 // Gram work item -> (row tile, column tile) with row tile <= column tile
 __device__ __forceinline__ void upper_pair(int t, int nrb, int &mt, int &nt)
 {
@@ -167,37 +194,40 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(const TcParams p)
     using S = TcShape<NS>;
     extern __shared__ __align__(1024) unsigned char smem[];
     const unsigned sbase = smem_u32(smem);
-    const unsigned bar_full = sbase + S::bar_off;  // [2]
-    const unsigned bar_empty = bar_full + 16;      // [2]
-    const unsigned bar_accf = bar_full + 32;
-    const unsigned bar_acce = bar_full + 40;
-    const unsigned bar_done = bar_full + 48;
-    unsigned *tmem_slot = reinterpret_cast<unsigned *>(smem + S::bar_off + 56);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::bar_off + 60);
+    constexpr int NST = S::nstage;
+    const unsigned bar_full = sbase + S::bar_off;     // [NST]
+    const unsigned bar_empty = bar_full + 8 * NST;    // [NST]
+    const unsigned bar_accf = bar_empty + 8 * NST;
+    const unsigned bar_acce = bar_accf + 8;
+    const unsigned bar_done = bar_accf + 16;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(smem + S::bar_off + 16 * NST + 24);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + S::bar_off + 16 * NST + 28);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    // ---- work item
-    int mt, nt, ks0, ks1, split = 0;
-    if (p.mode == 0) {
-        const int npairs = p.nrbA * (p.nrbA + 1) / 2;
-        const int t = blockIdx.x % npairs;
-        split = blockIdx.x / npairs;
-        upper_pair(t, p.nrbA, mt, nt);
-        const int per = (p.ksteps + p.ksplit - 1) / p.ksplit;
-        ks0 = split * per;
-        ks1 = min(p.ksteps, ks0 + per);
-    } else {
-        mt = blockIdx.x / p.nrbB;
-        nt = blockIdx.x - mt * p.nrbB;
-        ks0 = 0;
-        ks1 = p.ksteps;
-    }
-    const int nsteps = max(0, ks1 - ks0);
-    const int nchunks = (nsteps + CHUNK_STEPS - 1) / CHUNK_STEPS;
+    // ---- work items: tiles t = blockIdx.x, + gridDim.x, ...; the copy ring and the
+    // accumulator barriers run on across tiles, so each CTA pays its set-up once
+    const int ntiles = p.mode == 0 ? p.nrbA * (p.nrbA + 1) / 2 * p.ksplit : p.nrbA * p.nrbB;
+    auto tile_of = [&](int t, int &mt, int &nt, int &ks0, int &ks1, int &split) {
+        if (p.mode == 0) {
+            const int npairs = p.nrbA * (p.nrbA + 1) / 2;
+            split = t / npairs;
+            upper_pair(t - split * npairs, p.nrbA, mt, nt);
+            const int per = (p.ksteps + p.ksplit - 1) / p.ksplit;
+            ks0 = split * per;
+            ks1 = min(p.ksteps, ks0 + per);
+        } else {
+            mt = t / p.nrbB;
+            nt = t - mt * p.nrbB;
+            ks0 = 0;
+            ks1 = p.ksteps;
+            split = 0;
+        }
+        if (ks1 < ks0) ks1 = ks0;
+    };
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NSTAGE; s++) {
+        for (int s = 0; s < NST; s++) {
             mbar_init(bar_full + 8 * s, 1);
             mbar_init(bar_empty + 8 * s, 1);
         }
@@ -226,70 +256,79 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(const TcParams p)
     if (warp == 0) {
         // ---------------- producer: one bulk copy of the NS slices of A and of B per step
         if (lane == 0) {
-            int issued = 0;
-            for (int it = 0; it < nsteps; it++) {
-                const int st = it & 1;
-                if (it >= NSTAGE && !mbar_wait_bounded(bar_empty + 8 * st, ((it >> 1) - 1) & 1)) {
-                    fail();
-                    break;
+            int it = 0;  // steps issued by this CTA (ring position)
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                int mt, nt, ks0, ks1, split;
+                tile_of(t, mt, nt, ks0, ks1, split);
+                for (int s = ks0; s < ks1; s++, it++) {
+                    const int st = it % NST;
+                    if (it >= NST && !mbar_wait_bounded(bar_empty + 8 * st, (it / NST - 1) & 1)) {
+                        fail();
+                        break;
+                    }
+                    if (*abort_flag) break;
+                    const __nv_bfloat16 *a = p.A + ((long)s * p.nrbA + mt) * (long)NS * TILE_ELEMS;
+                    const __nv_bfloat16 *b = p.B + ((long)s * p.nrbB + nt) * (long)NS * TILE_ELEMS;
+                    const unsigned dst = sbase + st * S::stage_bytes;
+                    mbar_arrive_tx(bar_full + 8 * st, 2u * NS * TILE_BYTES);
+                    bulk_g2s(dst, a, NS * TILE_BYTES, bar_full + 8 * st);
+                    bulk_g2s(dst + NS * TILE_BYTES, b, NS * TILE_BYTES, bar_full + 8 * st);
                 }
-                if (*abort_flag) break;
-                const int s = ks0 + it;
-                const __nv_bfloat16 *a = p.A + ((long)s * p.nrbA + mt) * (long)NS * TILE_ELEMS;
-                const __nv_bfloat16 *b = p.B + ((long)s * p.nrbB + nt) * (long)NS * TILE_ELEMS;
-                const unsigned dst = sbase + st * S::stage_bytes;
-                mbar_arrive_tx(bar_full + 8 * st, 2u * NS * TILE_BYTES);
-                bulk_g2s(dst, a, NS * TILE_BYTES, bar_full + 8 * st);
-                bulk_g2s(dst + NS * TILE_BYTES, b, NS * TILE_BYTES, bar_full + 8 * st);
-                issued = it + 1;
             }
             // no copy may land after the block exits: wait for the last fill of each stage
-            for (int st = 0; st < NSTAGE; st++) {
-                const int last = issued - 1 - ((issued - 1 - st) % NSTAGE + NSTAGE) % NSTAGE;
-                if (last >= 0 && !mbar_wait_bounded(bar_full + 8 * st, (last >> 1) & 1)) fail();
+            const int issued = it;
+            for (int st = 0; st < NST; st++) {
+                const int last = issued - 1 - ((issued - 1 - st) % NST + NST) % NST;
+                if (last >= 0 && !mbar_wait_bounded(bar_full + 8 * st, (last / NST) & 1)) fail();
             }
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer
         if (lane == 0) {
-            int it = 0;
-            for (int c = 0; c < nchunks && !*abort_flag; c++) {
-                if (c > 0 && !mbar_wait_bounded(bar_acce, (c - 1) & 1)) {
-                    fail();
-                    break;
-                }
-                tc_fence_after();
-                const int cend = min(nsteps, (c + 1) * CHUNK_STEPS);
-                for (; it < cend; it++) {
-                    const int st = it & 1;
-                    if (!mbar_wait_bounded(bar_full + 8 * st, (it >> 1) & 1)) {
+            int it = 0, cg = 0;  // steps consumed, chunks completed (over all tiles)
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                int mt, nt, ks0, ks1, split;
+                tile_of(t, mt, nt, ks0, ks1, split);
+                const int nsteps = ks1 - ks0;
+                const int nchunks = (nsteps + CHUNK_STEPS - 1) / CHUNK_STEPS;
+                for (int c = 0; c < nchunks && !*abort_flag; c++, cg++) {
+                    if (cg > 0 && !mbar_wait_bounded(bar_acce, (cg - 1) & 1)) {
                         fail();
                         break;
                     }
-                    if (*abort_flag) break;
                     tc_fence_after();
-                    const unsigned a0 = sbase + st * S::stage_bytes;
-                    const unsigned b0 = a0 + NS * TILE_BYTES;
-                    const bool chunk_first = it == c * CHUNK_STEPS;
+                    const int cend = min(nsteps, (c + 1) * CHUNK_STEPS);
+                    for (int k = c * CHUNK_STEPS; k < cend; k++, it++) {
+                        const int st = it % NST;
+                        if (!mbar_wait_bounded(bar_full + 8 * st, (it / NST) & 1)) {
+                            fail();
+                            break;
+                        }
+                        if (*abort_flag) break;
+                        tc_fence_after();
+                        const unsigned a0 = sbase + st * S::stage_bytes;
+                        const unsigned b0 = a0 + NS * TILE_BYTES;
+                        const bool chunk_first = k == c * CHUNK_STEPS;
 #pragma unroll
-                    for (int i = 0; i < NS; i++) {
+                        for (int i = 0; i < NS; i++) {
 #pragma unroll
-                        for (int j = 0; i + j < NS; j++) {
-                            const int acc = min(i + j, 3);
-                            const bool acc_first = i == 0 && j <= 3;
+                            for (int j = 0; i + j < NS; j++) {
+                                const int acc = min(i + j, 3);
+                                const bool acc_first = i == 0 && j <= 3;
 #pragma unroll
-                            for (int kk = 0; kk < 2; kk++) {
-                                const unsigned accum =
-                                    (chunk_first && acc_first && kk == 0) ? 0u : 1u;
-                                mma_bf16(tmem + acc * TN,
-                                         smem_desc(a0 + i * TILE_BYTES + kk * 256),
-                                         smem_desc(b0 + j * TILE_BYTES + kk * 256), accum);
+                                for (int kk = 0; kk < 2; kk++) {
+                                    const unsigned accum =
+                                        (chunk_first && acc_first && kk == 0) ? 0u : 1u;
+                                    mma_bf16(tmem + acc * TN,
+                                             smem_desc(a0 + i * TILE_BYTES + kk * 256),
+                                             smem_desc(b0 + j * TILE_BYTES + kk * 256), accum);
+                                }
                             }
                         }
+                        mma_commit(bar_empty + 8 * st);  // the stage is free once these complete
                     }
-                    mma_commit(bar_empty + 8 * st);  // the stage is free once these complete
+                    mma_commit(bar_accf);  // the chunk's sums are complete
                 }
-                mma_commit(bar_accf);  // the chunk's sums are complete
             }
             mma_commit(bar_done);
             if (!mbar_wait_bounded(bar_done, 0)) fail();  // nothing in flight at dealloc
@@ -299,61 +338,73 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_tc_gemm(const TcParams p)
         const int q = warp & 3;         // TMEM lane quarter this warp may access
         const int h = (warp - 2) >> 2;  // column half: 64 columns per warp
         const unsigned tl = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(64 * h);
-        float hi[64], lo[64];
+        int cg = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            int mt, nt, ks0, ks1, split;
+            tile_of(t, mt, nt, ks0, ks1, split);
+            const int nchunks = (ks1 - ks0 + CHUNK_STEPS - 1) / CHUNK_STEPS;
+            float hi[64], lo[64];
 #pragma unroll
-        for (int c = 0; c < 64; c++) hi[c] = lo[c] = 0.f;
-        for (int c = 0; c < nchunks; c++) {
+            for (int c = 0; c < 64; c++) hi[c] = lo[c] = 0.f;
+            for (int c = 0; c < nchunks; c++, cg++) {
+                if (*abort_flag) break;
+                if (!mbar_wait_bounded(bar_accf, cg & 1)) {
+                    fail();
+                    break;
+                }
+                tc_fence_after();
+                // levels 0, 1, 2, then the rest, into the running sums (cascaded TwoSum)
+#pragma unroll
+                for (int a = 0; a < (NS > 3 ? 4 : 3); a++) {
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        float l[16];
+                        tmem_ld16(tl + a * TN + 16 * g, l);
+#pragma unroll
+                        for (int e = 0; e < 16; e++) {
+                            float sum, err;
+                            two_sum(hi[16 * g + e], l[e], sum, err);
+                            hi[16 * g + e] = sum;
+                            lo[16 * g + e] += err;
+                        }
+                    }
+                }
+                // the accumulators are free for the next chunk (of this tile or the next)
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar_acce);
+            }
             if (*abort_flag) break;
-            if (!mbar_wait_bounded(bar_accf, c & 1)) {
-                fail();
-                break;
-            }
-            tc_fence_after();
-            // levels 0, 1, 2, then the rest, into the running sums (cascaded TwoSum)
+            // ---- results: (hi + lo) times the two row scales
+            const int m = mt * TM + 32 * q + lane;
+            if (m < p.M) {
+                const int em = p.eA[m];
+                const int n0 = nt * TN + 64 * h;
+                if (p.mode == 0) {
+                    double *part = p.C + (long)split * p.N * p.M;  // [N][M], column-major
 #pragma unroll
-            for (int a = 0; a < (NS > 3 ? 4 : 3); a++) {
-#pragma unroll
-                for (int g = 0; g < 4; g++) {
-                    float l[16];
-                    tmem_ld16(tl + a * TN + 16 * g, l);
-#pragma unroll
-                    for (int e = 0; e < 16; e++) {
-                        float sum, err;
-                        two_sum(hi[16 * g + e], l[e], sum, err);
-                        hi[16 * g + e] = sum;
-                        lo[16 * g + e] += err;
+                    for (int c = 0; c < 64; c++) {
+                        const int n = n0 + c;
+                        // the upper triangle, mirrored: the result is exactly symmetric
+                        if (n < p.N && (mt != nt || m <= n)) {
+                            const double v =
+                                scale2(f2d_exact(hi[c]) + f2d_exact(lo[c]), em + p.eB[n]);
+                            part[(long)n * p.M + m] = v;
+                            part[(long)m * p.M + n] = v;
+                        }
                     }
-                }
-            }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(bar_acce);
-        }
-        // ---- results: (hi + lo) times the two row scales
-        const int m = mt * TM + 32 * q + lane;
-        if (!*abort_flag && m < p.M) {
-            const int em = p.eA[m];
-            const int n0 = nt * TN + 64 * h;
-            if (p.mode == 0) {
-                double *part = p.C + (long)split * p.N * p.M;  // [N][M], column-major
+                } else {
 #pragma unroll
-                for (int c = 0; c < 64; c++) {
-                    const int n = n0 + c;
-                    // the upper triangle, mirrored: the result is exactly symmetric
-                    if (n < p.N && (mt != nt || m <= n)) {
-                        const double v = ldexp((double)hi[c] + (double)lo[c], em + p.eB[n]);
-                        part[(long)n * p.M + m] = v;
-                        part[(long)m * p.M + n] = v;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 64; c++) {
-                    const int n = n0 + c;
-                    if (n < p.N) {
-                        const double v = ldexp((double)hi[c] + (double)lo[c], em + p.eB[n]);
-                        if (p.C32) p.C32[(long)n * p.ldc + m] = (float)v;
-                        else p.C[(long)n * p.ldc + m] = v;
+                    for (int c = 0; c < 64; c++) {
+                        const int n = n0 + c;
+                        if (n < p.N) {
+                            if (p.C32)  // FP32 output: no FP64 arithmetic
+                                p.C32[(long)n * p.ldc + m] =
+                                    scale2f(__fadd_rn(hi[c], lo[c]), em + p.eB[n]);
+                            else
+                                p.C[(long)n * p.ldc + m] =
+                                    scale2(f2d_exact(hi[c]) + f2d_exact(lo[c]), em + p.eB[n]);
+                        }
                     }
                 }
             }
@@ -562,9 +613,12 @@ __global__ void k_reduce_parts(const double *__restrict__ part, int ksplit, int 
 }
 
 template <int NS>
-int launch_gemm(sgpu_ctx *ctx, const TcParams &p, int nblocks, cudaStream_t st)
+int launch_gemm(sgpu_ctx *ctx, const TcParams &p, int ntiles, cudaStream_t st)
 {
     constexpr unsigned smem = TcShape<NS>::smem_bytes;
+    int nsm = 0;
+    SGPU_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int nblocks = std::max(1, std::min(ntiles, nsm));  // persistent: one CTA per SM
     auto kern = k_tc_gemm<NS>;
     SGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
