@@ -428,7 +428,10 @@ int sgpu_Symmetrize_forces(int n_atom, double *forces);
 int sgpu_last_filter_ms(sgpu_ctx *ctx, float *ms);
 
 /* The context's CUDA stream (cudaStream_t), on which every call of this context runs, so that
- * a caller can order its own work or record timing events against it. */
+ * a caller can order its own work or record timing events against it. The stream does not
+ * synchronise with the legacy default stream: device arrays produced on another stream must
+ * be complete (or ordered before this stream) when a call starts. Calls synchronise this
+ * stream before they return. */
 int sgpu_get_stream(sgpu_ctx *ctx, void **stream);
 
 /* Read and clear the context's kernel status word (synchronises the stream). Kernels that

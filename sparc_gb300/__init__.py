@@ -132,11 +132,17 @@ def _check(rc):
 
 
 def _ptr(a):
-    """Raw pointer of a numpy array or a torch tensor (host or device)."""
+    """Raw pointer of a numpy array or a torch tensor (host or device). The library runs on
+    its own CUDA stream, so work torch queued on a device tensor's current stream is waited
+    for first: the call then reads the finished tensor (each call synchronises its own stream
+    before returning, so its results are ready for torch afterwards)."""
     if a is None:
         return None
     if isinstance(a, np.ndarray):
         return _vp(a.ctypes.data)
+    if getattr(a, "is_cuda", False):
+        import torch
+        torch.cuda.current_stream(a.device).synchronize()
     return _vp(a.data_ptr())
 
 
