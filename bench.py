@@ -549,14 +549,24 @@ def rr_gemm_block(sg, torch, dev, device=0, steps=3, grid=77, ns=520, only=None)
         Mp.copy_(M0)
         ctx.Solve_Generalized_EigenProblem(Hp, Mp, lam)
 
-    for _ in range(2):
-        eig()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        eig()
-    torch.cuda.synchronize()
-    out["generalized_eig_fp64_ms"] = round((time.perf_counter() - t0) / steps * 1e3, 3)
+    lam_ref = None
+    for mode, tag in ((0, "dsygvd"), (1, "potrf_trsm_syevd"), (2, "potrf_trsm_syevj")):
+        ctx.set_eig_solver(mode)
+        for _ in range(2):
+            eig()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            eig()
+        torch.cuda.synchronize()
+        rec = {"ms": round((time.perf_counter() - t0) / steps * 1e3, 3)}
+        if lam_ref is None:
+            lam_ref = lam.clone()
+            out["generalized_eig_fp64_ms"] = rec["ms"]
+        else:
+            rec["max_eig_diff_vs_dsygvd"] = float((lam - lam_ref).abs().max().item())
+        out.setdefault("generalized_eig", {})[tag] = rec
+    ctx.set_eig_solver(0)
     ctx.close()
     return out
 

@@ -539,6 +539,13 @@ int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode);
  * reference (which calls cblas_dgemm). */
 int sgpu_set_rr_products(sgpu_ctx *ctx, int mode);
 
+/* How sgpu_Solve_Generalized_EigenProblem and the SCF solve Hp q = lambda Mp q
+ * (DP_Solve_Generalized_EigenProblem, src/eigenSolver.c:1262; LAPACKE_dsygvd at :1318):
+ * mode 0 (default): cuSOLVER dsygvd; 1: the same reduction as separate calls (dpotrf, two
+ * dtrsm, dsyevd, dtrsm); 2: the reduction with a Jacobi eigensolver (dsyevj). All FP64;
+ * results agree to the eigensolvers' accuracy. */
+int sgpu_set_eig_solver(sgpu_ctx *ctx, int mode);
+
 /* FP32 filter with the projections carried across degrees (mode 1, 2 or 4) or not (0). When
  * on, every degree's nonlocal apply is the range form with the projection of the iterate it
  * finishes fused in (alpha of the next degree is formed from the finished values while they

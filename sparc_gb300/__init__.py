@@ -42,7 +42,7 @@ EXPORTED = [
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
     "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
     "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation", "sgpu_measure_fp64_rate",
-    "sgpu_set_rr_products",
+    "sgpu_set_rr_products", "sgpu_set_eig_solver",
 ]
 
 
@@ -616,6 +616,11 @@ class Context:
         """Rayleigh-Ritz products: 1 tensor-core split slices for FP32 blocks and the mixed
         SCF's FP64 phase, 2 also for plain FP64 calls, 0 cuBLAS (sgpu_set_rr_products)."""
         _check(lib().sgpu_set_rr_products(self._h, int(mode)))
+
+    def set_eig_solver(self, mode):
+        """Subspace eigensolver: 0 dsygvd, 1 Cholesky reduction + dsyevd, 2 reduction +
+        Jacobi dsyevj (sgpu_set_eig_solver)."""
+        _check(lib().sgpu_set_eig_solver(self._h, int(mode)))
 
     def measure_fp64_rate(self):
         """This GPU's FP64 FMA rate in TFLOP/s (sgpu_measure_fp64_rate)."""

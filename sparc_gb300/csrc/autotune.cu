@@ -227,6 +227,16 @@ int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode)
     return SGPU_OK;
 }
 
+int sgpu_set_eig_solver(sgpu_ctx *ctx, int mode)
+{
+    if (!ctx || mode < 0 || mode > 2) {
+        set_error("sgpu_set_eig_solver: need a context and mode 0, 1 or 2");
+        return SGPU_ERR_ARG;
+    }
+    ctx->eig_mode = mode;
+    return SGPU_OK;
+}
+
 int sgpu_set_rr_products(sgpu_ctx *ctx, int mode)
 {
     if (!ctx || mode < 0 || mode > 2) {

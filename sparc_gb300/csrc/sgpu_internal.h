@@ -164,6 +164,8 @@ struct sgpu_ctx {
     int gemm_mode = 0;  // FP32-block products: 0 cuBLAS FP32 GEMM (BF16x9 emulation where
                         // cuBLAS expects a gain), 1 the same with eager emulation, 2 the
                         // library's three-part BF16 split on the tensor cores (cuBLAS GEMMs)
+    int eig_mode = 0;   // subspace eigensolver: 0 dsygvd, 1 Cholesky reduction + dsyevd,
+                        // 2 Cholesky reduction + Jacobi dsyevj (sgpu_set_eig_solver)
     int rr_tc = 1;      // Rayleigh-Ritz products on the library's own tcgen05 split-slice
                         // kernels (rr_tc.cu): 1 (default) for FP32 blocks (FP32-accurate) and
                         // the mixed SCF's FP64 phase (FP64-accurate), 2 also for plain FP64

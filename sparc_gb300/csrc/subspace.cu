@@ -183,13 +183,44 @@ int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *
     return SGPU_OK;
 }
 
+static int potrf_upper(sgpu_ctx *ctx, int n, double *M, cudaStream_t st);
+static int standard_eig_j(sgpu_ctx *ctx, int n, double *A, double *lambda_dev, bool jacobi,
+                          cudaStream_t st);
+
+// The same pencil reduced by hand: Mp = Uᵀ U (dpotrf), C = U^-T Hp U^-1 (two dtrsm), C = V Λ Vᵀ
+// (dsyevd, or Jacobi dsyevj), Q = U^-1 V (dtrsm); the steps LAPACK's dsygvd takes, as
+// separate library calls (eig_mode 1 and 2: timed against dsygvd by bench.py --rr-gemm)
+static int generalized_eig_reduced(sgpu_ctx *ctx, int n, double *Hp, double *Mp,
+                                   double *lambda_dev, bool jacobi, cudaStream_t st)
+{
+    SGPU_TRY(potrf_upper(ctx, n, Mp, st));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    const double one = 1.0;
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER,
+                                    CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, n, &one, Mp, n, Hp, n));
+        SGPU_CUBLAS_TRY(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER,
+                                    CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one, Mp, n, Hp, n));
+    }
+    SGPU_TRY(standard_eig_j(ctx, n, Hp, lambda_dev, jacobi, st));
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    SGPU_CUBLAS_TRY(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER,
+                                CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one, Mp, n, Hp, n));
+    return SGPU_OK;
+}
+
 // Hp q = lambda Mp q (upper triangles referenced); on return Hp holds Q, lambda ascending.
-// Mp is overwritten by its Cholesky factor.
+// Mp is overwritten by its Cholesky factor. ctx->eig_mode: 0 cuSOLVER dsygvd (the reference's
+// LAPACKE_dsygvd, src/eigenSolver.c:1318), 1 Cholesky reduction + dsyevd, 2 Cholesky
+// reduction + Jacobi dsyevj.
 int generalized_eig(sgpu_ctx *ctx, int n, double *Hp, double *Mp, double *lambda_dev,
                     cudaStream_t st)
 {
     SGPU_TRY(ensure_handles(ctx));
     cusolverDnSetStream(ctx->cusolver, st);
+    if (ctx->eig_mode == 1 || ctx->eig_mode == 2)
+        return generalized_eig_reduced(ctx, n, Hp, Mp, lambda_dev, ctx->eig_mode == 2, st);
     int lwork = 0;
     if (cusolverDnDsygvd_bufferSize(ctx->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
                                     CUBLAS_FILL_MODE_UPPER, n, Hp, n, Mp, n, lambda_dev,
@@ -272,6 +303,59 @@ int cholqr_f64(sgpu_ctx *ctx, int ncol, double *Y, long ldy, cudaStream_t st)
                                 CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, (int)ctx->Nd, ncol, &one, M,
                                 ncol, Y, (int)ldy));
     return SGPU_OK;
+}
+
+// A = V Λ Vᵀ with Jacobi sweeps (cuSOLVER dsyevj, tolerance 1e-15, up to 100 sweeps); A
+// becomes V, lambda ascending
+static int syevj(sgpu_ctx *ctx, int n, double *A, double *lambda_dev, cudaStream_t st)
+{
+    syevjInfo_t params = nullptr;
+    if (cusolverDnCreateSyevjInfo(&params) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnCreateSyevjInfo failed");
+        return SGPU_ERR_CUDA;
+    }
+    cusolverDnXsyevjSetTolerance(params, 1e-15);
+    cusolverDnXsyevjSetMaxSweeps(params, 100);
+    int lwork = 0, rc = SGPU_OK;
+    if (cusolverDnDsyevj_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR,
+                                    CUBLAS_FILL_MODE_UPPER, n, A, n, lambda_dev, &lwork,
+                                    params) != CUSOLVER_STATUS_SUCCESS) {
+        cusolverDnDestroySyevjInfo(params);
+        set_error("cusolverDnDsyevj_bufferSize failed");
+        return SGPU_ERR_CUDA;
+    }
+    char *wsp = nullptr;
+    rc = ws_get(ctx, WS_MISC, sizeof(double) * ((size_t)lwork + 1) + 64, (void **)&wsp);
+    if (rc == SGPU_OK) {
+        double *work = reinterpret_cast<double *>(wsp);
+        int *info = reinterpret_cast<int *>(wsp + sizeof(double) * ((size_t)lwork + 1));
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        if (cusolverDnDsyevj(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+                             A, n, lambda_dev, work, lwork, info,
+                             params) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnDsyevj failed to launch");
+            rc = SGPU_ERR_CUDA;
+        } else {
+            int hinfo = 0;
+            if (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) {
+                set_error("dsyevj: reading info failed");
+                rc = SGPU_ERR_CUDA;
+            } else if (hinfo != 0) {
+                set_error("dsyevj: info = " + std::to_string(hinfo));
+                rc = SGPU_ERR_LINALG;
+            }
+        }
+    }
+    cusolverDnDestroySyevjInfo(params);
+    return rc;
+}
+
+static int standard_eig_j(sgpu_ctx *ctx, int n, double *A, double *lambda_dev, bool jacobi,
+                          cudaStream_t st)
+{
+    return jacobi ? syevj(ctx, n, A, lambda_dev, st) : standard_eig(ctx, n, A, lambda_dev, st);
 }
 
 // Hp q = lambda q (upper triangle; dsyevd, the STANDARD_EIGEN branch of

@@ -112,3 +112,27 @@ def test_fp32_accurate_products_on_fp32_blocks(gpu_available):
     assert rel(Xd.cpu().numpy().astype(np.float64), Q @ y64) < 1e-5
     assert ctx.kernel_status() == 0
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_generalized_eigensolver_modes(gpu_available, mode):
+    """sgpu_Solve_Generalized_EigenProblem in each solver mode (dsygvd; Cholesky reduction with
+    dsyevd; with Jacobi dsyevj) against scipy's eigh on an SPD pencil like the subspace's:
+    eigenvalues 1e-10 of the largest, Mp-orthonormal eigenvectors with residual 1e-9."""
+    import scipy.linalg as sl
+    rng = np.random.default_rng(9 + mode)
+    ctx, Nd = _ctx(rng)
+    ctx.set_eig_solver(mode)
+    n = 90
+    A = rng.normal(size=(n, n))
+    H = A + A.T
+    B = rng.normal(size=(n, n)) / n
+    M = B @ B.T + np.eye(n)
+    Hp, Mp, lam = H.copy(), M.copy(), np.zeros(n)
+    ctx.Solve_Generalized_EigenProblem(Hp, Mp, lam)
+    lo = sl.eigh(H, M, eigvals_only=True)
+    assert np.abs(lam - lo).max() < 1e-10 * np.abs(lo).max()
+    Q = Hp.T  # C array rows are the column-major eigenvectors
+    assert np.abs(H @ Q - M @ Q * lam[None, :]).max() < 1e-9 * np.abs(lo).max()
+    assert np.abs(Q.T @ M @ Q - np.eye(n)).max() < 1e-9
+    ctx.close()
