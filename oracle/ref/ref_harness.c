@@ -11,6 +11,9 @@
  *   Hamiltonian_vectors_mult     src/hamiltonianVecRoutines.c:45
  *   ChebyshevFiltering           src/eigenSolver.c:722
  *   poisson_residual             src/lapVecRoutines.c:69
+ *   AAR                          src/linearSolver.c:37 (with Jacobi_preconditioner)
+ *   Kerker_precond               src/mixing.c:462
+ *   Mixing_periodic_pulay        src/mixing.c:213 (after Update_mixing_hist_xk)
  * One system per process: the reference keeps its state in the SPARC_OBJ built here.
  */
 #include <stdio.h>
@@ -26,6 +29,9 @@
 #include "hamiltonianVecRoutines.h"
 #include "eigenSolver.h"
 #include "orbitalElecDensInit.h"
+#include "linearSolver.h"
+#include "mixing.h"
+#include "electronicGroundState.h"
 
 static SPARC_OBJ S;
 static int g_ready = 0;
@@ -253,6 +259,39 @@ void ref_poisson(const double *rho, double *phi)
     memcpy(S.elecstPotential, phi, sizeof(double) * S.Nd);
     Calculate_elecstPotential(&S);
     memcpy(phi, S.elecstPotential, sizeof(double) * S.Nd);
+}
+
+/* AAR (src/linearSolver.c:37) with the reference's residual and Jacobi preconditioner and
+ * its Poisson settings (omega = beta = 0.6, m = 7, p = 6, src/electrostatics.c:1653-1659):
+ * solves b + (Lap + c) x = 0 in place from the initial x */
+void ref_aar(double c, double *x, double *b, double tol, int max_iter)
+{
+    AAR(&S, poisson_residual, Jacobi_preconditioner, c, S.Nd_d, x, b, 0.6, 0.6, 7, 6, tol,
+        max_iter, S.dmcomm_phi);
+}
+
+/* Kerker_precond (src/mixing.c:462) with the input's kTF, idiemac and TOL_PRECOND */
+void ref_kerker(double *f, double a, double *Pf)
+{
+    Kerker_precond(&S, f, a, S.precond_kerker_kTF, S.precond_kerker_thresh, S.TOL_PRECOND,
+                   S.Nd_d, S.DMVertices, Pf, S.dmcomm_phi);
+}
+
+/* periodic Pulay density mixing: ref_mix_init starts the history from rho0
+ * (Update_mixing_hist_xk, src/electronicGroundState.c:1255), each ref_mix_step hands the
+ * output density g of SCF iteration iter to Mixing_periodic_pulay and returns the mixed
+ * density in g */
+void ref_mix_init(const double *rho0)
+{
+    memcpy(S.electronDens, rho0, sizeof(double) * S.Nd_d);
+    Update_mixing_hist_xk(&S);
+}
+
+void ref_mix_step(int iter, double *g)
+{
+    memcpy(S.electronDens, g, sizeof(double) * S.Nd_d);
+    Mixing_periodic_pulay(&S, iter);
+    memcpy(g, S.electronDens, sizeof(double) * S.Nd_d);
 }
 
 SPARC_OBJ *ref_harness_obj(void) { return &S; }

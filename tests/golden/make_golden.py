@@ -176,6 +176,43 @@ def capture_scf_result(sysd, psp_dir, out_json, sparc_bin):
         json.dump(ref, fh, indent=1)
 
 
+def mixing_inputs(rho0, nsteps=9, seed=31):
+    """A seeded sequence of SCF output densities around rho0 for the mixing fixtures: each is
+    the previous mixed density perturbed by 2 % (multiplicative, seeded), independent of the
+    mixer, so the reference and the restatement see the same inputs."""
+    rng = np.random.default_rng(seed)
+    g = rho0.copy()
+    out = []
+    for _ in range(nsteps):
+        g = g * (1.0 + 0.02 * rng.standard_normal(g.size))
+        out.append(g.copy())
+    return np.array(out)
+
+
+def capture_mixing(sysd, psp_dir, out_npz):
+    """Golden vectors of the SCF-side solvers from the reference itself on the system's own
+    set-up: periodic Pulay mixing over nine iterations (past the history of seven), a Kerker
+    preconditioning, and AAR solves of b + (Lap + c) x = 0 (c = 0 and c = -1)."""
+    from ref_capture import RefSystem
+
+    tmp = tempfile.mkdtemp(prefix="sparc_mix_")
+    base = systems.write_system(sysd, tmp, psp_dir)
+    r = RefSystem(base)
+    f = r.setup_fields()
+    rho0 = f["rho0"]
+    outputs = mixing_inputs(rho0)
+    mixed = r.mix(rho0, outputs)
+    rng = np.random.default_rng(5)
+    kf = rho0 * 0.05 * rng.standard_normal(rho0.size)
+    Pf = r.kerker(kf, 0.3)
+    b = rng.standard_normal(r.Nd)
+    aar_c0 = r.aar(0.0, np.zeros(r.Nd), b - b.mean(), 1e-10)
+    aar_c1 = r.aar(-1.0, np.zeros(r.Nd), b, 1e-10)
+    np.savez_compressed(out_npz, rho0=rho0, outputs=outputs, mixed=mixed, kerker_f=kf,
+                        kerker_a=0.3, kerker_Pf=Pf, aar_b=b, aar_x_c0=aar_c0, aar_x_c1=aar_c1,
+                        aar_tol=1e-10)
+
+
 def capture_setup(sysd, psp_dir, out_npz):
     """Inputs and outputs of the reference's per-geometry set-up: parsed pseudopotential
     tables, atom positions as read, pseudocharge cut-offs, pseudocharge densities, initial and
@@ -212,7 +249,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=reference_root(),
                     help="reference tree (default: $SPARC_REFERENCE, else /root/reference)")
-    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "setup", "si216"], default=None,
+    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "setup", "si216", "mixing"],
+                    default=None,
                     help="regenerate one group of fixtures only")
     args = ap.parse_args()
     psp_dir = os.path.join(args.ref, "psps")
@@ -224,6 +262,16 @@ def main():
         capture_scf_result(systems.si216_c4(), psp_dir, js, sparc_bin)
         print("wrote", js)
         return
+    if args.only in (None, "mixing"):
+        path = os.path.join(HERE, "Si8_c1_mixing.npz")
+        p = ctx.Process(target=capture_mixing, args=(systems.si8_c1(), psp_dir, path))
+        p.start()
+        p.join()
+        if p.exitcode != 0:
+            raise SystemExit("mixing capture failed")
+        print("wrote", path, os.path.getsize(path), "bytes")
+        if args.only == "mixing":
+            return
     if args.only in (None, "setup"):
         for sysd in (systems.si2_small(), systems.si8_c1(), systems.al4_small()):
             path = os.path.join(HERE, f"{sysd['name']}_setup.npz")

@@ -156,6 +156,33 @@ class RefSystem:
         self.lib.ref_poisson_residual(ctypes.c_double(c), _d(x), _d(b), _d(r))
         return r
 
+    def aar(self, c, x0, b, tol, max_iter=3000):
+        """The reference's AAR (Poisson settings) on b + (Lap + c) x = 0 from x0."""
+        x = np.array(x0, dtype=np.float64)
+        b = np.array(b, dtype=np.float64)
+        self.lib.ref_aar(ctypes.c_double(c), _d(x), _d(b), ctypes.c_double(tol),
+                         ctypes.c_int(max_iter))
+        return x
+
+    def kerker(self, f, a):
+        """The reference's Kerker_precond of f with mixing parameter a."""
+        f = np.array(f, dtype=np.float64)
+        Pf = np.zeros_like(f)
+        self.lib.ref_kerker(_d(f), ctypes.c_double(a), _d(Pf))
+        return Pf
+
+    def mix(self, rho0, outputs):
+        """The reference's periodic Pulay mixing over a sequence of output densities: the
+        mixed density after each SCF iteration."""
+        r0 = np.ascontiguousarray(rho0, dtype=np.float64)
+        self.lib.ref_mix_init(_d(r0))
+        mixed = []
+        for it, g in enumerate(outputs):
+            g = np.array(g, dtype=np.float64)
+            self.lib.ref_mix_step(ctypes.c_int(it), _d(g))
+            mixed.append(g)
+        return np.array(mixed)
+
 
 class RefKpt:
     """k-point (complex) kernels of a RefSystem built from a system with a k-point grid.

@@ -98,6 +98,34 @@ def test_pulay_mixing_vs_oracle(gpu_available):
         g = 0.7 * g + 0.3 * xo
 
 
+def test_mixing_and_aar_match_reference_routines(gpu_available):
+    """The device mixing (Mixing_init + Mixing_periodic_pulay, Kerker inside) and AAR against
+    the reference's own Mixing_periodic_pulay (src/mixing.c:213) and AAR (src/linearSolver.c:37)
+    called through oracle/ref/ref_harness.c on the Si8 set-up (tests/golden/Si8_c1_mixing.npz):
+    nine mixing steps within 1e-8 of the reference's densities (its Kerker solves stop at
+    TOL_PRECOND, so an iteration more or less inside one of them moves the result), AAR at its
+    1e-10 stopping tolerance."""
+    import os
+    d, grid, nl, ref = load_scf()
+    m = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "Si8_c1_mixing.npz"))
+    ctx = make_ctx(grid, None)
+    ctx.Mixing_init(m["rho0"], -float(d["Nelectron"]), tol_precond=ref["params"]["TOL_PRECOND"])
+    for it, g in enumerate(m["outputs"]):
+        x = g.copy()
+        ctx.Mixing_periodic_pulay(it, x)
+        assert np.abs(x - m["mixed"][it]).max() <= 1e-8 * np.abs(m["mixed"][it]).max(), it
+    b = m["aar_b"]
+    for c, key, rhs in ((0.0, "aar_x_c0", b - b.mean()), (-1.0, "aar_x_c1", b)):
+        x = np.zeros(ctx.Nd)
+        it, ok = ctx.AAR(c, x, rhs, tol=float(m["aar_tol"]), max_iter=3000)
+        assert ok
+        xr = m[key]
+        if c == 0.0:  # defined up to a constant on the periodic grid
+            x, xr = x - x.mean(), xr - xr.mean()
+        assert np.abs(x - xr).max() <= 1e-8 * np.abs(xr).max(), c
+
+
 def test_rayleigh_ritz_vs_lapack(gpu_available):
     import scipy.linalg as sl
     d, grid, nl, ref = load_scf()
@@ -214,6 +242,7 @@ def test_scf_matches_reference_program(gpu_available, precision, carried):
     occupied = occ_ref > 1e-3
     assert np.abs(lam[occupied] - lam_ref[occupied]).max() < 1e-5
     assert abs(rho.sum() * grid["dV"] - float(d["Nelectron"])) < 1e-8
-    assert abs(res["scf_iters"] - ref["scf_iters"]) <= 6
+    # plain FP64 follows the reference's iteration path; the FP32 phase may shift it slightly
+    assert abs(res["scf_iters"] - ref["scf_iters"]) <= (1 if precision == 64 else 2)
     if precision == 32:
         assert res["fp64_switch_iter"] > 0
