@@ -288,6 +288,28 @@ typedef struct {
 int sgpu_ChebyshevFiltering_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks,
                                     int m, int precision);
 
+/* Rayleigh-Ritz step at a k-point, complex128 (interleaved) blocks Nd x ncol and Ns x Ns
+ * column-major matrices, host or device. Project: HY = H_k Y (written to HY), Hp = Yᴴ HY,
+ * Mp = Yᴴ Y; replaces DP_Project_Hamiltonian_kpt (src/eigenSolverKpt.c:676; its ZGEMMs at
+ * :747-760). Solve: Hp q = lambda Mp q (upper triangles; cuSOLVER zhegvd), Hp becomes Q;
+ * replaces DP_Solve_Generalized_EigenProblem_kpt (:836). Rotation: X = Y Q; replaces
+ * DP_Subspace_Rotation_kpt (:947). */
+int sgpu_Project_Hamiltonian_kpt(sgpu_ctx *ctx, int spin, const double *k, const double *Y,
+                                 int ldi, double *HY, int ldo, int ncol, double *Hp, double *Mp);
+int sgpu_Solve_Generalized_EigenProblem_kpt(sgpu_ctx *ctx, int Ns, double *Hp, double *Mp,
+                                            double *lambda);
+int sgpu_Subspace_Rotation_kpt(sgpu_ctx *ctx, const double *Y, int ldi, const double *Q,
+                               int ncol, double *X, int ldo);
+
+/* One CheFSI pass over all (k, spin) blocks (eigSolve_CheFSI_kpt's per-block filter,
+ * projection, eigensolve and rotation, src/eigenSolverKpt.c:165-300): the batched filter of
+ * sgpu_ChebyshevFiltering_batched, then per block H Y, Hp = Yᴴ HY, Mp = Yᴴ Y (ZGEMM, or
+ * CGEMM for complex64 blocks), the FP64 generalized eigensolve and X = Y Q. On return each
+ * block's X holds its Ritz vectors and Y its filtered block; lambda (host, sum of ncol)
+ * receives the blocks' Ritz values, block after block, ascending within a block. */
+int sgpu_CheFSI_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks, int m,
+                        int precision, double *lambda);
+
 /* ----------------------------------------------------------------- set-up (per geometry) */
 
 /* Radial tables of one atom type, as read_pseudopotential_PSP (src/readfiles.c:1957) leaves

@@ -42,7 +42,8 @@ EXPORTED = [
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
     "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
     "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation", "sgpu_measure_fp64_rate",
-    "sgpu_set_rr_products", "sgpu_set_eig_solver",
+    "sgpu_set_rr_products", "sgpu_set_eig_solver", "sgpu_Project_Hamiltonian_kpt",
+    "sgpu_Solve_Generalized_EigenProblem_kpt", "sgpu_Subspace_Rotation_kpt", "sgpu_CheFSI_batched",
 ]
 
 
@@ -424,15 +425,53 @@ class Context:
         """Filter several (k-point, spin) blocks in one call. blocks: list of dicts with spin,
         k (3), X, Y (device torch tensors of shape (ncol, Nd), complex128 for FP64 or
         complex64 for FP32) and the bounds a, b, a0."""
+        arr = self._blocks(blocks)
+        _check(lib().sgpu_ChebyshevFiltering_batched(self._h, len(blocks), arr, int(m),
+                                                     int(precision)))
+
+    def _blocks(self, blocks):
         arr = (FilterBlock * len(blocks))()
         for i, b in enumerate(blocks):
             X, Y = b["X"], b["Y"]
             ncol = int(X.shape[0]) if X.dim() == 2 else 1
             arr[i] = FilterBlock(int(b.get("spin", 0)), (ctypes.c_double * 3)(*b["k"]),
-                                 X.data_ptr(), self.Nd, Y.data_ptr(), self.Nd, ncol,
+                                 _ptr(X).value, self.Nd, _ptr(Y).value, self.Nd, ncol,
                                  float(b["a"]), float(b["b"]), float(b["a0"]))
-        _check(lib().sgpu_ChebyshevFiltering_batched(self._h, len(blocks), arr, int(m),
-                                                     int(precision)))
+        return arr
+
+    def CheFSI_batched(self, blocks, m, precision=SGPU_PREC_FP64):
+        """One CheFSI pass over (k-point, spin) blocks (as ChebyshevFiltering_batched): the
+        filter, then per block H Y, the projection, the generalized eigensolve and the
+        rotation into X. Returns the Ritz values of every block (list of arrays)."""
+        arr = self._blocks(blocks)
+        ncols = [int(b["X"].shape[0]) if b["X"].dim() == 2 else 1 for b in blocks]
+        lam = np.zeros(max(1, sum(ncols)))
+        _check(lib().sgpu_CheFSI_batched(self._h, len(blocks), arr, int(m), int(precision),
+                                         _ptr(lam)))
+        out, off = [], 0
+        for n in ncols:
+            out.append(lam[off:off + n].copy())
+            off += n
+        return out
+
+    def Project_Hamiltonian_kpt(self, k, Y, HY, Hp, Mp, spin=0):
+        """Complex128 blocks (ncol, Nd) and Ns x Ns matrices (column-major C arrays)."""
+        ncol, ld = self._ncol_ld(Y)
+        kv = self._kvec(k)
+        _check(lib().sgpu_Project_Hamiltonian_kpt(self._h, int(spin), _ptr(kv), _ptr(Y), ld,
+                                                  _ptr(HY), ld, ncol, _ptr(Hp), _ptr(Mp)))
+        return Hp, Mp
+
+    def Solve_Generalized_EigenProblem_kpt(self, Hp, Mp, lam):
+        _check(lib().sgpu_Solve_Generalized_EigenProblem_kpt(self._h, int(Hp.shape[0]),
+                                                             _ptr(Hp), _ptr(Mp), _ptr(lam)))
+        return Hp, lam
+
+    def Subspace_Rotation_kpt(self, Y, Q, X):
+        ncol, ld = self._ncol_ld(Y)
+        _check(lib().sgpu_Subspace_Rotation_kpt(self._h, _ptr(Y), ld, _ptr(Q), ncol, _ptr(X),
+                                                ld))
+        return X
 
     # ---- Rayleigh-Ritz
     def Project_Hamiltonian(self, Y, HY, Hp, Mp, spin=0):

@@ -1029,6 +1029,150 @@ template int chebyshev_z<float2>(sgpu_ctx *, int, const double *, float2 *, long
 
 int kpoint_set_phases(sgpu_ctx *ctx, const double *k, cudaStream_t st) { return set_phases(ctx, k, st); }
 
+// ---- Rayleigh-Ritz step at a k-point: DP_Project_Hamiltonian_kpt (src/eigenSolverKpt.c:676,
+// Hp = Yᴴ HY and Mp = Yᴴ Y by ACCEL_ZGEMM / cblas_zgemm, :747-760),
+// DP_Solve_Generalized_EigenProblem_kpt (:836, LAPACKE_zhegvd) and DP_Subspace_Rotation_kpt
+// (:947, X = Y Q). The Ns x Ns products of these small blocks (C3: 64 states) go to cuBLAS
+// (ZGEMM, or CGEMM for complex64 blocks), the eigenproblem to cuSOLVER zhegvd in complex128.
+
+// Hp = Yᴴ HY, Mp = Yᴴ Y (ncol x ncol complex128, column-major, ld ncol)
+template <typename CT>
+int project_z(sgpu_ctx *ctx, int ncol, const CT *Y, long ldy, const CT *HY, long ldh,
+              double2 *Hp, double2 *Mp, cudaStream_t st)
+{
+    SGPU_TRY(ensure_solver_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    const int Nd = (int)ctx->Nd;
+    if constexpr (sizeof(CT) == 16) {
+        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasZgemm(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, ncol, ncol, Nd, &one,
+                                    Y, (int)ldy, Y, (int)ldy, &zero, Mp, ncol));
+        SGPU_CUBLAS_TRY(cublasZgemm(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, ncol, ncol, Nd, &one,
+                                    Y, (int)ldy, HY, (int)ldh, &zero, Hp, ncol));
+    } else {
+        float2 *tmp = nullptr;
+        const size_t n2 = (size_t)ncol * ncol;
+        SGPU_TRY(ws_get(ctx, WS_TC_PART, sizeof(float2) * 2 * n2, (void **)&tmp));
+        const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+        {
+            ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+            SGPU_CUBLAS_TRY(cublasCgemm(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, ncol, ncol, Nd,
+                                        &one, Y, (int)ldy, Y, (int)ldy, &zero, tmp, ncol));
+            SGPU_CUBLAS_TRY(cublasCgemm(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, ncol, ncol, Nd,
+                                        &one, Y, (int)ldy, HY, (int)ldh, &zero, tmp + n2, ncol));
+        }
+        SGPU_TRY(convert_cols<float, double>(reinterpret_cast<float *>(tmp), 2 * (long)n2,
+                                             reinterpret_cast<double *>(Mp), 2 * (long)n2,
+                                             2 * (long)n2, 1, st));
+        SGPU_TRY(convert_cols<float, double>(reinterpret_cast<float *>(tmp + n2), 2 * (long)n2,
+                                             reinterpret_cast<double *>(Hp), 2 * (long)n2,
+                                             2 * (long)n2, 1, st));
+    }
+    return SGPU_OK;
+}
+
+// Hp q = lambda Mp q (upper triangles): Hp becomes Q, lambda (device) ascending
+int generalized_eig_z(sgpu_ctx *ctx, int n, double2 *Hp, double2 *Mp, double *lambda_dev,
+                      cudaStream_t st)
+{
+    SGPU_TRY(ensure_solver_handles(ctx));
+    cusolverDnSetStream(ctx->cusolver, st);
+    int lwork = 0;
+    if (cusolverDnZhegvd_bufferSize(ctx->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                    CUBLAS_FILL_MODE_UPPER, n, Hp, n, Mp, n, lambda_dev,
+                                    &lwork) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnZhegvd_bufferSize failed");
+        return SGPU_ERR_CUDA;
+    }
+    char *wsp = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_MISC, sizeof(double2) * ((size_t)lwork + 1) + 64, (void **)&wsp));
+    double2 *work = reinterpret_cast<double2 *>(wsp);
+    int *info = reinterpret_cast<int *>(wsp + sizeof(double2) * ((size_t)lwork + 1));
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        if (cusolverDnZhegvd(ctx->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                             CUBLAS_FILL_MODE_UPPER, n, Hp, n, Mp, n, lambda_dev, work, lwork,
+                             info) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnZhegvd failed to launch");
+            return SGPU_ERR_CUDA;
+        }
+    }
+    int hinfo = 0;
+    SGPU_CUDA_TRY(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hinfo != 0) {
+        set_error("zhegvd: info = " + std::to_string(hinfo) +
+                  (hinfo > n ? " (Mp is not positive definite)" : " (no convergence)"));
+        return SGPU_ERR_LINALG;
+    }
+    return SGPU_OK;
+}
+
+// X = Y Q (Q ncol x ncol complex128, ld ncol)
+template <typename CT>
+int rotate_z(sgpu_ctx *ctx, int ncol, const CT *Y, long ldy, const double2 *Q, CT *X, long ldx,
+             cudaStream_t st)
+{
+    SGPU_TRY(ensure_solver_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    const int Nd = (int)ctx->Nd;
+    if constexpr (sizeof(CT) == 16) {
+        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasZgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, Nd, ncol, ncol, &one,
+                                    Y, (int)ldy, Q, ncol, &zero, X, (int)ldx));
+    } else {
+        float2 *q32 = nullptr;
+        const long n2 = (long)ncol * ncol;
+        SGPU_TRY(ws_get(ctx, WS_TC_PART, sizeof(float2) * n2, (void **)&q32));
+        SGPU_TRY(convert_cols<double, float>(reinterpret_cast<const double *>(Q), 2 * n2,
+                                             reinterpret_cast<float *>(q32), 2 * n2, 2 * n2, 1,
+                                             st));
+        const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        SGPU_CUBLAS_TRY(cublasCgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, Nd, ncol, ncol, &one,
+                                    Y, (int)ldy, q32, ncol, &zero, X, (int)ldx));
+    }
+    return SGPU_OK;
+}
+
+// One CheFSI pass over all (k, spin) blocks: the batched filter, then per block H Y into X,
+// the projection, the eigenproblem and the rotation into X; lambda (host) receives each
+// block's Ritz values, blocks one after another.
+template <typename CT>
+int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
+                   double *lambda, cudaStream_t st)
+{
+    SGPU_TRY(chebyshev_batched<CT>(ctx, nblk, blk, m, st));
+    int nmax = 0;
+    for (int b = 0; b < nblk; b++) nmax = std::max(nmax, blk[b].ncol);
+    char *buf = nullptr;
+    const size_t n2 = (size_t)nmax * nmax;
+    SGPU_TRY(ws_get(ctx, WS_EIG, sizeof(double2) * 2 * n2 + sizeof(double) * nmax + 64,
+                    (void **)&buf));
+    double2 *Hp = reinterpret_cast<double2 *>(buf), *Mp = Hp + n2;
+    double *dlam = reinterpret_cast<double *>(Mp + n2);
+    long off = 0;
+    for (int b = 0; b < nblk; b++) {
+        const sgpu_filter_block &f = blk[b];
+        if (f.ncol == 0) continue;
+        CT *X = reinterpret_cast<CT *>(f.X);
+        CT *Y = reinterpret_cast<CT *>(f.Y);
+        SGPU_TRY(set_phases(ctx, f.k, st));
+        SGPU_TRY(hamiltonian_z<CT>(ctx, f.spin, f.k, f.ncol, 0.0, Y, f.ldo, X, f.ldi, 1.0, 0.0,
+                                   nullptr, 0, st));
+        SGPU_TRY(project_z<CT>(ctx, f.ncol, Y, f.ldo, X, f.ldi, Hp, Mp, st));
+        SGPU_TRY(generalized_eig_z(ctx, f.ncol, Hp, Mp, dlam, st));
+        SGPU_TRY(rotate_z<CT>(ctx, f.ncol, Y, f.ldo, Hp, X, f.ldi, st));
+        SGPU_CUDA_TRY(cudaMemcpyAsync(lambda + off, dlam, sizeof(double) * f.ncol,
+                                      cudaMemcpyDeviceToHost, st));
+        off += f.ncol;
+    }
+    SGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    return SGPU_OK;
+}
+
 }  // namespace sgpu
 
 using namespace sgpu;
@@ -1209,8 +1353,9 @@ int sgpu_ChebyshevFiltering_kpt(sgpu_ctx *ctx, int spin, const double *k, double
     return SGPU_OK;
 }
 
-int sgpu_ChebyshevFiltering_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks,
-                                    int m, int precision)
+// argument checks shared by the batched filter and the batched CheFSI pass
+static int batched_check(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks, int m,
+                         int precision)
 {
     if (!ctx || nblk < 0 || (nblk > 0 && !blocks) || m < 1) {
         set_error("ChebyshevFiltering_batched: need a context, nblk >= 0 blocks and m >= 1");
@@ -1240,6 +1385,124 @@ int sgpu_ChebyshevFiltering_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_b
             return SGPU_ERR_ARG;
         }
     }
+    return SGPU_OK;
+}
+
+// complex Ns x Ns matrix to the device (interleaved doubles, ld n)
+static int zmat_in(sgpu_ctx *ctx, int slot, const double *h, int n, bool copy, double2 **d)
+{
+    if (is_device_ptr(h)) {
+        *d = reinterpret_cast<double2 *>(const_cast<double *>(h));
+        return SGPU_OK;
+    }
+    SGPU_TRY(ws_get(ctx, slot, sizeof(double2) * (size_t)n * n, (void **)d));
+    if (copy)
+        SGPU_CUDA_TRY(cudaMemcpyAsync(*d, h, sizeof(double2) * (size_t)n * n,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    return SGPU_OK;
+}
+
+static int zmat_out(sgpu_ctx *ctx, const double2 *d, double *h, int n)
+{
+    if ((const void *)d == (const void *)h) return SGPU_OK;
+    SGPU_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_Project_Hamiltonian_kpt(sgpu_ctx *ctx, int spin, const double *k, const double *Y,
+                                 int ldi, double *HY, int ldo, int ncol, double *Hp, double *Mp)
+{
+    SGPU_TRY(kcheck(ctx, ncol, ldi, ldo));
+    if (!k || !Hp || !Mp) {
+        set_error("Project_Hamiltonian_kpt: null argument");
+        return SGPU_ERR_ARG;
+    }
+    if (ncol == 0) return SGPU_OK;
+    double2 *dY, *dH, *dHp, *dMp;
+    long lY, lH;
+    SGPU_TRY(zstage_in(ctx, WS_STAGE_A, Y, ldi, ncol, true, &dY, &lY));
+    SGPU_TRY(zstage_in(ctx, WS_STAGE_B, HY, ldo, ncol, false, &dH, &lH));
+    SGPU_TRY(zmat_in(ctx, WS_POIS, Hp, ncol, false, &dHp));
+    SGPU_TRY(zmat_in(ctx, WS_MIX, Mp, ncol, false, &dMp));
+    SGPU_TRY(kpoint_set_phases(ctx, k, ctx->stream));
+    SGPU_TRY(hamiltonian_z<double2>(ctx, spin, k, ncol, 0.0, dY, lY, dH, lH, 1.0, 0.0, nullptr,
+                                    0, ctx->stream));
+    SGPU_TRY(project_z<double2>(ctx, ncol, dY, lY, dH, lH, dHp, dMp, ctx->stream));
+    SGPU_TRY(zstage_out(ctx, dH, lH, HY, ldo, ncol));
+    SGPU_TRY(zmat_out(ctx, dHp, Hp, ncol));
+    SGPU_TRY(zmat_out(ctx, dMp, Mp, ncol));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_Solve_Generalized_EigenProblem_kpt(sgpu_ctx *ctx, int Ns, double *Hp, double *Mp,
+                                            double *lambda)
+{
+    if (!ctx || Ns <= 0 || !Hp || !Mp || !lambda) {
+        set_error("Solve_Generalized_EigenProblem_kpt: bad arguments");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_CUDA_TRY(cudaSetDevice(ctx->device));
+    double2 *dHp, *dMp;
+    SGPU_TRY(zmat_in(ctx, WS_POIS, Hp, Ns, true, &dHp));
+    SGPU_TRY(zmat_in(ctx, WS_MIX, Mp, Ns, true, &dMp));
+    double *dl = lambda;
+    if (!is_device_ptr(lambda)) SGPU_TRY(ws_get(ctx, WS_RED, sizeof(double) * Ns, (void **)&dl));
+    SGPU_TRY(generalized_eig_z(ctx, Ns, dHp, dMp, dl, ctx->stream));
+    SGPU_TRY(zmat_out(ctx, dHp, Hp, Ns));
+    SGPU_TRY(zmat_out(ctx, dMp, Mp, Ns));
+    if (dl != lambda)
+        SGPU_CUDA_TRY(cudaMemcpyAsync(lambda, dl, sizeof(double) * Ns, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_Subspace_Rotation_kpt(sgpu_ctx *ctx, const double *Y, int ldi, const double *Q,
+                               int ncol, double *X, int ldo)
+{
+    SGPU_TRY(kcheck(ctx, ncol, ldi, ldo));
+    if (!Q) {
+        set_error("Subspace_Rotation_kpt: null Q");
+        return SGPU_ERR_ARG;
+    }
+    if (ncol == 0) return SGPU_OK;
+    double2 *dY, *dX, *dQ;
+    long lY, lX;
+    SGPU_TRY(zstage_in(ctx, WS_STAGE_A, Y, ldi, ncol, true, &dY, &lY));
+    SGPU_TRY(zstage_in(ctx, WS_STAGE_B, X, ldo, ncol, false, &dX, &lX));
+    SGPU_TRY(zmat_in(ctx, WS_POIS, Q, ncol, true, &dQ));
+    SGPU_TRY(rotate_z<double2>(ctx, ncol, dY, lY, dQ, dX, lX, ctx->stream));
+    SGPU_TRY(zstage_out(ctx, dX, lX, X, ldo, ncol));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_CheFSI_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks, int m,
+                        int precision, double *lambda)
+{
+    SGPU_TRY(batched_check(ctx, nblk, blocks, m, precision));
+    if (nblk == 0) return SGPU_OK;
+    if (!lambda) {
+        set_error("CheFSI_batched: null lambda");
+        return SGPU_ERR_ARG;
+    }
+    SGPU_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (precision == SGPU_PREC_FP64)
+        SGPU_TRY(chefsi_batched<double2>(ctx, nblk, blocks, m, lambda, ctx->stream));
+    else
+        SGPU_TRY(chefsi_batched<float2>(ctx, nblk, blocks, m, lambda, ctx->stream));
+    SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    SGPU_CUDA_TRY(cudaEventElapsedTime(&ctx->last_filter_ms, ctx->ev0, ctx->ev1));
+    return SGPU_OK;
+}
+
+int sgpu_ChebyshevFiltering_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blocks,
+                                    int m, int precision)
+{
+    SGPU_TRY(batched_check(ctx, nblk, blocks, m, precision));
     if (nblk == 0) return SGPU_OK;
     SGPU_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
     if (precision == SGPU_PREC_FP64)

@@ -281,6 +281,7 @@ int project_f32(sgpu_ctx *ctx, int ncol, const float *Y, long ldy, const float *
                 double *Hp, double *Mp, cudaStream_t st);
 int generalized_eig(sgpu_ctx *ctx, int n, double *Hp, double *Mp, double *lambda_dev,
                     cudaStream_t st);
+int ensure_solver_handles(sgpu_ctx *ctx);
 template <typename T>
 int tc_project(sgpu_ctx *ctx, int ncol, const T *Y, long ldy, const T *HY, long ldh, double *Hp,
                double *Mp, bool fp64_accurate, cudaStream_t st);

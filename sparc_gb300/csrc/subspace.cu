@@ -23,7 +23,11 @@
 
 namespace sgpu {
 
-static int ensure_handles(sgpu_ctx *ctx)
+int ensure_solver_handles(sgpu_ctx *ctx);
+static int ensure_handles(sgpu_ctx *ctx) { return ensure_solver_handles(ctx); }
+
+// cuBLAS / cuSOLVER handles of the context, on its stream (created on first use)
+int ensure_solver_handles(sgpu_ctx *ctx)
 {
     if (!ctx->cublas) {
         SGPU_CUBLAS_TRY(cublasCreate(&ctx->cublas));
