@@ -411,6 +411,23 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b,
              const double *rho_init, const double *rho_core, double *rho_out,
              double *lambda_out, double *occ_out, sgpu_scf_result *res);
 
+/* The same SCF on a k-point grid with complex Bloch orbitals (eigSolve_CheFSI_kpt,
+ * src/eigenSolverKpt.c:72-215; Lanczos_kpt bounds per k-point; the Fermi level, band energy,
+ * entropy and density weighted by kptWts / Nkpts, src/occupation.c:445,
+ * src/electronDensity.c:128, src/energy.c:221-255). kpts: nkpt Cartesian Bloch vectors
+ * (1/Bohr, 3 per point, as k1_loc/k2_loc/k3_loc); kpt_wts: their weights as kptWts_loc
+ * (normalised by their sum, which is Nkpts for a symmetry-reduced full grid). Needs the
+ * k-point geometry of the context (sgpu_set_kpoint_geometry or
+ * sgpu_CalculateNonlocalProjectors). Each filter pass runs all k-points through one batched
+ * filter and then each k-point's Rayleigh-Ritz step (sgpu_CheFSI_batched). precision
+ * SGPU_PREC_FP32 runs complex64 orbitals until the error falls below fp64_switch_error;
+ * graded_tail must be 0. lambda_out and occ_out (nkpt * Nstates) are k-point after k-point;
+ * psi_out, when set, receives nkpt blocks of Nd x Nstates complex128 (interleaved). */
+int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const double *kpts,
+                 const double *kpt_wts, const double *b, const double *rho_init,
+                 const double *rho_core, double *rho_out, double *lambda_out, double *occ_out,
+                 sgpu_scf_result *res);
+
 /* ------------------------------------------------------------------- forces */
 
 /* Local (pseudocharge) force components of the atoms at atom_pos (as for

@@ -27,7 +27,7 @@ EXPORTED = [
     "sgpu_Solve_Generalized_EigenProblem", "sgpu_Subspace_Rotation", "sgpu_Lanczos",
     "sgpu_CalculateDensity_psi", "sgpu_Calculate_Vxc_LDA_PW", "sgpu_AAR",
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
-    "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_Vnl_vec_mult_noalloc",
+    "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_scf_kpt", "sgpu_Vnl_vec_mult_noalloc",
     "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
     "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
     "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
@@ -582,6 +582,46 @@ class Context:
         try:
             _check(lib().sgpu_scf(self._h, ctypes.byref(params), _ptr(b), _ptr(r0), _ptr(rc_),
                                   _ptr(rho), _ptr(lam), _ptr(occ), ctypes.byref(res)))
+        finally:
+            params.history = None
+            params.psi_out = params.phi_out = params.vxc_out = None
+        out = res.as_dict()
+        h = hist.reshape(-1, 3)[:out["scf_iters"]]
+        out["history"] = {"Etot": h[:, 0].tolist(), "scf_error": h[:, 1].tolist(),
+                          "time_s": h[:, 2].tolist()}
+        return out, rho, lam, occ
+
+    def scf_kpt(self, params, kpts, kpt_wts, b, rho_init, rho_core=None, fields=None):
+        """Run sgpu_scf_kpt on the k-points kpts (nkpt x 3, Cartesian 1/Bohr) with weights
+        kpt_wts (as the reference's kptWts_loc); returns (result dict, final density,
+        eigenvalues nkpt x Nstates, occupations nkpt x Nstates). With fields a dict, it also
+        receives the final orbitals ("psi", nkpt x Nstates x Nd complex128), "phi" and "vxc"."""
+        Ns = params.Nstates
+        kp = np.ascontiguousarray(kpts, dtype=np.float64).reshape(-1, 3)
+        wt = np.ascontiguousarray(kpt_wts, dtype=np.float64).reshape(-1)
+        nk = kp.shape[0]
+        if wt.shape[0] != nk:
+            raise ValueError("one weight per k-point")
+        rho = np.zeros(self.Nd)
+        lam = np.zeros((nk, Ns))
+        occ = np.zeros((nk, Ns))
+        res = ScfResult()
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        r0 = np.ascontiguousarray(rho_init, dtype=np.float64)
+        rc_ = None if rho_core is None else np.ascontiguousarray(rho_core, dtype=np.float64)
+        hist = np.full(3 * max(1, params.maxit_scf), np.nan)
+        params.history = hist.ctypes.data
+        if fields is not None:
+            fields["psi"] = np.zeros((nk, Ns, self.Nd), dtype=np.complex128)
+            fields["phi"] = np.zeros(self.Nd)
+            fields["vxc"] = np.zeros(self.Nd)
+            params.psi_out = fields["psi"].ctypes.data
+            params.phi_out = fields["phi"].ctypes.data
+            params.vxc_out = fields["vxc"].ctypes.data
+        try:
+            _check(lib().sgpu_scf_kpt(self._h, ctypes.byref(params), int(nk), _ptr(kp), _ptr(wt),
+                                      _ptr(b), _ptr(r0), _ptr(rc_), _ptr(rho), _ptr(lam),
+                                      _ptr(occ), ctypes.byref(res)))
         finally:
             params.history = None
             params.psi_out = params.phi_out = params.vxc_out = None

@@ -1173,6 +1173,11 @@ int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
     return SGPU_OK;
 }
 
+template int chefsi_batched<double2>(sgpu_ctx *, int, const sgpu_filter_block *, int, double *,
+                                     cudaStream_t);
+template int chefsi_batched<float2>(sgpu_ctx *, int, const sgpu_filter_block *, int, double *,
+                                    cudaStream_t);
+
 }  // namespace sgpu
 
 using namespace sgpu;

@@ -11,9 +11,9 @@
 // scalars (energy terms, SCF error) and the m x m Anderson systems come back to the host.
 //
 // Mixed precision (SGPU_PREC_FP32): while the SCF error is above fp64_switch_error the orbital
-// block is FP32, the filter runs in FP32 and the projection / rotation products are FP32
-// GEMMs (cuBLAS, BF16x9 emulation requested); the eigenproblem, Poisson, XC, mixing and all
-// energy reductions stay FP64. Below the threshold (or once the FP32 error stalls) the block
+// block is FP32, the filter runs in FP32 and the projection / rotation products are
+// FP32-accurate split products on the tensor cores (rr_tc.cu); the eigenproblem, Poisson, XC,
+// mixing and all energy reductions stay FP64. Below the threshold (or once the FP32 error stalls) the block
 // is widened to FP64 and the remaining iterations are either the plain FP64 path or, with
 // graded_tail, an FP32 filter whose last degrees run in FP64 followed by an FP64
 // Rayleigh-Ritz step (chebyshev_graded).
@@ -21,12 +21,12 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <functional>
 #include <vector>
 
 #include "sgpu_internal.h"
 
 namespace sgpu {
-namespace {
 
 __global__ void k_init_orbitals(double *X, long n, unsigned long long seed)
 {
@@ -41,19 +41,28 @@ __global__ void k_init_orbitals(double *X, long n, unsigned long long seed)
     }
 }
 
+void init_orbitals(sgpu_ctx *ctx, double *X, long n, unsigned long long seed, int blocks,
+                   cudaStream_t st)
+{
+    k_init_orbitals<<<blocks, 256, 0, st>>>(X, n, seed);
+    ctx->launches++;
+}
+
 double smearing(double beta, double lam, double ef, int type)
 {
     return type ? 0.5 * (1.0 - std::erf(beta * (lam - ef))) : 1.0 / (1.0 + std::exp(beta * (lam - ef)));
 }
 
-// Brent root finding for sum_n occfac * f(lambda_n) = Nelectron (Numerical-Recipes style
-// bracketing with inverse quadratic interpolation, as local_Calculate_FermiLevel does)
-double fermi_level(const std::vector<double> &lam, double occfac, double nelec, double beta,
-                   int type, double x1, double x2, double tol, int max_iter, int *status)
+// Brent root finding for sum_n w_n f(lambda_n) = Nelectron (Numerical-Recipes style
+// bracketing with inverse quadratic interpolation, as local_Calculate_FermiLevel does; w_n is
+// occfac at the Gamma point and occfac * kptWts / Nkpts at k-points, src/occupation.c:445-466)
+double fermi_level(const std::vector<double> &lam, const std::vector<double> &w, double nelec,
+                   double beta, int type, double x1, double x2, double tol, int max_iter,
+                   int *status)
 {
     auto g = [&](double ef) {
         double s = 0.0;
-        for (double l : lam) s += occfac * smearing(beta, l, ef, type);
+        for (size_t i = 0; i < lam.size(); i++) s += w[i] * smearing(beta, lam[i], ef, type);
         return s - nelec;
     };
     double a = std::min(x1, x2), b = std::max(x1, x2), c = b, d = 0, e = 0;
@@ -115,6 +124,8 @@ double fermi_level(const std::vector<double> &lam, double occfac, double nelec, 
     return b;
 }
 
+namespace {
+
 // Extreme eigenvalues of the symmetric tridiagonal matrix (diag a[0..n-1], off b[0..n-2]) by
 // Sturm-sequence bisection
 void tridiag_extremes(int n, const double *a, const double *b, double *lo, double *hi)
@@ -150,12 +161,16 @@ void tridiag_extremes(int n, const double *a, const double *b, double *lo, doubl
 
 }  // namespace
 
-// Lanczos estimate of the extreme eigenvalues of H (spin block), restating Lanczos
-// (src/eigenSolver.c:1920-2129): stop when both extremes change by less than tol.
-int lanczos_dev(sgpu_ctx *ctx, int spin, const double *x0, double tol, int maxit,
-                double *eigmin, double *eigmax, cudaStream_t st)
+// Lanczos estimate of the extreme eigenvalues of a symmetric operator on vectors of len
+// doubles, restating Lanczos (src/eigenSolver.c:1920-2129): stop when both extremes change by
+// less than tol. A Hermitian H_k acting on complex vectors stored as interleaved (re, im)
+// doubles runs through the same recurrence (Lanczos_kpt, src/eigenSolverKpt.c:1361): its
+// coefficients are real and Re(x^H y) is the dot product of the interleaved arrays.
+int lanczos_run(sgpu_ctx *ctx, long len, const std::function<int(const double *, double *)> &apply,
+                const double *x0, double tol, int maxit, double *eigmin, double *eigmax,
+                cudaStream_t st)
 {
-    const long N = ctx->Nd;
+    const long N = len;
     double *v = nullptr;
     SGPU_TRY(ws_get(ctx, WS_SCF2, sizeof(double) * (size_t)N * 3, (void **)&v));
     double *Vjm1 = v, *Vj = v + N, *Vjp1 = v + 2 * N;
@@ -163,7 +178,7 @@ int lanczos_dev(sgpu_ctx *ctx, int spin, const double *x0, double tol, int maxit
     double nrm2 = 0.0;
     SGPU_TRY(dot_host(ctx, Vjm1, Vjm1, N, &nrm2, st));
     SGPU_TRY(axpby_dev(ctx, N, 1.0 / std::sqrt(nrm2), Vjm1, 0.0, nullptr, Vjm1, st));
-    SGPU_TRY(hamiltonian_dev<double>(ctx, spin, 1, 0.0, Vjm1, N, Vj, N, 1.0, 0.0, nullptr, 0, st));
+    SGPU_TRY(apply(Vjm1, Vj));
     std::vector<double> a(maxit + 2), b(maxit + 2);
     SGPU_TRY(dot_host(ctx, Vjm1, Vj, N, &a[0], st));
     SGPU_TRY(axpby_dev(ctx, N, 1.0, Vj, -a[0], Vjm1, Vj, st));
@@ -178,7 +193,7 @@ int lanczos_dev(sgpu_ctx *ctx, int spin, const double *x0, double tol, int maxit
     double errmin = tol + 1.0, errmax = tol + 1.0;
     int j = 0;
     while ((errmin > tol || errmax > tol) && j < maxit) {
-        SGPU_TRY(hamiltonian_dev<double>(ctx, spin, 1, 0.0, Vj, N, Vjp1, N, 1.0, 0.0, nullptr, 0, st));
+        SGPU_TRY(apply(Vj, Vjp1));
         SGPU_TRY(dot_host(ctx, Vj, Vjp1, N, &a[j + 1], st));
         // Vjp1 -= a[j+1] Vj + b[j] Vjm1 ; Vjm1 = Vj
         SGPU_TRY(axpby_dev(ctx, N, 1.0, Vjp1, -a[j + 1], Vj, Vjp1, st));
@@ -198,6 +213,17 @@ int lanczos_dev(sgpu_ctx *ctx, int spin, const double *x0, double tol, int maxit
     *eigmin = emin;
     *eigmax = emax;
     return SGPU_OK;
+}
+
+// Lanczos on the Gamma-point H of one spin block
+int lanczos_dev(sgpu_ctx *ctx, int spin, const double *x0, double tol, int maxit,
+                double *eigmin, double *eigmax, cudaStream_t st)
+{
+    const long N = ctx->Nd;
+    auto apply = [&](const double *in, double *out) {
+        return hamiltonian_dev<double>(ctx, spin, 1, 0.0, in, N, out, N, 1.0, 0.0, nullptr, 0, st);
+    };
+    return lanczos_run(ctx, N, apply, x0, tol, maxit, eigmin, eigmax, st);
 }
 
 }  // namespace sgpu
@@ -654,8 +680,7 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
     struct G4 { float *p; ~G4() { if (p) cudaFree(p); } } g32{X32};
     if (mixed && !ctx->stencil_tuned)  // tuned at the block width the filter runs at
         SGPU_TRY(sgpu_autotune(ctx, Ns, nullptr, nullptr));
-    k_init_orbitals<<<152 * 8, 256, 0, st>>>(X64, nb, prm->seed);
-    ctx->launches++;
+    init_orbitals(ctx, X64, nb, prm->seed, 152 * 8, st);
     if (mixed) SGPU_TRY(convert_cols<double, float>(X64, nb, X32, nb, nb, 1, st));
 
     const double occfac = 2.0;  // spin-unpolarised
@@ -699,8 +724,7 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                 // Lanczos on H from a random start vector, then the reference's safety margins
                 double *x0 = nullptr;
                 SGPU_TRY(ws_get(ctx, WS_SCF, sizeof(double) * N, (void **)&x0));
-                k_init_orbitals<<<152, 256, 0, st>>>(x0, N, prm->seed ^ 0x5bd1e995ull);
-                ctx->launches++;
+                init_orbitals(ctx, x0, N, prm->seed ^ 0x5bd1e995ull, 152, st);
                 SGPU_TRY(lanczos_dev(ctx, 0, x0, prm->tol_lanczos, 1000, &eigmin, &eigmax, st));
                 eigmax *= 1.01;
                 eigmin -= 0.1;
@@ -748,8 +772,9 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
                                           cudaMemcpyDeviceToHost, st));
             SGPU_CUDA_TRY(cudaStreamSynchronize(st));
             int fst = 0;
-            efermi = fermi_level(lam, occfac, prm->Nelectron, prm->Beta, prm->elec_T_type,
-                                 lam[0] - 1.0, lam[Ns - 1] + 1.0, 1e-12, 100, &fst);
+            efermi = fermi_level(lam, std::vector<double>(Ns, occfac), prm->Nelectron, prm->Beta,
+                                 prm->elec_T_type, lam[0] - 1.0, lam[Ns - 1] + 1.0, 1e-12, 100,
+                                 &fst);
             if (fst) {
                 set_error("sgpu_scf: cannot bracket the Fermi level");
                 return SGPU_ERR_LINALG;

@@ -77,6 +77,24 @@ __global__ void k_density(const T *__restrict__ psi, long ld, int ncol,
     }
 }
 
+// complex columns (re, im interleaved): rho[i] (+)= sum_n w_n |psi[i, n]|^2
+template <typename CT>
+__global__ void k_density_z(const CT *__restrict__ psi, long ld, int ncol,
+                            const double *__restrict__ w, double *__restrict__ rho, long Nd,
+                            int accumulate)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < Nd;
+         i += (long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int n = 0; n < ncol; n++) {
+            const CT v = psi[i + (long)n * ld];
+            const double re = (double)v.x, im = (double)v.y;
+            s += w[n] * (re * re + im * im);
+        }
+        rho[i] = accumulate ? rho[i] + s : s;
+    }
+}
+
 // LDA: Slater exchange + Perdew-Wang 92 correlation on rho + rho_core (clamped at rhotol).
 // vxc = vx + vc, exc = ex + ec (energy per particle). Constants are the published values of
 // the functional (J. P. Perdew and Y. Wang, PRB 45, 13244 (1992)).
@@ -323,6 +341,21 @@ template int density_dev<double>(sgpu_ctx *, const double *, long, int, const do
                                  double *, cudaStream_t);
 template int density_dev<float>(sgpu_ctx *, const float *, long, int, const double *, double *,
                                 cudaStream_t);
+
+template <typename CT>
+int density_z_dev(sgpu_ctx *ctx, const CT *psi, long ld, int ncol, const double *w_dev,
+                  double *rho, bool accumulate, cudaStream_t st)
+{
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    k_density_z<CT><<<egrid(ctx->Nd), 256, 0, st>>>(psi, ld, ncol, w_dev, rho, ctx->Nd,
+                                                    accumulate ? 1 : 0);
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+template int density_z_dev<double2>(sgpu_ctx *, const double2 *, long, int, const double *,
+                                    double *, bool, cudaStream_t);
+template int density_z_dev<float2>(sgpu_ctx *, const float2 *, long, int, const double *,
+                                   double *, bool, cudaStream_t);
 
 int lda_pw_dev(sgpu_ctx *ctx, const double *rho, const double *rho_core, double rhotol,
                double *vxc, double *exc, cudaStream_t st)

@@ -7,6 +7,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -318,6 +319,32 @@ int kerker_dev(sgpu_ctx *ctx, const double *f, double a, double kTF, double idie
                double tol, double *Pf, cudaStream_t st);
 int mixing_init(sgpu_ctx *ctx, const MixParams &prm, const double *x0);
 int mixing_step(sgpu_ctx *ctx, int iter_count, double *g, cudaStream_t st);
+// rho (+)= sum_n w_n |psi_n|^2 over ncol complex columns (CT = double2 or float2)
+template <typename CT>
+int density_z_dev(sgpu_ctx *ctx, const CT *psi, long ld, int ncol, const double *w_dev,
+                  double *rho, bool accumulate, cudaStream_t st);
+
+// ---- SCF pieces shared by the Gamma-point and k-point drivers (scf.cu)
+// uniform [-0.5, 0.5) values from (seed, index)
+void init_orbitals(sgpu_ctx *ctx, double *X, long n, unsigned long long seed, int blocks,
+                   cudaStream_t st);
+double smearing(double beta, double lam, double ef, int type);
+// Fermi level: sum_i w_i f(lam_i) = nelec; *status = 1 when no bracket is found
+double fermi_level(const std::vector<double> &lam, const std::vector<double> &w, double nelec,
+                   double beta, int type, double x1, double x2, double tol, int max_iter,
+                   int *status);
+int lanczos_run(sgpu_ctx *ctx, long len, const std::function<int(const double *, double *)> &apply,
+                const double *x0, double tol, int maxit, double *eigmin, double *eigmax,
+                cudaStream_t st);
+// complex (k-point) Rayleigh-Ritz pieces (kpoint.cu)
+template <typename CT>
+int hamiltonian_z(sgpu_ctx *ctx, int spin, const double *k, int ncol, double c, const CT *x,
+                  long ldx, CT *hx, long ldh, double s1, double s2, const CT *z, long ldz,
+                  cudaStream_t st);
+int kpoint_set_phases(sgpu_ctx *ctx, const double *k, cudaStream_t st);
+template <typename CT>
+int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
+                   double *lambda, cudaStream_t st);
 
 // ---- elementwise helpers (util.cu)
 template <typename T>

@@ -141,12 +141,23 @@ def capture_scf(sysd, psp_dir, out_npz, out_json, sparc_bin):
                    stdout=subprocess.DEVNULL)
     ref = parse_reference_outputs(base)
     r = RefSystem(base)
-    types, images = r.nonlocal_data()
+    extra = {}
+    if "kpoint_grid" in sysd:
+        # k-point run: the reduced k-points with their weights (k1_loc.., kptWts_loc) and the
+        # projector images with their coordinates (the Bloch phases need them)
+        from ref_capture import RefKpt
+        rk = RefKpt(r)
+        types, images = rk.images()
+        extra = dict(kpts=rk.kpts, kpt_wts=rk.wts,
+                     img_coords=np.stack([im["coords"] for im in images]) if images
+                     else np.zeros((0, 3)))
+    else:
+        types, images = r.nonlocal_data()
     flat = flatten_nonlocal(types, images, r.n_atom)
     fields, params = scf_setup(r)
     np.savez_compressed(
         out_npz, Nx=r.Nx, Ny=r.Ny, Nz=r.Nz, FDn=r.order // 2, h=r.h, L=r.L, dV=r.dV,
-        cx=r.cx, cy=r.cy, cz=r.cz, n_atom=r.n_atom, Nstates=r.Nstates,
+        cx=r.cx, cy=r.cy, cz=r.cz, n_atom=r.n_atom, Nstates=r.Nstates, **extra,
         **{k: v for k, v in fields.items()}, **{"nl_" + k: v for k, v in flat.items()})
     ref["params"] = params
     ref["system"] = sysd["name"]
@@ -249,7 +260,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=reference_root(),
                     help="reference tree (default: $SPARC_REFERENCE, else /root/reference)")
-    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "setup", "si216", "mixing"],
+    ap.add_argument("--only", choices=["kernels", "kpt", "scf", "scf_kpt", "setup", "si216",
+                                       "mixing"],
                     default=None,
                     help="regenerate one group of fixtures only")
     args = ap.parse_args()
@@ -262,6 +274,19 @@ def main():
         capture_scf_result(systems.si216_c4(), psp_dir, js, sparc_bin)
         print("wrote", js)
         return
+    if args.only in (None, "scf_kpt"):
+        sparc_bin = os.path.join(HERE, "..", "..", "oracle", "_ref", "sparc")
+        sysd = systems.si2_kpt()
+        npz = os.path.join(HERE, f"{sysd['name']}_scf.npz")
+        js = os.path.join(HERE, f"{sysd['name']}_scf_ref.json")
+        p = ctx.Process(target=capture_scf, args=(sysd, psp_dir, npz, js, sparc_bin))
+        p.start()
+        p.join()
+        if p.exitcode != 0:
+            raise SystemExit("k-point SCF capture failed")
+        print("wrote", npz, os.path.getsize(npz), "bytes and", js)
+        if args.only == "scf_kpt":
+            return
     if args.only in (None, "mixing"):
         path = os.path.join(HERE, "Si8_c1_mixing.npz")
         p = ctx.Process(target=capture_mixing, args=(systems.si8_c1(), psp_dir, path))
