@@ -234,6 +234,15 @@ int sgpu_CalculateDensity_psi(sgpu_ctx *ctx, const double *psi, int ld, int ncol
 int sgpu_Calculate_Vxc_LDA_PW(sgpu_ctx *ctx, const double *rho, const double *rho_core,
                               double xc_rhotol, double *vxc, double *exc);
 
+/* Spin-polarised LDA (Slater exchange + PW92 correlation, collinear spin): each spin density
+ * plus half of rho_core (may be NULL), clamped at xc_rhotol; vxc receives 2 Nd values (up,
+ * then down), exc Nd values (energy per particle of the total). Replaces the spin branch of
+ * Calculate_Vxc (src/exchangeCorrelation.c:227-347, slater_spin :759, pw_spin :787,
+ * add_rho_core :1254 with three columns). */
+int sgpu_Calculate_Vxc_LSDA_PW(sgpu_ctx *ctx, const double *rho_up, const double *rho_dn,
+                               const double *rho_core, double xc_rhotol, double *vxc,
+                               double *exc);
+
 /* Alternating Anderson-Richardson solve of b + (Lap + c) x = 0 with the Jacobi preconditioner
  * (x: initial guess in, solution out). Replaces AAR (src/linearSolver.c:37) called with
  * poisson_residual and Jacobi_preconditioner (src/electrostatics.c:1682). Returns
@@ -259,6 +268,20 @@ int sgpu_Mixing_init(sgpu_ctx *ctx, int history, int pulay_frequency, int pulay_
                      double kTF, double idiemac, double tol_precond, double neg_charge,
                      const double *rho_in);
 int sgpu_Mixing_periodic_pulay(sgpu_ctx *ctx, int iter_count, double *rho);
+
+/* The same mixing for collinear spin (spin_typ 1): the mixed vector is [rho, magz]
+ * (src/mixing.c:250-258); the total-density residual is preconditioned as above, the
+ * magnetization residual by MixingParameterMag / MixingParameterSimpleMag alone
+ * (MixingPrecondMag = 0, the reference's default), each part is shifted to keep its residual's
+ * integral (src/mixing.c:376-385), and only rho is clamped and rescaled. rho and mag (Nd each)
+ * hold the output density and magnetization of iteration iter_count on entry and the next
+ * input on return. */
+int sgpu_Mixing_init_spin(sgpu_ctx *ctx, int history, int pulay_frequency, int pulay_restart,
+                          double mixing_parameter, double mixing_parameter_simple,
+                          double mixing_parameter_mag, double mixing_parameter_simple_mag,
+                          int kerker, double kTF, double idiemac, double tol_precond,
+                          double neg_charge, const double *rho_in, const double *mag_in);
+int sgpu_Mixing_periodic_pulay_spin(sgpu_ctx *ctx, int iter_count, double *rho, double *mag);
 
 /* error = ||rho_out - rho_in|| / ||rho_out||. Replaces Evaluate_scf_error
  * (src/electronicGroundState.c:1160). */
@@ -391,7 +414,14 @@ typedef struct {
     double *psi_out;            /* optional (host or device) Nd x Nstates: the final orbitals,
                                    as the force calculation uses them (NULL: not returned) */
     double *phi_out;            /* optional Nd: electrostatic potential of the final density */
-    double *vxc_out;            /* optional Nd: exchange-correlation potential of the same */
+    double *vxc_out;            /* optional Nd: exchange-correlation potential of the same
+                                   (2 Nd, up then down, with collinear spin) */
+    int spin_typ;               /* 0: spin-unpolarised; 1: collinear spin (sgpu_scf_kpt only) */
+    const double *mag_init;     /* spin_typ 1: initial magnetization density, Nd (the
+                                   reference's mag after Init_electronDensity) */
+    double mixing_param_mag;    /* MixingParameterMag (<= 0: mixing_param) */
+    double mixing_param_simple_mag; /* MixingParameterSimpleMag (<= 0: the value above) */
+    double *mag_out;            /* optional Nd: the final (mixed) magnetization density */
 } sgpu_scf_params;
 
 typedef struct {
@@ -399,6 +429,8 @@ typedef struct {
     double Etot, Eband, E1, E2, E3, Exc, Esc, Entropy, Efermi, scf_error;
     double time_s;              /* wall time of the SCF (without the optional field outputs) */
     double filter_ms;           /* device time of filter + projection products */
+    double net_mag;             /* collinear spin: net magnetization of the last output
+                                   density, sum(mag) dV (Bohr magneton) */
 } sgpu_scf_result;
 
 /* Single-point SCF for an orthogonal periodic Gamma-point cell, spin-unpolarised, LDA (PW92),

@@ -13,7 +13,9 @@
  *   poisson_residual             src/lapVecRoutines.c:69
  *   AAR                          src/linearSolver.c:37 (with Jacobi_preconditioner)
  *   Kerker_precond               src/mixing.c:462
- *   Mixing_periodic_pulay        src/mixing.c:213 (after Update_mixing_hist_xk)
+ *   Mixing_periodic_pulay        src/mixing.c:213 (after Update_mixing_hist_xk), also with
+ *                                collinear spin ([rho, magz], src/mixing.c:250-258)
+ *   Calculate_Vxc (spin branch)  src/exchangeCorrelation.c:227
  * One system per process: the reference keeps its state in the SPARC_OBJ built here.
  */
 #include <stdio.h>
@@ -292,6 +294,51 @@ void ref_mix_step(int iter, double *g)
     memcpy(S.electronDens, g, sizeof(double) * S.Nd_d);
     Mixing_periodic_pulay(&S, iter);
     memcpy(g, S.electronDens, sizeof(double) * S.Nd_d);
+}
+
+/* ---- collinear spin (spin_typ 1). ref_spin_fields: prm = MixingParameterMag,
+ * MixingParameterSimpleMag, MixingPrecondMag; for a spin run also the initial [total, up,
+ * down] density and magnetization as Init_electronDensity left them (src/orbitalElecDensInit.c
+ * :145-151). Returns spin_typ. */
+int ref_spin_fields(double *rho3, double *mag, double *prm)
+{
+    prm[0] = S.MixingParameterMag;
+    prm[1] = S.MixingParameterSimpleMag;
+    prm[2] = S.MixingPrecondMag;
+    if (S.spin_typ == 1) {
+        memcpy(rho3, S.electronDens, sizeof(double) * 3 * S.Nd);
+        memcpy(mag, S.mag, sizeof(double) * S.Nd);
+    }
+    return S.spin_typ;
+}
+
+/* spin Vxc of the reference (Calculate_Vxc, spin branch) for [total, up, down] rho3:
+ * vxc (2 Nd: up, down) and e_xc (Nd) */
+void ref_vxc_spin(const double *rho3, double *vxc, double *exc)
+{
+    memcpy(S.electronDens, rho3, sizeof(double) * 3 * S.Nd);
+    Calculate_Vxc(&S);
+    memcpy(vxc, S.XCPotential, sizeof(double) * 2 * S.Nd);
+    memcpy(exc, S.e_xc, sizeof(double) * S.Nd);
+}
+
+/* spin mixing: the history starts from [rho0, mag0]; each step hands [g, gmag] (output
+ * density and magnetization of iteration iter) to Mixing_periodic_pulay and returns the
+ * mixed pair in place */
+void ref_mix_init_spin(const double *rho0, const double *mag0)
+{
+    memcpy(S.electronDens, rho0, sizeof(double) * S.Nd_d);
+    memcpy(S.mag, mag0, sizeof(double) * S.Nd_d);
+    Update_mixing_hist_xk(&S);
+}
+
+void ref_mix_step_spin(int iter, double *g, double *gmag)
+{
+    memcpy(S.electronDens, g, sizeof(double) * S.Nd_d);
+    memcpy(S.mag, gmag, sizeof(double) * S.Nd_d);
+    Mixing_periodic_pulay(&S, iter);
+    memcpy(g, S.electronDens, sizeof(double) * S.Nd_d);
+    memcpy(gmag, S.mag, sizeof(double) * S.Nd_d);
 }
 
 SPARC_OBJ *ref_harness_obj(void) { return &S; }

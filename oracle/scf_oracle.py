@@ -40,6 +40,47 @@ def lda_pw(rho, rho_core, rhotol):
     return vx + vc, ex + ec
 
 
+def _pw92_g(rs, A, a1, b1, b2, b3, b4):
+    """PW92 G(rs) for one parameter set and its rs derivative (PRB 45, 13244, eq. 10)."""
+    rsq = np.sqrt(rs)
+    q1 = 2.0 * A * (b1 * rsq + b2 * rs + b3 * rs * rsq + b4 * rs * rs)
+    dq1 = A * (b1 / rsq + 2.0 * b2 + 3.0 * b3 * rsq + 4.0 * b4 * rs)
+    lg = np.log(1.0 + 1.0 / q1)
+    q0 = -2.0 * A * (1.0 + a1 * rs)
+    return q0 * lg, -2.0 * A * a1 * lg - q0 * dq1 / (q1 * (q1 + 1.0))
+
+
+def lsda_pw(up, dn, rho_core, rhotol):
+    """Spin-polarised Slater exchange + PW92 correlation (collinear spin): each spin density
+    plus half the core density, clamped at rhotol; returns (vxc (2, Nd), exc). Restates
+    slater_spin (src/exchangeCorrelation.c:759), pw_spin (:787) with its zeta scaling by
+    1 - 1e-6, and add_rho_core with three columns (:1254)."""
+    hc = 0.5 * rho_core if rho_core is not None else 0.0
+    ru = np.maximum(up + hc, rhotol)
+    rd = np.maximum(dn + hc, rhotol)
+    r = ru + rd
+    kx = 0.75 * (6.0 / math.pi) ** (1.0 / 3.0)
+    exu, exd = -kx * np.cbrt(ru), -kx * np.cbrt(rd)
+    ex = (exu * ru + exd * rd) / r
+    rs = (3.0 / (4.0 * math.pi)) ** (1.0 / 3.0) / np.cbrt(r)
+    e0, de0 = _pw92_g(rs, 0.031091, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294)
+    e1, de1 = _pw92_g(rs, 0.015545, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517)
+    am, dam = _pw92_g(rs, 0.016887, 0.11125, 10.357, 3.6231, 0.88026, 0.49671)  # -alpha_c
+    az, fpp0 = 1.0 - 1e-6, 1.709921
+    fden = 1.0 / (2.0 ** (4.0 / 3.0) - 2.0)
+    z = (ru - rd) / r
+    zp, zm = 1.0 + az * z, 1.0 - az * z
+    f = (zp ** (4.0 / 3.0) + zm ** (4.0 / 3.0) - 2.0) * fden
+    df = (4.0 / 3.0) * az * (np.cbrt(zp) - np.cbrt(zm)) * fden
+    z4 = z ** 4
+    ec = e0 - am / fpp0 * f * (1.0 - z4) + (e1 - e0) * f * z4
+    dec_drs = de0 - dam / fpp0 * f * (1.0 - z4) + (de1 - de0) * f * z4
+    dec_dz = -am / fpp0 * (df * (1.0 - z4) - 4.0 * z ** 3 * f) + (e1 - e0) * (df * z4 + 4.0 * z ** 3 * f)
+    base = ec - rs / 3.0 * dec_drs - z * dec_dz
+    vxc = np.stack([4.0 / 3.0 * exu + base + dec_dz, 4.0 / 3.0 * exd + base - dec_dz])
+    return vxc, ex + ec
+
+
 def _lstsq_min_norm(A, b):
     """Minimum-norm least squares as LAPACK dgelsd with rcond = -1 (machine epsilon)."""
     return np.linalg.lstsq(A, b, rcond=np.finfo(float).eps)[0]
@@ -106,13 +147,20 @@ def kerker(orc, f, a, kTF, idiemac, tol, Pf0):
 
 class PulayMixer:
     """Periodic-Pulay density mixing with Kerker preconditioning, restating
-    Mixing_periodic_pulay (src/mixing.c:213-455) and AndersonExtrapWtdAvg (:77)."""
+    Mixing_periodic_pulay (src/mixing.c:213-455) and AndersonExtrapWtdAvg (:77). With
+    nspden = 2 (collinear spin) x is [rho, magz]: the magnetization residual is scaled by
+    beta_mag / omega_mag alone (MixingPrecondMag = 0), both preconditioned parts are shifted
+    to their residual's integral (:376-385), and only rho is clamped and rescaled."""
 
     def __init__(self, orc, x0, neg_charge, dV, m=7, p=1, beta=0.3, omega=0.3, kerker_on=1,
-                 kTF=1.0, idiemac=0.1, precond_tol=1e-4):
+                 kTF=1.0, idiemac=0.1, precond_tol=1e-4, nspden=1, beta_mag=None,
+                 omega_mag=None):
         self.orc, self.m, self.p, self.beta, self.omega = orc, m, p, beta, omega
         self.kerker, self.kTF, self.idiemac, self.tol = kerker_on, kTF, idiemac, precond_tol
         self.neg_charge, self.dV = neg_charge, dV
+        self.nspden = nspden
+        self.beta_mag = beta if beta_mag is None else beta_mag
+        self.omega_mag = self.beta_mag if omega_mag is None else omega_mag
         N = x0.size
         self.x_k = x0.copy()
         self.x_km1 = np.zeros(N)
@@ -138,13 +186,21 @@ class PulayMixer:
             fw = self.f_k - gam @ self.F
         else:
             xw, fw = self.x_k.copy(), self.f_k.copy()
+        nd = g.size // self.nspden
+        Pf = self.Pf.copy()
         if self.kerker:
-            self.Pf = kerker(self.orc, fw, amix, self.kTF, self.idiemac, self.tol, self.Pf)
+            Pf[:nd] = kerker(self.orc, fw[:nd], amix, self.kTF, self.idiemac, self.tol, Pf[:nd])
         else:
-            self.Pf = amix * fw
-        x = xw + self.Pf
-        x[x < 0.0] = 0.0
-        x *= -self.neg_charge / (x.sum() * self.dV)
+            Pf[:nd] = amix * fw[:nd]
+        if self.nspden == 2:
+            Pf[nd:] = (self.beta_mag if pulay else self.omega_mag) * fw[nd:]
+            for c in range(2):
+                seg = slice(c * nd, (c + 1) * nd)
+                Pf[seg] += (fw[seg].sum() - Pf[seg].sum()) / nd
+        self.Pf = Pf
+        x = xw + Pf
+        x[:nd][x[:nd] < 0.0] = 0.0
+        x[:nd] *= -self.neg_charge / (x[:nd].sum() * self.dV)
         self.x_km1 = self.x_k
         self.x_k = x.copy()
         return x

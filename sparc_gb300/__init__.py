@@ -28,6 +28,7 @@ EXPORTED = [
     "sgpu_CalculateDensity_psi", "sgpu_Calculate_Vxc_LDA_PW", "sgpu_AAR",
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
     "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_scf_kpt", "sgpu_Vnl_vec_mult_noalloc",
+    "sgpu_Calculate_Vxc_LSDA_PW", "sgpu_Mixing_init_spin", "sgpu_Mixing_periodic_pulay_spin",
     "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
     "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
     "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
@@ -86,7 +87,9 @@ class ScfParams(ctypes.Structure):
                 ("tail_fp64_degrees", ctypes.c_int), ("seed", ctypes.c_ulonglong),
                 ("verbose", ctypes.c_int), ("history", ctypes.c_void_p),
                 ("psi_out", ctypes.c_void_p), ("phi_out", ctypes.c_void_p),
-                ("vxc_out", ctypes.c_void_p)]
+                ("vxc_out", ctypes.c_void_p), ("spin_typ", ctypes.c_int),
+                ("mag_init", ctypes.c_void_p), ("mixing_param_mag", ctypes.c_double),
+                ("mixing_param_simple_mag", ctypes.c_double), ("mag_out", ctypes.c_void_p)]
 
 
 class ScfResult(ctypes.Structure):
@@ -97,7 +100,7 @@ class ScfResult(ctypes.Structure):
                 ("E3", ctypes.c_double), ("Exc", ctypes.c_double), ("Esc", ctypes.c_double),
                 ("Entropy", ctypes.c_double), ("Efermi", ctypes.c_double),
                 ("scf_error", ctypes.c_double), ("time_s", ctypes.c_double),
-                ("filter_ms", ctypes.c_double)]
+                ("filter_ms", ctypes.c_double), ("net_mag", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -548,6 +551,30 @@ class Context:
                                       ctypes.c_double(tol_precond), ctypes.c_double(neg_charge),
                                       _ptr(rho_in)))
 
+    def Calculate_Vxc_LSDA_PW(self, rho_up, rho_dn, rho_core, xc_rhotol, vxc, exc):
+        """vxc: 2 x Nd (up, down); exc: Nd."""
+        _check(lib().sgpu_Calculate_Vxc_LSDA_PW(self._h, _ptr(rho_up), _ptr(rho_dn),
+                                                _ptr(rho_core), ctypes.c_double(xc_rhotol),
+                                                _ptr(vxc), _ptr(exc)))
+        return vxc, exc
+
+    def Mixing_init_spin(self, rho_in, mag_in, neg_charge, history=7, pulay_frequency=1,
+                         pulay_restart=0, mixing_parameter=0.3, mixing_parameter_simple=0.3,
+                         mixing_parameter_mag=0.3, mixing_parameter_simple_mag=0.3, kerker=1,
+                         kTF=1.0, idiemac=0.1, tol_precond=1e-4):
+        _check(lib().sgpu_Mixing_init_spin(
+            self._h, int(history), int(pulay_frequency), int(pulay_restart),
+            ctypes.c_double(mixing_parameter), ctypes.c_double(mixing_parameter_simple),
+            ctypes.c_double(mixing_parameter_mag), ctypes.c_double(mixing_parameter_simple_mag),
+            int(kerker), ctypes.c_double(kTF), ctypes.c_double(idiemac),
+            ctypes.c_double(tol_precond), ctypes.c_double(neg_charge), _ptr(rho_in),
+            _ptr(mag_in)))
+
+    def Mixing_periodic_pulay_spin(self, iter_count, rho, mag):
+        _check(lib().sgpu_Mixing_periodic_pulay_spin(self._h, int(iter_count), _ptr(rho),
+                                                     _ptr(mag)))
+        return rho, mag
+
     def Mixing_periodic_pulay(self, iter_count, rho):
         _check(lib().sgpu_Mixing_periodic_pulay(self._h, int(iter_count), _ptr(rho)))
         return rho
@@ -591,40 +618,51 @@ class Context:
                           "time_s": h[:, 2].tolist()}
         return out, rho, lam, occ
 
-    def scf_kpt(self, params, kpts, kpt_wts, b, rho_init, rho_core=None, fields=None):
+    def scf_kpt(self, params, kpts, kpt_wts, b, rho_init, rho_core=None, fields=None,
+                mag_init=None):
         """Run sgpu_scf_kpt on the k-points kpts (nkpt x 3, Cartesian 1/Bohr) with weights
         kpt_wts (as the reference's kptWts_loc); returns (result dict, final density,
-        eigenvalues nkpt x Nstates, occupations nkpt x Nstates). With fields a dict, it also
-        receives the final orbitals ("psi", nkpt x Nstates x Nd complex128), "phi" and "vxc"."""
+        eigenvalues nblk x Nstates, occupations nblk x Nstates), nblk = nkpt, or 2 nkpt with
+        collinear spin (mag_init given: the initial magnetization; blocks spin-major). With
+        fields a dict, it also receives the final orbitals ("psi", nblk x Nstates x Nd
+        complex128), "phi", "vxc" (nspin x Nd) and, with spin, the magnetization "mag"."""
         Ns = params.Nstates
         kp = np.ascontiguousarray(kpts, dtype=np.float64).reshape(-1, 3)
         wt = np.ascontiguousarray(kpt_wts, dtype=np.float64).reshape(-1)
         nk = kp.shape[0]
         if wt.shape[0] != nk:
             raise ValueError("one weight per k-point")
+        mag0 = None if mag_init is None else np.ascontiguousarray(mag_init, dtype=np.float64)
+        nspin = 1 if mag0 is None else 2
         rho = np.zeros(self.Nd)
-        lam = np.zeros((nk, Ns))
-        occ = np.zeros((nk, Ns))
+        lam = np.zeros((nspin * nk, Ns))
+        occ = np.zeros((nspin * nk, Ns))
         res = ScfResult()
         b = np.ascontiguousarray(b, dtype=np.float64)
         r0 = np.ascontiguousarray(rho_init, dtype=np.float64)
         rc_ = None if rho_core is None else np.ascontiguousarray(rho_core, dtype=np.float64)
         hist = np.full(3 * max(1, params.maxit_scf), np.nan)
         params.history = hist.ctypes.data
+        params.spin_typ = nspin - 1
+        params.mag_init = None if mag0 is None else mag0.ctypes.data
         if fields is not None:
-            fields["psi"] = np.zeros((nk, Ns, self.Nd), dtype=np.complex128)
+            fields["psi"] = np.zeros((nspin * nk, Ns, self.Nd), dtype=np.complex128)
             fields["phi"] = np.zeros(self.Nd)
-            fields["vxc"] = np.zeros(self.Nd)
+            fields["vxc"] = np.zeros((nspin, self.Nd))
             params.psi_out = fields["psi"].ctypes.data
             params.phi_out = fields["phi"].ctypes.data
             params.vxc_out = fields["vxc"].ctypes.data
+            if nspin == 2:
+                fields["mag"] = np.zeros(self.Nd)
+                params.mag_out = fields["mag"].ctypes.data
         try:
             _check(lib().sgpu_scf_kpt(self._h, ctypes.byref(params), int(nk), _ptr(kp), _ptr(wt),
                                       _ptr(b), _ptr(r0), _ptr(rc_), _ptr(rho), _ptr(lam),
                                       _ptr(occ), ctypes.byref(res)))
         finally:
             params.history = None
-            params.psi_out = params.phi_out = params.vxc_out = None
+            params.psi_out = params.phi_out = params.vxc_out = params.mag_out = None
+            params.mag_init = None
         out = res.as_dict()
         h = hist.reshape(-1, 3)[:out["scf_iters"]]
         out["history"] = {"Etot": h[:, 0].tolist(), "scf_error": h[:, 1].tolist(),

@@ -590,9 +590,88 @@ int sgpu_Mixing_init(sgpu_ctx *ctx, int history, int pulay_frequency, int pulay_
     return mixing_init(ctx, prm, rho_in);
 }
 
+int sgpu_Calculate_Vxc_LSDA_PW(sgpu_ctx *ctx, const double *rho_up, const double *rho_dn,
+                               const double *rho_core, double xc_rhotol, double *vxc,
+                               double *exc)
+{
+    SGPU_TRY(check(ctx));
+    const long N = ctx->Nd;
+    double *du, *dd, *dc = nullptr;
+    SGPU_TRY(stage_vec(ctx, WS_STAGE_A, rho_up, N, &du));
+    SGPU_TRY(stage_vec(ctx, WS_STAGE_B, rho_dn, N, &dd));
+    if (rho_core) SGPU_TRY(stage_vec(ctx, WS_RHS, rho_core, N, &dc));
+    double *out = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_STAGE_C, sizeof(double) * 3 * (size_t)N, (void **)&out));
+    double *dv = is_device_ptr(vxc) ? vxc : out;
+    double *de = is_device_ptr(exc) ? exc : out + 2 * N;
+    SGPU_TRY(lsda_pw_dev(ctx, du, dd, dc, xc_rhotol, dv, dv + N, de, ctx->stream));
+    SGPU_TRY(unstage_vec(ctx, dv, vxc, 2 * N));
+    SGPU_TRY(unstage_vec(ctx, de, exc, N));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
+int sgpu_Mixing_init_spin(sgpu_ctx *ctx, int history, int pulay_frequency, int pulay_restart,
+                          double mixing_parameter, double mixing_parameter_simple,
+                          double mixing_parameter_mag, double mixing_parameter_simple_mag,
+                          int kerker, double kTF, double idiemac, double tol_precond,
+                          double neg_charge, const double *rho_in, const double *mag_in)
+{
+    SGPU_TRY(check(ctx));
+    if (!rho_in || !mag_in) {
+        set_error("sgpu_Mixing_init_spin: null density or magnetization");
+        return SGPU_ERR_ARG;
+    }
+    MixParams prm;
+    prm.m = history;
+    prm.pulay_freq = std::max(1, pulay_frequency);
+    prm.restart = pulay_restart;
+    prm.beta = mixing_parameter;
+    prm.omega = mixing_parameter_simple;
+    prm.kerker = kerker;
+    prm.kTF = kTF;
+    prm.idiemac = idiemac;
+    prm.precond_tol = tol_precond;
+    prm.neg_charge = neg_charge;
+    prm.nspden = 2;
+    prm.beta_mag = mixing_parameter_mag;
+    prm.omega_mag = mixing_parameter_simple_mag;
+    const long N = ctx->Nd;
+    double *x0 = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_STAGE_A, sizeof(double) * 2 * (size_t)N, (void **)&x0));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(x0, rho_in, sizeof(double) * N, cudaMemcpyDefault, ctx->stream));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(x0 + N, mag_in, sizeof(double) * N, cudaMemcpyDefault,
+                                  ctx->stream));
+    return mixing_init(ctx, prm, x0);
+}
+
+int sgpu_Mixing_periodic_pulay_spin(sgpu_ctx *ctx, int iter_count, double *rho, double *mag)
+{
+    SGPU_TRY(check(ctx));
+    if (!ctx->mix || ctx->mix->prm.nspden != 2) {
+        set_error("sgpu_Mixing_periodic_pulay_spin: call sgpu_Mixing_init_spin first");
+        return SGPU_ERR_STATE;
+    }
+    const long N = ctx->Nd;
+    double *g = nullptr;
+    SGPU_TRY(ws_get(ctx, WS_STAGE_A, sizeof(double) * 2 * (size_t)N, (void **)&g));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(g, rho, sizeof(double) * N, cudaMemcpyDefault, ctx->stream));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(g + N, mag, sizeof(double) * N, cudaMemcpyDefault, ctx->stream));
+    SGPU_TRY(mixing_step(ctx, iter_count, g, ctx->stream));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(rho, g, sizeof(double) * N, cudaMemcpyDefault, ctx->stream));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(mag, g + N, sizeof(double) * N, cudaMemcpyDefault, ctx->stream));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SGPU_OK;
+}
+
 int sgpu_Mixing_periodic_pulay(sgpu_ctx *ctx, int iter_count, double *rho)
 {
     SGPU_TRY(check(ctx));
+    if (ctx->mix && ctx->mix->prm.nspden != 1) {
+        set_error("sgpu_Mixing_periodic_pulay: the history was set up for spin "
+                  "(use sgpu_Mixing_periodic_pulay_spin)");
+        return SGPU_ERR_STATE;
+    }
     double *dr;
     SGPU_TRY(stage_vec(ctx, WS_STAGE_A, rho, ctx->Nd, &dr));
     SGPU_TRY(mixing_step(ctx, iter_count, dr, ctx->stream));
@@ -636,6 +715,11 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b, const d
     }
     if (prm->precision != SGPU_PREC_FP64 && prm->precision != SGPU_PREC_FP32) {
         set_error("sgpu_scf: precision must be SGPU_PREC_FP64 or SGPU_PREC_FP32");
+        return SGPU_ERR_ARG;
+    }
+    if (prm->spin_typ != 0) {
+        set_error("sgpu_scf: spin-polarised runs go through sgpu_scf_kpt (a k = 0 grid for the "
+                  "Gamma point)");
         return SGPU_ERR_ARG;
     }
     if (prm->graded_tail < 0 || prm->graded_tail > 1 ||

@@ -126,6 +126,73 @@ __global__ void k_lda_pw(const double *__restrict__ rho, const double *__restric
     }
 }
 
+// PW92 correlation energy per particle of one parameter set (unpolarised, fully polarised
+// or the spin stiffness), G(rs) = -2A (1 + a1 rs) ln(1 + 1 / (2A (b1 rs^1/2 + b2 rs +
+// b3 rs^3/2 + b4 rs^2))), and its rs derivative
+__device__ __forceinline__ void pw92_g(double rs, double rsq, double A, double a1, double b1,
+                                       double b2, double b3, double b4, double *g, double *dg)
+{
+    const double q1 = 2.0 * A * (b1 * rsq + b2 * rs + b3 * rs * rsq + b4 * rs * rs);
+    const double dq1 = A * (b1 / rsq + 2.0 * b2 + 3.0 * b3 * rsq + 4.0 * b4 * rs);
+    const double lg = log(1.0 + 1.0 / q1);
+    const double q0 = -2.0 * A * (1.0 + a1 * rs);
+    *g = q0 * lg;
+    *dg = -2.0 * A * a1 * lg - q0 * dq1 / (q1 * (q1 + 1.0));
+}
+
+// LSDA: spin-polarised Slater exchange + PW92 correlation (J. P. Perdew and Y. Wang, PRB 45,
+// 13244 (1992), eqs. 8-10 and table I) on the spin densities (up, dn) with half the model
+// core density added to each and each clamped at rhotol; the total is their sum. The spin
+// interpolation f(zeta) takes zeta scaled by 1 - 1e-6, which keeps it finite at full
+// polarisation, as the reference's pw_spin does. Outputs Vxc_up, Vxc_dn and
+// exc = ex + ec per particle of the total density.
+__global__ void k_lsda_pw(const double *__restrict__ up_in, const double *__restrict__ dn_in,
+                          const double *__restrict__ rho_core, double rhotol,
+                          double *__restrict__ vxc_up, double *__restrict__ vxc_dn,
+                          double *__restrict__ exc, long n)
+{
+    const double kx = 0.9305257363491000;     // (3/4) (6/pi)^(1/3): ex_s = -kx rho_s^(1/3)
+    const double C31 = 0.6203504908993999;    // (3/(4 pi))^(1/3)
+    const double fpp0_inv = 1.0 / 1.709921;   // 1 / f''(0)
+    const double fden = 1.0 / (2.0 * 1.2599210498948732 - 2.0);  // 1 / (2^(4/3) - 2)
+    const double az = 1.0 - 1.0e-6;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const double hc = rho_core ? 0.5 * rho_core[i] : 0.0;
+        double ru = up_in[i] + hc, rd = dn_in[i] + hc;
+        if (ru < rhotol) ru = rhotol;
+        if (rd < rhotol) rd = rhotol;
+        const double r = ru + rd;
+        const double cu = cbrt(ru), cd = cbrt(rd);
+        // exchange: E_x = sum_s -kx rho_s^(4/3)
+        const double exu = -kx * cu, exd = -kx * cd;
+        const double ex = (exu * ru + exd * rd) / r;
+        const double vxu = (4.0 / 3.0) * exu, vxd = (4.0 / 3.0) * exd;
+        // correlation
+        const double rs = C31 / cbrt(r);
+        const double rsq = sqrt(rs);
+        double e0, de0, e1, de1, am, dam;   // am = -alpha_c
+        pw92_g(rs, rsq, 0.031091, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294, &e0, &de0);
+        pw92_g(rs, rsq, 0.015545, 0.20548, 14.1189, 6.1977, 3.3662, 0.62517, &e1, &de1);
+        pw92_g(rs, rsq, 0.016887, 0.11125, 10.357, 3.6231, 0.88026, 0.49671, &am, &dam);
+        const double z = (ru - rd) / r;
+        const double zp = 1.0 + az * z, zm = 1.0 - az * z;
+        const double czp = cbrt(zp), czm = cbrt(zm);
+        const double f = (zp * czp + zm * czm - 2.0) * fden;
+        const double df = (4.0 / 3.0) * az * (czp - czm) * fden;
+        const double z3 = z * z * z, z4 = z3 * z;
+        // ec = e0 - am f (1 - z^4) / f''(0) + (e1 - e0) f z^4
+        const double ec = e0 - am * fpp0_inv * f * (1.0 - z4) + (e1 - e0) * f * z4;
+        const double dec_drs = de0 - dam * fpp0_inv * f * (1.0 - z4) + (de1 - de0) * f * z4;
+        const double dec_dz = -am * fpp0_inv * (df * (1.0 - z4) - 4.0 * z3 * f) +
+                              (e1 - e0) * (df * z4 + 4.0 * z3 * f);
+        const double base = ec - (rs / 3.0) * dec_drs - z * dec_dz;
+        vxc_up[i] = vxu + base + dec_dz;
+        vxc_dn[i] = vxd + base - dec_dz;
+        exc[i] = ex + ec;
+    }
+}
+
 // AAR bookkeeping for one iteration (after the residual r is known):
 //   f = minv * r; if hist >= 0: X[:,hist] = x - x_old, F[:,hist] = f - f_old;
 //   x_old = x; f_old = f; if richardson: x = x_old + omega * f
@@ -202,6 +269,16 @@ __global__ void k_poisson_rhs(long n, const double *__restrict__ b,
 }
 
 // x = max(x, 0); flag set if any was negative
+// x += (*a - *b) * scale: the shift that gives x the integral *a in place of *b
+__global__ void k_shift_to(long n, double *__restrict__ x, const double *__restrict__ a,
+                           const double *__restrict__ b, double scale)
+{
+    const double s = (*a - *b) * scale;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x)
+        x[i] += s;
+}
+
 __global__ void k_clamp_neg(long n, double *__restrict__ x, int *__restrict__ flag)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
@@ -366,6 +443,16 @@ int lda_pw_dev(sgpu_ctx *ctx, const double *rho, const double *rho_core, double 
     return SGPU_OK;
 }
 
+int lsda_pw_dev(sgpu_ctx *ctx, const double *up, const double *dn, const double *rho_core,
+                double rhotol, double *vxc_up, double *vxc_dn, double *exc, cudaStream_t st)
+{
+    ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+    k_lsda_pw<<<egrid(ctx->Nd), 256, 0, st>>>(up, dn, rho_core, rhotol, vxc_up, vxc_dn, exc,
+                                              ctx->Nd);
+    SGPU_CUDA_TRY(cudaGetLastError());
+    return SGPU_OK;
+}
+
 int axpby_dev(sgpu_ctx *ctx, long n, double a, const double *x, double b, const double *y,
               double *z, cudaStream_t st)
 {
@@ -398,11 +485,11 @@ int remove_mean_dev(sgpu_ctx *ctx, double *x, cudaStream_t st)
 }
 
 int scf_error_dev(sgpu_ctx *ctx, const double *out, const double *in, double *err,
-                  cudaStream_t st)
+                  cudaStream_t st, long n)
 {
     double *part = nullptr;
     SGPU_TRY(ws_get(ctx, WS_RED, sizeof(double) * (kRedBlocks * 2 + 8), (void **)&part));
-    k_err_partial<<<kRedBlocks, 256, 0, st>>>(out, in, ctx->Nd, part);
+    k_err_partial<<<kRedBlocks, 256, 0, st>>>(out, in, n > 0 ? n : ctx->Nd, part);
     ctx->launches++;
     std::vector<double> h(2 * kRedBlocks);
     SGPU_CUDA_TRY(cudaMemcpyAsync(h.data(), part, sizeof(double) * 2 * kRedBlocks,
@@ -545,13 +632,18 @@ int mixing_init(sgpu_ctx *ctx, const MixParams &prm, const double *x0)
         set_error("mixing: history length must be in [1, 16]");
         return SGPU_ERR_ARG;
     }
-    const long N = ctx->Nd;
+    if (prm.nspden != 1 && prm.nspden != 2) {
+        set_error("mixing: Nspden must be 1 or 2");
+        return SGPU_ERR_ARG;
+    }
+    const long N = ctx->Nd * prm.nspden;  // length of the mixed vector
     MixState *ms = ctx->mix;
-    if (!ms || ms->m != prm.m) {
+    if (!ms || ms->m != prm.m || ms->prm.nspden != prm.nspden) {
         delete ms;
         ms = new MixState();
         ctx->mix = ms;
         ms->m = prm.m;
+        ms->prm.nspden = prm.nspden;
         if (cudaMalloc(&ms->buf, sizeof(double) * (size_t)N * (8 + 2 * prm.m)) != cudaSuccess) {
             set_error("mixing: device allocation failed");
             delete ms;
@@ -572,8 +664,12 @@ int mixing_init(sgpu_ctx *ctx, const MixParams &prm, const double *x0)
     return SGPU_OK;
 }
 
-// One periodic-Pulay step (density mixing, no spin): g (the output density of this SCF
-// iteration) is replaced in place by the next input density x_{k+1}.
+// One periodic-Pulay step of density mixing (Mixing_periodic_pulay, src/mixing.c:213-450):
+// g (the output density of this SCF iteration; with collinear spin the vector [rho, magz]
+// of 2 Nd values) is replaced in place by the next input x_{k+1}. With spin, the total density
+// residual is preconditioned as without (Kerker or amix), the magnetization residual by
+// amix_mag alone (MixingPrecondMag = 0), and each preconditioned part is shifted to keep the
+// integral of its residual (src/mixing.c:376-385).
 int mixing_step(sgpu_ctx *ctx, int iter_count, double *g, cudaStream_t st)
 {
     MixState *ms = ctx->mix;
@@ -582,10 +678,12 @@ int mixing_step(sgpu_ctx *ctx, int iter_count, double *g, cudaStream_t st)
         return SGPU_ERR_STATE;
     }
     const MixParams &p = ms->prm;
-    const long N = ctx->Nd;
+    const long Nd = ctx->Nd;
+    const long N = Nd * p.nspden;
     const int m = ms->m;
     const bool pulay = ((iter_count + 1) % p.pulay_freq == 0) && iter_count > 0;
     const double amix = pulay ? p.beta : p.omega;
+    const double amix_mag = pulay ? p.beta_mag : p.omega_mag;
     if (iter_count > 0)
         SGPU_CUDA_TRY(cudaMemcpyAsync(ms->f_km1, ms->f_k, sizeof(double) * N,
                                       cudaMemcpyDeviceToDevice, st));
@@ -614,21 +712,34 @@ int mixing_step(sgpu_ctx *ctx, int iter_count, double *g, cudaStream_t st)
     if (p.kerker) {
         SGPU_TRY(kerker_dev(ctx, ms->f_wavg, amix, p.kTF, p.idiemac, p.precond_tol, ms->Pf, st));
     } else {
-        SGPU_TRY(axpby_dev(ctx, N, amix, ms->f_wavg, 0.0, nullptr, ms->Pf, st));
+        SGPU_TRY(axpby_dev(ctx, Nd, amix, ms->f_wavg, 0.0, nullptr, ms->Pf, st));
     }
-    // x_{k+1} = x_wavg + Pf, clamp negatives, renormalise to the electron count
-    SGPU_TRY(axpby_dev(ctx, N, 1.0, ms->x_wavg, 1.0, ms->Pf, g, st));
     int *flag = nullptr;
     double *part = nullptr;
     SGPU_TRY(ws_get(ctx, WS_RED, sizeof(double) * (kRedBlocks * 2 + 8 + kMaxHist * (kMaxHist + 1)),
                     (void **)&part));
     flag = reinterpret_cast<int *>(part + kRedBlocks * 2 + 4);
     double *sum = part + kRedBlocks * 2 + 2;
+    if (p.nspden == 2) {
+        SGPU_TRY(axpby_dev(ctx, Nd, amix_mag, ms->f_wavg + Nd, 0.0, nullptr, ms->Pf + Nd, st));
+        // per component: Pf += (sum f_wavg - sum Pf) / Nd
+        double *sums = nullptr;
+        SGPU_TRY(ws_get(ctx, WS_ALPHA2, sizeof(double) * 8, (void **)&sums));
+        for (int c = 0; c < 2; c++) {
+            double *sf = sums + c * 2, *sp = sf + 1;
+            SGPU_TRY(dot_dev(ctx, ms->f_wavg + c * Nd, nullptr, Nd, sf, st));
+            SGPU_TRY(dot_dev(ctx, ms->Pf + c * Nd, nullptr, Nd, sp, st));
+            k_shift_to<<<egrid(Nd), 256, 0, st>>>(Nd, ms->Pf + c * Nd, sf, sp, 1.0 / (double)Nd);
+            ctx->launches++;
+        }
+    }
+    // x_{k+1} = x_wavg + Pf, clamp negative densities, renormalise to the electron count
+    SGPU_TRY(axpby_dev(ctx, N, 1.0, ms->x_wavg, 1.0, ms->Pf, g, st));
     SGPU_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    k_clamp_neg<<<egrid(N), 256, 0, st>>>(N, g, flag);
-    SGPU_TRY(dot_dev(ctx, g, nullptr, N, sum, st));
+    k_clamp_neg<<<egrid(Nd), 256, 0, st>>>(Nd, g, flag);
+    SGPU_TRY(dot_dev(ctx, g, nullptr, Nd, sum, st));
     // scale = -NegCharge / (dV * sum)
-    k_scale_by<<<egrid(N), 256, 0, st>>>(N, g, sum, -p.neg_charge / ctx->dV);
+    k_scale_by<<<egrid(Nd), 256, 0, st>>>(Nd, g, sum, -p.neg_charge / ctx->dV);
     ctx->launches += 2;
     SGPU_CUDA_TRY(cudaMemcpyAsync(ms->x_km1, ms->x_k, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
     SGPU_CUDA_TRY(cudaMemcpyAsync(ms->x_k, g, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));

@@ -120,6 +120,9 @@ struct MixParams {
     double idiemac = 0.1;      // precond_kerker_thresh
     double precond_tol = 1e-4; // TOL_PRECOND
     double neg_charge = 0.0;   // NegCharge (minus the electron count)
+    int nspden = 1;            // Nspden: 1, or 2 for collinear spin (mixed vector [rho, magz])
+    double beta_mag = 0.3;     // MixingParameterMag
+    double omega_mag = 0.3;    // MixingParameterSimpleMag
 };
 
 // device-resident mixing history (mixing_hist_* of SPARC_OBJ)
@@ -309,8 +312,12 @@ int lda_pw_dev(sgpu_ctx *ctx, const double *rho, const double *rho_core, double 
 int axpby_dev(sgpu_ctx *ctx, long n, double a, const double *x, double b, const double *y,
               double *z, cudaStream_t st);
 int remove_mean_dev(sgpu_ctx *ctx, double *x, cudaStream_t st);
+// ||out - in|| / ||out|| over n values (n <= 0: Nd)
 int scf_error_dev(sgpu_ctx *ctx, const double *out, const double *in, double *err,
-                  cudaStream_t st);
+                  cudaStream_t st, long n = 0);
+// spin-polarised LDA (PW92) on the spin densities; rho_core may be null
+int lsda_pw_dev(sgpu_ctx *ctx, const double *up, const double *dn, const double *rho_core,
+                double rhotol, double *vxc_up, double *vxc_dn, double *exc, cudaStream_t st);
 int aar_dev(sgpu_ctx *ctx, double c, double *x, const double *b, double omega, double beta,
             int m, int p, double tol, int max_iter, int *iters, cudaStream_t st);
 int poisson_dev(sgpu_ctx *ctx, const double *rho, const double *b, double *phi, double tol,

@@ -155,6 +155,21 @@ def capture_scf(sysd, psp_dir, out_npz, out_json, sparc_bin):
         types, images = r.nonlocal_data()
     flat = flatten_nonlocal(types, images, r.n_atom)
     fields, params = scf_setup(r)
+    if sysd.get("spins"):
+        # collinear spin: initial [total, up, down] density and magnetization, the reference's
+        # spin Vxc on them, and a spin mixing sequence from the same start
+        from ref_capture import mix_spin, spin_fields, vxc_spin
+        st, rho3, mag0, mprm = spin_fields(r)
+        assert st == 1
+        vxc2, exc_s = vxc_spin(r, rho3)
+        outs = mixing_inputs(rho3[0], nsteps=9, seed=37)
+        rng = np.random.default_rng(41)
+        mouts = np.array([mag0 * (1.0 + 0.05 * rng.standard_normal(r.Nd)) + 0.01 * o
+                          for o in outs])
+        rho_m, mag_m = mix_spin(r, rho3[0], mag0, outs, mouts)
+        extra.update(rho3_0=rho3, mag0=mag0, vxc0_spin=vxc2, exc0_spin=exc_s,
+                     mix_outputs=outs, mix_mag_outputs=mouts, mix_rho=rho_m, mix_mag=mag_m)
+        params.update(mprm)
     np.savez_compressed(
         out_npz, Nx=r.Nx, Ny=r.Ny, Nz=r.Nz, FDn=r.order // 2, h=r.h, L=r.L, dV=r.dV,
         cx=r.cx, cy=r.cy, cz=r.cz, n_atom=r.n_atom, Nstates=r.Nstates, **extra,
@@ -276,15 +291,15 @@ def main():
         return
     if args.only in (None, "scf_kpt"):
         sparc_bin = os.path.join(HERE, "..", "..", "oracle", "_ref", "sparc")
-        sysd = systems.si2_kpt()
-        npz = os.path.join(HERE, f"{sysd['name']}_scf.npz")
-        js = os.path.join(HERE, f"{sysd['name']}_scf_ref.json")
-        p = ctx.Process(target=capture_scf, args=(sysd, psp_dir, npz, js, sparc_bin))
-        p.start()
-        p.join()
-        if p.exitcode != 0:
-            raise SystemExit("k-point SCF capture failed")
-        print("wrote", npz, os.path.getsize(npz), "bytes and", js)
+        for sysd in (systems.si2_kpt(), systems.al4_spin_kpt()):
+            npz = os.path.join(HERE, f"{sysd['name']}_scf.npz")
+            js = os.path.join(HERE, f"{sysd['name']}_scf_ref.json")
+            p = ctx.Process(target=capture_scf, args=(sysd, psp_dir, npz, js, sparc_bin))
+            p.start()
+            p.join()
+            if p.exitcode != 0:
+                raise SystemExit(f"k-point SCF capture failed for {sysd['name']}")
+            print("wrote", npz, os.path.getsize(npz), "bytes and", js)
         if args.only == "scf_kpt":
             return
     if args.only in (None, "mixing"):

@@ -184,6 +184,42 @@ class RefSystem:
         return np.array(mixed)
 
 
+def spin_fields(r):
+    """Collinear-spin set-up of RefSystem r: (spin_typ, [total, up, down] initial density,
+    initial magnetization, magnetization mixing parameters)."""
+    rho3 = np.zeros(3 * r.Nd)
+    mag = np.zeros(r.Nd)
+    prm = np.zeros(3)
+    st = r.lib.ref_spin_fields(_d(rho3), _d(mag), _d(prm))
+    return int(st), rho3.reshape(3, r.Nd), mag, dict(MixingParameterMag=float(prm[0]),
+                                                       MixingParameterSimpleMag=float(prm[1]),
+                                                       MixingPrecondMag=float(prm[2]))
+
+
+def vxc_spin(r, rho3):
+    """The reference's spin Vxc (2 x Nd) and e_xc (Nd) for [total, up, down] rho3."""
+    rho3 = np.ascontiguousarray(rho3, dtype=np.float64).reshape(-1)
+    vxc = np.zeros(2 * r.Nd)
+    exc = np.zeros(r.Nd)
+    r.lib.ref_vxc_spin(_d(rho3), _d(vxc), _d(exc))
+    return vxc.reshape(2, r.Nd), exc
+
+
+def mix_spin(r, rho0, mag0, outputs, mag_outputs):
+    """The reference's collinear-spin periodic Pulay mixing: (mixed densities, mixed
+    magnetizations) after each SCF iteration."""
+    r.lib.ref_mix_init_spin(_d(np.ascontiguousarray(rho0, dtype=np.float64)),
+                            _d(np.ascontiguousarray(mag0, dtype=np.float64)))
+    rho_m, mag_m = [], []
+    for it, (g, gm) in enumerate(zip(outputs, mag_outputs)):
+        g = np.array(g, dtype=np.float64)
+        gm = np.array(gm, dtype=np.float64)
+        r.lib.ref_mix_step_spin(ctypes.c_int(it), _d(g), _d(gm))
+        rho_m.append(g)
+        mag_m.append(gm)
+    return np.array(rho_m), np.array(mag_m)
+
+
 class RefKpt:
     """k-point (complex) kernels of a RefSystem built from a system with a k-point grid.
     Complex blocks are numpy complex128 arrays of shape (ncol, Nd)."""
@@ -309,14 +345,24 @@ def parse_reference_outputs(base):
             elif line.startswith("-Entropy*kb*T"):
                 out["Entropy"] = float(line.split(":")[1].split()[0])
     lam, occ = [], []
+    lam_dn, occ_dn = [], []  # collinear spin: the second pair of columns
     with open(base + ".eigen") as fh:
         for line in fh:
             p = line.split()
-            if len(p) == 3 and p[0].isdigit():
+            if len(p) in (3, 5) and p[0].isdigit():
                 lam.append(float(p[1]))
                 occ.append(float(p[2]))
-    out["lambda"] = lam
-    out["occ"] = occ
+                if len(p) == 5:
+                    lam_dn.append(float(p[3]))
+                    occ_dn.append(float(p[4]))
+    # spin-major as the reference's lambda array (n + k Ns + spin Nk Ns); occupations as
+    # printed (occ * 2 / (Nspin Nspinor))
+    out["lambda"] = lam + lam_dn
+    out["occ"] = occ + occ_dn
+    with open(base + ".out") as fh:
+        for line in fh:
+            if line.startswith("Net magnetization"):
+                out["net_mag"] = float(line.split(":")[1].split()[0])
     forces = []
     with open(base + ".static") as fh:
         lines = fh.read().splitlines()

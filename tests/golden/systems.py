@@ -96,6 +96,18 @@ def si2_kpt(seed=8):
     return d
 
 
+def al4_spin_kpt(seed=10):
+    """The Al4 FCC cell with a 2x2x2 k-point grid, spin-polarised (collinear) from seeded
+    initial moments of +-0.2 per atom: a small case of the batched k-point/spin SCF."""
+    d = al4_small(seed)
+    rng = np.random.default_rng(seed + 1)
+    d["name"] = "Al4_spin_kpt"
+    d["kpoint_grid"] = (2, 2, 2)
+    d["spins"] = {"Al": rng.choice([-0.2, 0.2], size=4) + rng.normal(0.0, 0.02, size=4)}
+    d["keys"] = dict(d["keys"], SPIN_TYP="1", NSTATES="16", SMEARING="0.003", MESH_SPACING="0.45")
+    return d
+
+
 def write_system(sysd, outdir, psp_dir):
     """Write <name>.inpt and <name>.ion for the system into outdir."""
     os.makedirs(outdir, exist_ok=True)
@@ -114,6 +126,8 @@ def write_system(sysd, outdir, psp_dir):
         ion += [f"ATOM_TYPE: {sym}", f"N_TYPE_ATOM: {len(pos)}",
                 f"PSEUDO_POT: {os.path.join(psp_dir, psp[sym])}", "COORD:"]
         ion += [f"  {p[0]:.12f} {p[1]:.12f} {p[2]:.12f}" for p in pos]
+        if sym in sysd.get("spins", {}):
+            ion += ["SPIN:"] + [f"  {v:.12f}" for v in sysd["spins"][sym]]
         ion.append("")
     with open(os.path.join(outdir, name + ".ion"), "w") as f:
         f.write("\n".join(ion) + "\n")

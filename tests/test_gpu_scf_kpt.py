@@ -1,7 +1,9 @@
-"""GPU parity of the k-point SCF (sgpu_scf_kpt) against the reference program's own run of the
-Si2 box with a 3x3x3 k-point grid (14 symmetry-reduced k-points; tests/golden/Si2_kpt_scf.npz
-holds the reference's set-up, k-points and weights, Si2_kpt_scf_ref.json its converged
-result, both made by tests/golden/make_golden.py --only scf_kpt).
+"""GPU parity of the k-point SCF (sgpu_scf_kpt) against the reference program's own runs:
+the Si2 box with a 3x3x3 k-point grid (14 symmetry-reduced k-points) and, with collinear spin,
+the Al4 FCC cell with a 2x2x2 grid from seeded +-0.2 moments. tests/golden/<name>_scf.npz
+holds the reference's set-up, k-points and weights (and for Al4 the spin start, the
+reference's spin Vxc and a spin mixing sequence), <name>_scf_ref.json its converged result;
+both are made by tests/golden/make_golden.py --only scf_kpt.
 Tolerances: free energy 1e-5 Ha/atom, Fermi level 1e-4 Ha, occupied eigenvalues of every
 k-point 1e-5 Ha (the SCF's parity bars), electron count 1e-8."""
 import numpy as np
@@ -80,3 +82,66 @@ def test_scf_kpt_rejects_bad_input(gpu_available):
     prm.graded_tail = 0
     with pytest.raises(sg.SgpuError):  # no k-point geometry installed
         ctx3.scf_kpt(prm, d["kpts"], d["kpt_wts"], d["b"], d["rho0"], d["rho_core"])
+
+
+def test_lsda_matches_reference(gpu_available):
+    d, grid, nl, ref = load_scf("Al4_spin_kpt")
+    ctx = make_kctx(d, grid, nl)
+    rho3 = d["rho3_0"]
+    vxc = np.zeros((2, ctx.Nd))
+    exc = np.zeros(ctx.Nd)
+    ctx.Calculate_Vxc_LSDA_PW(rho3[1], rho3[2], d["rho_core"], ref["params"]["xc_rhotol"], vxc,
+                              exc)
+    assert np.abs(vxc - d["vxc0_spin"]).max() <= 1e-12 * np.abs(d["vxc0_spin"]).max()
+    assert np.abs(exc - d["exc0_spin"]).max() <= 1e-12 * np.abs(d["exc0_spin"]).max()
+
+
+def test_spin_mixing_matches_reference(gpu_available):
+    """Device [rho, magz] mixing against the reference's Mixing_periodic_pulay over nine
+    iterations (past the history of seven)."""
+    d, grid, nl, ref = load_scf("Al4_spin_kpt")
+    p = ref["params"]
+    ctx = make_kctx(d, grid, nl)
+    ctx.Mixing_init_spin(d["rho3_0"][0], d["mag0"], -float(d["Nelectron"]),
+                         history=int(p["MixingHistory"]), mixing_parameter=p["MixingParameter"],
+                         mixing_parameter_simple=p["MixingParameterSimple"],
+                         mixing_parameter_mag=p["MixingParameterMag"],
+                         mixing_parameter_simple_mag=p["MixingParameterSimpleMag"],
+                         kerker=int(p["MixingPrecond"] == 1), kTF=p["precond_kerker_kTF"],
+                         idiemac=p["precond_kerker_thresh"], tol_precond=p["TOL_PRECOND"])
+    for it, (g, gm) in enumerate(zip(d["mix_outputs"], d["mix_mag_outputs"])):
+        r, m = ctx.Mixing_periodic_pulay_spin(it, g.copy(), gm.copy())
+        assert np.abs(r - d["mix_rho"][it]).max() <= 1e-10 * np.abs(d["mix_rho"][it]).max(), it
+        assert np.abs(m - d["mix_mag"][it]).max() <= 1e-10 * np.abs(d["mix_mag"][it]).max(), it
+    with pytest.raises(sg.SgpuError):  # the unpolarised entry point refuses a spin history
+        ctx.Mixing_periodic_pulay(9, d["mix_outputs"][0].copy())
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_spin_scf_kpt_matches_reference_program(gpu_available, precision):
+    """Collinear-spin k-point SCF (Al4, 4 k-points x 2 spins = 8 blocks) against the
+    reference program: free energy, Fermi level, occupied eigenvalues of every (spin, k)
+    block, net magnetization."""
+    d, grid, nl, ref = load_scf("Al4_spin_kpt")
+    p = ref["params"]
+    ctx = make_kctx(d, grid, nl)
+    prm = scf_params(sg, d, ref, precision=precision, switch=1e-4)
+    prm.mixing_param_mag = p["MixingParameterMag"]
+    prm.mixing_param_simple_mag = p["MixingParameterSimpleMag"]
+    fields = {}
+    res, rho, lam, occ = ctx.scf_kpt(prm, d["kpts"], d["kpt_wts"], d["b"], d["rho3_0"][0],
+                                     d["rho_core"], fields=fields, mag_init=d["mag0"])
+    n_atom = int(d["n_atom"])
+    nk, Ns = d["kpts"].shape[0], int(d["Nstates"])
+    assert res["converged"] == 1
+    assert abs(res["Etot"] / n_atom - ref["Etot_per_atom"]) < 1e-5
+    assert abs(res["Efermi"] - ref["Efermi"]) < 1e-4
+    lam_ref = np.array(ref["lambda"]).reshape(2 * nk, Ns)
+    occ_ref = np.array(ref["occ"]).reshape(2 * nk, Ns)   # printed as occ / 2 with spin
+    occupied = occ_ref > 1e-3
+    assert np.abs(lam[occupied] - lam_ref[occupied]).max() < 1e-5
+    assert np.abs(0.5 * occ - occ_ref).max() < 2e-3
+    assert abs(res["net_mag"] - ref["net_mag"]) < 1e-3
+    assert abs(fields["mag"].sum() * grid["dV"] - ref["net_mag"]) < 1e-3
+    assert abs(rho.sum() * grid["dV"] - float(d["Nelectron"])) < 1e-8
+    assert abs(res["scf_iters"] - ref["scf_iters"]) <= (1 if precision == 64 else 2)
