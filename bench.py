@@ -73,6 +73,11 @@ def parse():
                          "fp32_eager, fp32_bf16_split, fp64)")
     ap.add_argument("--fp64-only", action="store_true",
                     help="only the FP64 filter steps, no tuning or side blocks (profiling)")
+    ap.add_argument("--c3-prec", type=int, default=0, choices=[0, 32, 64],
+                    help="C3 block: only this precision (0: both)")
+    ap.add_argument("--c3-filter-only", action="store_true",
+                    help="C3 block: the batched filter timing only (no CheFSI pass, no per-block "
+                         "calls)")
     ap.add_argument("--c3-only", action="store_true",
                     help="print only the batched k-point/spin block (profiling)")
     ap.add_argument("--stencil-variant", type=int, default=None,
@@ -372,7 +377,49 @@ def al32_system():
     return 2 * a, pos + rng.normal(0.0, 0.05, size=pos.shape)
 
 
-def batched_c3_block(sg, torch, dev, device=0, steps=3):
+# the 10 points of a Gamma-centred 4x4x4 grid that are distinct under the cubic group, in
+# units of (2 pi / L) / 4, with their multiplicities (sum 64)
+C3_KRED = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (1, 1, 0), (2, 1, 0), (2, 2, 0), (1, 1, 1),
+           (2, 1, 1), (2, 2, 1), (2, 2, 2)]
+C3_KWTS = [1, 6, 3, 12, 12, 3, 8, 12, 6, 1]
+
+
+def scf_c3_block(sg, device=0):
+    """Spin-polarised k-point SCF of the C3 system: Al32 (34^3 grid), the 10 weighted
+    k-points, collinear spin from seeded +-0.2 moments, 64 states per (k, spin) block (20
+    blocks), degree 18, from the library's own set-up. Plain complex128 against the
+    complex64-first mixed mode (complex128 below an SCF error of 1e-4); wall time to TOL_SCF
+    and the difference of the two energies. (The SCF machinery is pinned to the reference
+    program on the Al4 spin k-point run; the reference has no cubic-symmetry k-reduction, so
+    this 10-point set has no reference run.)"""
+    golden = os.path.join(ROOT, "tests", "golden")
+    from sparc_gb300.psp8 import load_tables
+    from sparc_gb300.setup import CellSystem
+    L, pos = al32_system()
+    cs = CellSystem((L, L, L), (34, 34, 34), [("Al", pos)],
+                    {"Al": load_tables(os.path.join(golden, "psp_Al.npz"))}, device=device)
+    spins = np.random.default_rng(20261206).choice([-0.2, 0.2], size=len(pos))
+    kpts = np.array([[2 * np.pi / L * q / 4 for q in kk] for kk in C3_KRED])
+    wts = np.array(C3_KWTS, dtype=np.float64)
+    out = {"system": "Al32, 34^3, 10 k (cubic-reduced 4x4x4) x 2 spins, 64 states, degree 18, "
+                     "smearing 0.003 Ha, TOL_SCF 1e-6", "net_moment_start": float(spins.sum())}
+    for tag, prec in (("complex128", sg.SGPU_PREC_FP64), ("complex64_first", sg.SGPU_PREC_FP32)):
+        prm = cs.scf_params(Nstates=64, cheb_degree=18, smearing=0.003, precision=prec,
+                            fp64_switch_error=1e-4)
+        res, rho, lam, occ = cs.scf_kpt(prm, kpts, wts, atom_spin_z=spins)
+        out[tag] = {"time_s": round(res["time_s"], 3), "scf_iters": res["scf_iters"],
+                    "converged": res["converged"], "Etot_per_atom": res["Etot"] / cs.n_atom,
+                    "net_mag": round(res["net_mag"], 6),
+                    "filter_rr_s": round(res["filter_ms"] / 1e3, 3),
+                    "switch_iter": res["fp64_switch_iter"]}
+    out["dE_per_atom_mixed_vs_complex128"] = abs(out["complex64_first"]["Etot_per_atom"] -
+                                                 out["complex128"]["Etot_per_atom"])
+    out["speedup_mixed"] = round(out["complex128"]["time_s"] / out["complex64_first"]["time_s"], 3)
+    cs.close()
+    return out
+
+
+def batched_c3_block(sg, torch, dev, device=0, steps=3, prec_only=0, filter_only=False):
     """Batched complex filter and CheFSI pass over (k-point, spin) blocks: 32-atom Al, 34^3
     grid (h = 0.45),
     the 10 symmetry-distinct points of a 4x4x4 k-grid times 2 spins = 20 blocks of 64 states,
@@ -398,8 +445,7 @@ def batched_c3_block(sg, torch, dev, device=0, steps=3):
     ctx.Calculate_Vxc_LDA_PW(f["rho_at"], f["rho_core"], 1e-14, vxc, exc)
     v0 = phi + vxc
     ctx.set_veff(np.concatenate([v0 + 0.02, v0 - 0.02]), nspin=2)
-    kred = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (1, 1, 0), (2, 1, 0), (2, 2, 0), (1, 1, 1),
-            (2, 1, 1), (2, 2, 1), (2, 2, 2)]  # in units of (2 pi / L) / 4
+    kred = C3_KRED
     ncol, m = 64, 18
     a0, a, b = -0.6, 0.35, 45.0
     gen = torch.Generator(device=dev)
@@ -408,6 +454,8 @@ def batched_c3_block(sg, torch, dev, device=0, steps=3):
                      "of 64 states, degree 18", "blocks": 20}
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     for name, prec, cdt in (("complex128", 64, torch.complex128), ("complex64", 32, torch.complex64)):
+        if prec_only and prec != prec_only:
+            continue
         blocks = []
         for kk in kred:
             for spin in (0, 1):
@@ -437,8 +485,19 @@ def batched_c3_block(sg, torch, dev, device=0, steps=3):
 
         lam_last = [None]
         res = {}
-        runs = [("batched_graph", batched), ("chefsi_pass", chefsi)] + \
-            ([("per_block_calls", per_block)] if prec == 64 else [])
+        def batched_one_point():  # complex64 with the one-point-per-thread stencil
+            ctx.set_zstencil_pairs(False)
+            try:
+                batched()
+            finally:
+                ctx.set_zstencil_pairs(True)
+
+        runs = [("batched_graph", batched)]
+        if prec == 32:
+            runs.append(("batched_graph_one_point_stencil", batched_one_point))
+        if not filter_only:
+            runs += [("chefsi_pass", chefsi)] + \
+                ([("per_block_calls", per_block)] if prec == 64 else [])
         for tag, fn in runs:
             fn()
             torch.cuda.synchronize()
@@ -598,8 +657,11 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if args.c3_only:
-        print(json.dumps({"batched_c3": batched_c3_block(sg, torch, dev, device=local,
-                                                         steps=args.steps)}), flush=True)
+        c3 = batched_c3_block(sg, torch, dev, device=local, steps=args.steps,
+                              prec_only=args.c3_prec, filter_only=args.c3_filter_only)
+        if not args.no_scf:
+            c3["scf"] = scf_c3_block(sg, device=local)
+        print(json.dumps({"batched_c3": c3}), flush=True)
         return
     if args.rr_gemm:
         only = args.rr_only.split(",") if args.rr_only else None
@@ -866,6 +928,8 @@ def main():
     c3 = None
     if rank == 0 and not args.no_c3:
         c3 = batched_c3_block(sg, torch, dev, device=local)
+        if not args.no_scf:
+            c3["scf"] = scf_c3_block(sg, device=local)
 
     if rank == 0:
         tune = {"stencil_variant": {"chosen": kernel_name,

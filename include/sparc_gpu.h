@@ -373,6 +373,16 @@ int sgpu_Generate_PseudoChargeDensity(sgpu_ctx *ctx, const double *cell, const i
                                       double *b_ref, double *rho_at, double *rho_core,
                                       double *scalars);
 
+/* Initial magnetization density of a collinear-spin run (spin_typ 1): the atoms' isolated-
+ * atom densities weighted by atom_spin_z[atom] / Znucl (n_atom values, type-major as
+ * atom_pos), accumulated over the same atom images as rho_at and not rescaled; atoms and
+ * cutoff as for sgpu_Generate_PseudoChargeDensity. mag_at (Nd) is overwritten. Replaces the
+ * magz part of Generate_PseudoChargeDensity (src/electrostatics.c:1031-1034), which
+ * Init_electronDensity copies into mag (src/orbitalElecDensInit.c:149-151). */
+int sgpu_Generate_InitialMagnetization(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                                       const double *atom_pos, const double *cutoff,
+                                       const double *atom_spin_z, double *mag_at);
+
 /* Build the nonlocal projectors of the atoms on the device (spline of UdV times real
  * spherical harmonics over the grid points of each image's rc-sphere) and install them as
  * sgpu_set_nonlocal would, together with the image coordinates for the k-point calls.
@@ -609,6 +619,12 @@ int sgpu_set_gemm_emulation(sgpu_ctx *ctx, int mode);
  * The Gram products compute the upper triangle and mirror it. No counterpart in the
  * reference (which calls cblas_dgemm). */
 int sgpu_set_rr_products(sgpu_ctx *ctx, int mode);
+
+/* complex64 stencil form: 1 (default) two x-neighbouring points per thread with packed reads
+ * and a per-k table of Bloch factors (used where Nx and the leading dimensions are even and
+ * the blocks 16-byte aligned); 0 the one-point-per-thread kernel. Both compute the same
+ * operation sequence per point up to the rounding of the Bloch factors. */
+int sgpu_set_zstencil_pairs(sgpu_ctx *ctx, int on);
 
 /* How sgpu_Solve_Generalized_EigenProblem and the SCF solve Hp q = lambda Mp q
  * (DP_Solve_Generalized_EigenProblem, src/eigenSolver.c:1262; LAPACKE_dsygvd at :1318):

@@ -29,6 +29,7 @@ EXPORTED = [
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
     "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_scf_kpt", "sgpu_Vnl_vec_mult_noalloc",
     "sgpu_Calculate_Vxc_LSDA_PW", "sgpu_Mixing_init_spin", "sgpu_Mixing_periodic_pulay_spin",
+    "sgpu_Generate_InitialMagnetization", "sgpu_set_zstencil_pairs",
     "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
     "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
     "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
@@ -244,6 +245,18 @@ class Context:
             int(net_charge), _ptr(b), _ptr(bref), _ptr(rho), _ptr(core), _ptr(sc)))
         return dict(b=b, b_ref=bref, rho_at=rho, rho_core=core, Esc=float(sc[0]),
                     PosCharge=float(sc[1]), NegCharge=float(sc[2]))
+
+    def Generate_InitialMagnetization(self, cell, nAtomv, atom_pos, atom_spin_z, cutoff=None):
+        """Initial magnetization density (Nd) of a collinear-spin run from per-atom spins."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        nat = np.ascontiguousarray(nAtomv, dtype=np.int32)
+        pos = np.ascontiguousarray(atom_pos, dtype=np.float64).reshape(-1)
+        sp = np.ascontiguousarray(atom_spin_z, dtype=np.float64).reshape(-1)
+        cut = None if cutoff is None else np.ascontiguousarray(cutoff, dtype=np.float64)
+        mag = np.zeros(self.Nd)
+        _check(lib().sgpu_Generate_InitialMagnetization(self._h, _ptr(cell), _ptr(nat), _ptr(pos),
+                                                        _ptr(cut), _ptr(sp), _ptr(mag)))
+        return mag
 
     def CalculateNonlocalProjectors(self, cell, nAtomv, atom_pos):
         cell = np.ascontiguousarray(cell, dtype=np.float64)
@@ -678,6 +691,9 @@ class Context:
 
     def set_stencil_variant(self, variant):
         _check(lib().sgpu_set_stencil_variant(self._h, int(variant)))
+
+    def set_zstencil_pairs(self, on):
+        _check(lib().sgpu_set_zstencil_pairs(self._h, int(bool(on))))
 
     def set_nonlocal_apply_variant(self, variant):
         _check(lib().sgpu_set_nonlocal_apply_variant(self._h, int(variant)))

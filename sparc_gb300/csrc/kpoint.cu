@@ -20,6 +20,7 @@
 
 #include "sgpu_internal.h"
 #include "zmath.cuh"
+#include "zstencil_c64.cuh"
 
 namespace sgpu {
 namespace {
@@ -174,6 +175,51 @@ __device__ __forceinline__ void stencil_z_body(const StencilZParams<CT> &p, int 
 #pragma unroll
         for (int m = 0; m <= 2 * R; m++) q[m] = q[m + 1];
     }
+}
+
+constexpr int kPairMaxThreads = 320;
+
+template <int R>
+__global__ void __launch_bounds__(kPairMaxThreads)
+    k_stencil_z_c64(const __grid_constant__ ZPairConst g, const ZPairParams p)
+{
+    stencil_c64_pairs<R>(g, p, blockIdx.z / g.nslab, blockIdx.z % g.nslab);
+}
+
+// Tile of the pair kernel: BX (even, points) with the least padding of Nx, then BY with
+// the least padding of Ny among the heights that keep the block within kPairMaxThreads.
+static void zpair_tile(int Nx, int Ny, int R, int *bx2, int *by)
+{
+    int best = 1 << 30;
+    *bx2 = 16;
+    for (int t = std::min(32, std::max(4, (Nx + 1) / 2)); t >= 4; t--) {
+        const int waste = (Nx + 2 * t - 1) / (2 * t) * (2 * t) - Nx;
+        if (waste < best) { best = waste; *bx2 = t; }
+    }
+    best = 1 << 30;
+    *by = R;
+    for (int t = std::max(R, kPairMaxThreads / *bx2); t >= R; t--) {
+        if (*bx2 * t > kPairMaxThreads) continue;
+        const int waste = (Ny + t - 1) / t * t - Ny;
+        if (waste < best) { best = waste; *by = t; }
+    }
+}
+
+// The pair kernel applies when every fetch is within one period of the cell and the pairs are
+// 16-byte aligned.
+static bool zpair_ok(int Nx, int Ny, int Nz, int R, int bx2, int by)
+{
+    const int BX = 2 * bx2;
+    const int tx = (Nx + BX - 1) / BX, ty = (Ny + by - 1) / by;
+    const ZRing z = zring_shape(bx2, by, R, kPairAhead);
+    return Nx % 2 == 0 && R % 2 == 0 && R < Nx && R < Ny && R < Nz &&
+           tx * BX + R <= 2 * Nx && ty * by + R <= 2 * Ny &&
+           z.ncopy <= kPairCopies * bx2 * by && z.bytes <= 200 * 1024;
+}
+
+static size_t zpair_smem(int bx2, int by, int R)
+{
+    return zring_shape(bx2, by, R, kPairAhead).bytes;
 }
 
 // Threads per block of the complex stencil: complex128 (FP64-pipe bound, more registers per
@@ -424,6 +470,7 @@ struct BBlock {
     CT *alpha;              // ntot x ncol projection coefficients (lda = ncol)
     const double2 *phase;   // e^{i theta_g} per image for this block's k
     double kL[3];           // k_d * L_d
+    double2 bf[9];          // e^{i d k_a L_a}, index 3 a + d + 1 (a = x, y, z; d = -1, 0, 1)
     int ncol, spin;
 };
 
@@ -464,6 +511,28 @@ __global__ void __launch_bounds__(zstencil_threads<CT>())
     stencil_z_body<CT, R>(p, bc.y, slab);
 }
 
+template <int R>
+__global__ void __launch_bounds__(kPairMaxThreads)
+    k_stencil_zb_c64(const BBlock<float2> *__restrict__ blocks, const BCoef *__restrict__ coef,
+                     const int2 *__restrict__ work, const __grid_constant__ ZPairConst g,
+                     const float *__restrict__ veff32, long Nd, int m, int deg, int in_sel,
+                     int out_sel, int z_sel)
+{
+    const int w = blockIdx.z / g.nslab, slab = blockIdx.z % g.nslab;
+    const int2 bc = work[w];
+    const BBlock<float2> &B = blocks[bc.x];
+    const BCoef cf = coef[(long)bc.x * m + deg];
+    ZPairParams p;
+    p.x = B.buf[in_sel]; p.ldx = B.ld[in_sel];
+    p.out = B.buf[out_sel]; p.ldo = B.ld[out_sel];
+    p.z = z_sel >= 0 ? B.buf[z_sel] : nullptr; p.ldz = z_sel >= 0 ? B.ld[z_sel] : 0;
+    p.v32 = veff32 + (long)B.spin * Nd;
+    p.c0 = (float)cf.c0; p.s1 = (float)cf.s1; p.s2 = (float)cf.s2;
+#pragma unroll
+    for (int i = 0; i < 9; i++) p.bf[i] = make_float2((float)B.bf[i].x, (float)B.bf[i].y);
+    stencil_c64_pairs<R>(g, p, bc.y, slab);
+}
+
 // grid (image, column group); cg[y] = (block, first column)
 template <typename CT, int MAXJ>
 __global__ void __launch_bounds__(256)
@@ -479,6 +548,75 @@ __global__ void __launch_bounds__(256)
     nl_project_z_body<CT, MAXJ>(img_atom, img_ndc, img_off, img_chi_off, grid_pos, chi,
                                 ip_displ, gamma, B.phase, B.ncol, B.buf[in_sel], B.ld[in_sel],
                                 B.alpha, B.ncol, dV, blockIdx.x, bc.y);
+}
+
+// complex64 projection: block = (image g, group of kProjCols columns of one block), eight warps
+// of four columns each. Lane = 8 c + p: column c of the warp, point phase p, so one load
+// instruction reads eight consecutive points of four columns (coalesced) and one Chi row
+// segment of eight points serves all four columns. Each lane accumulates every projector;
+// three shuffle steps sum the eight point phases (every lane ends with the totals) and lane p
+// adds projectors p, p+8, p+16: alpha[row, n] += e^{i theta_g} dV Gamma_row sum (atomic across
+// the images of one atom).
+template <int MAXJ>
+__global__ void __launch_bounds__(256)
+    k_nl_project_zb_c64(const BBlock<float2> *__restrict__ blocks, const int2 *__restrict__ cg,
+                        int in_sel, const int *__restrict__ img_atom,
+                        const int *__restrict__ img_ndc, const long *__restrict__ img_off,
+                        const long *__restrict__ img_chi_off, const int *__restrict__ grid_pos,
+                        const float *__restrict__ chi, const int *__restrict__ ip_displ,
+                        const double *__restrict__ gamma, double dV)
+{
+    const int g = blockIdx.x;
+    const int2 bc = cg[blockIdx.y];
+    const BBlock<float2> &B = blocks[bc.x];
+    const int a = img_atom[g];
+    const int np = ip_displ[a + 1] - ip_displ[a];
+    const int ndc = img_ndc[g];
+    const int *__restrict__ gp = grid_pos + img_off[g];
+    const float *__restrict__ ch = chi + img_chi_off[g];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int p = lane & 7, c = lane >> 3;
+    const int n = bc.y + wid * 4 + c;
+    const bool on = n < B.ncol;
+    const float2 *__restrict__ xc = B.buf[in_sel] + (long)(on ? n : bc.y) * B.ld[in_sel];
+    float2 acc[MAXJ];
+#pragma unroll
+    for (int jj = 0; jj < MAXJ; jj++) acc[jj] = make_float2(0.f, 0.f);
+#pragma unroll 2
+    for (int ii = p; ii < ndc; ii += 8) {
+        const float2 xv = on ? __ldg(xc + __ldg(gp + ii)) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int jj = 0; jj < MAXJ; jj++) {
+            if (jj < np) {
+                const float cv = __ldg(ch + (long)jj * ndc + ii);
+                acc[jj].x = fmaf(cv, xv.x, acc[jj].x);
+                acc[jj].y = fmaf(cv, xv.y, acc[jj].y);
+            }
+        }
+    }
+#pragma unroll
+    for (int jj = 0; jj < MAXJ; jj++) {
+        if (jj < np) {
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) {
+                acc[jj].x += __shfl_xor_sync(0xffffffffu, acc[jj].x, o);
+                acc[jj].y += __shfl_xor_sync(0xffffffffu, acc[jj].y, o);
+            }
+        }
+    }
+    if (!on) return;
+    const double2 ph = B.phase[g];
+#pragma unroll
+    for (int jj = 0; jj < MAXJ; jj++) {
+        if (jj < np && (jj & 7) == p) {
+            const int row = ip_displ[a] + jj;
+            const double f = dV * gamma[row];
+            const double sr = acc[jj].x, si = acc[jj].y;
+            float *dst = reinterpret_cast<float *>(B.alpha + (long)row * B.ncol + n);
+            atomicAdd(dst, (float)(f * (ph.x * sr - ph.y * si)));
+            atomicAdd(dst + 1, (float)(f * (ph.x * si + ph.y * sr)));
+        }
+    }
 }
 
 // staged, grouped: grid (chunk, column block, block); blocks with fewer columns return early
@@ -614,6 +752,56 @@ static int stencil_z(sgpu_ctx *ctx, const double *k, int ncol, double a, double 
     p.k.kLx = k[0] * ks->L[0];
     p.k.kLy = k[1] * ks->L[1];
     p.k.kLz = k[2] * ks->L[2];
+    if constexpr (sizeof(CT) == 8) {  // complex64: the pair kernel where it applies
+        int PX2, PY;
+        zpair_tile(ctx->Nx, ctx->Ny, R, &PX2, &PY);
+        bool ok = ctx->zpair_on && zpair_ok(ctx->Nx, ctx->Ny, ctx->Nz, R, PX2, PY) &&
+                  ldx % 2 == 0 && ldo % 2 == 0 && (!p.z || ldz % 2 == 0) &&
+                  (uintptr_t)x % 16 == 0 && (uintptr_t)out % 16 == 0 &&
+                  (!p.z || (uintptr_t)z % 16 == 0) && (!p.v32 || ctx->Nd % 2 == 0);
+        if (ok) {
+            ZPairParams zp;
+            ZPairConst zg;
+            zp.x = x; zp.out = out; zp.z = p.z; zp.v32 = p.v32;
+            zp.ldx = ldx; zp.ldo = ldo; zp.ldz = ldz;
+            zg.Nx = ctx->Nx; zg.Ny = ctx->Ny; zg.Nz = ctx->Nz;
+            for (int r = 0; r <= R; r++) {
+                zg.wx[r] = (float)p.wx[r]; zg.wy[r] = (float)p.wy[r]; zg.wz[r] = (float)p.wz[r];
+            }
+            // the potential scale bv multiplies the FP32 potential as in the generic kernel
+            zp.c0 = (float)p.c0; zp.s1 = (float)p.s1; zp.s2 = (float)p.s2;
+            const double kL[3] = {p.k.kLx, p.k.kLy, p.k.kLz};
+            for (int a = 0; a < 3; a++)
+                for (int d = -1; d <= 1; d++)
+                    zp.bf[3 * a + d + 1] = make_float2((float)std::cos(d * kL[a]),
+                                                       (float)std::sin(d * kL[a]));
+            if (p.v32 && bv != 1.0) ok = false;  // the pair kernel takes bv = 1
+            if (ok) {
+                const size_t psm = zpair_smem(PX2, PY, R);
+                SGPU_CUDA_TRY(cudaFuncSetAttribute(k_stencil_z_c64<R>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)psm));
+                const int ptx = (ctx->Nx + 2 * PX2 - 1) / (2 * PX2), pty = (ctx->Ny + PY - 1) / PY;
+                int nslab = 1;
+                while ((long)ptx * pty * ncol * nslab < 152L * 8 && ctx->Nz / (nslab * 2) >= 8)
+                    nslab *= 2;
+                zg.zlen = (ctx->Nz + nslab - 1) / nslab;
+                zg.nslab = nslab;
+                const int maxz = 65535 / nslab;
+                for (int c0i = 0; c0i < ncol; c0i += maxz) {
+                    const int nc = std::min(maxz, ncol - c0i);
+                    ZPairParams q = zp;
+                    q.x = x + (long)c0i * ldx;
+                    q.out = out + (long)c0i * ldo;
+                    if (q.z) q.z = zp.z + (long)c0i * ldz;
+                    ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
+                    k_stencil_z_c64<R><<<dim3(ptx, pty, nc * nslab), dim3(PX2, PY), psm, st>>>(zg, q);
+                }
+                SGPU_CUDA_TRY(cudaGetLastError());
+                return SGPU_OK;
+            }
+        }
+    }
     int BX, BY;
     zstencil_tile(ctx->Nx, ctx->Ny, R, zstencil_threads<CT>(), &BX, &BY);
     const size_t zsm = zstencil_smem<CT>(BX, BY, R);
@@ -808,6 +996,9 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
         B.alpha = has_nl ? alpha + (size_t)nl.ntot * coloff[b] : nullptr;
         B.phase = nullptr;  // set after the table is placed
         for (int d = 0; d < 3; d++) B.kL[d] = f.k[d] * ks->L[d];
+        for (int a = 0; a < 3; a++)
+            for (int d = -1; d <= 1; d++)
+                B.bf[3 * a + d + 1] = make_double2(std::cos(d * B.kL[a]), std::sin(d * B.kL[a]));
         B.ncol = f.ncol;
         B.spin = f.spin;
         // recurrence scalars of ChebyshevFiltering_kpt (src/eigenSolverKpt.c:458-550)
@@ -887,15 +1078,39 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
     cs.veff32 = ctx->veff32;
     int BX, BY;
     zstencil_tile(ctx->Nx, ctx->Ny, R, zstencil_threads<CT>(), &BX, &BY);
-    const size_t zsm = zstencil_smem<CT>(BX, BY, R);  // attribute set before any capture
+    size_t zsm = zstencil_smem<CT>(BX, BY, R);  // attribute set before any capture
     SGPU_CUDA_TRY(cudaFuncSetAttribute(k_stencil_zb<CT, R>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsm));
+    // complex64: the pair kernel when its alignment and one-period conditions hold
+    bool pairs = false;
+    int PX2 = 0, PY = 0;
+    if constexpr (sizeof(CT) == 8) {
+        zpair_tile(ctx->Nx, ctx->Ny, R, &PX2, &PY);
+        pairs = ctx->zpair_on && zpair_ok(ctx->Nx, ctx->Ny, ctx->Nz, R, PX2, PY) &&
+                (uintptr_t)W % 16 == 0 && Nd % 2 == 0;
+        for (int b = 0; b < nblk && pairs; b++)
+            pairs = blk[b].ldi % 2 == 0 && blk[b].ldo % 2 == 0 &&
+                    (uintptr_t)blk[b].X % 16 == 0 && (uintptr_t)blk[b].Y % 16 == 0;
+        if (pairs) {
+            BX = 2 * PX2;
+            BY = PY;
+            zsm = zpair_smem(PX2, PY, R);
+            SGPU_CUDA_TRY(cudaFuncSetAttribute(k_stencil_zb_c64<R>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)zsm));
+        }
+    }
     const int tilesx = (ctx->Nx + BX - 1) / BX, tilesy = (ctx->Ny + BY - 1) / BY;
     int nslab = 1;
     while ((long)tilesx * tilesy * totcols * nslab < 152L * 8 && ctx->Nz / (nslab * 2) >= 8)
         nslab *= 2;
     cs.nslab = nslab;
     cs.zlen = (ctx->Nz + nslab - 1) / nslab;
+    ZPairConst pg;  // launch-wide data of the complex64 pair kernel
+    for (int r = 0; r <= R; r++) {
+        pg.wx[r] = (float)cs.wx[r]; pg.wy[r] = (float)cs.wy[r]; pg.wz[r] = (float)cs.wz[r];
+    }
+    pg.Nx = cs.Nx; pg.Ny = cs.Ny; pg.Nz = cs.Nz; pg.nslab = cs.nslab; pg.zlen = cs.zlen;
     const long maxw = 65535 / nslab;
     const size_t abytes = has_nl ? sizeof(CT) * (size_t)nl.ntot * totcols : 0;
     int maxcol = 0;
@@ -930,7 +1145,17 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
                 SGPU_CUDA_TRY(cudaMemsetAsync(alpha, 0, abytes, st));
                 ProfScope ps(ctx, SGPU_KERNEL_NL_PROJECT, st);
                 const dim3 pg(nl.nimg, (unsigned)hg.size());
-                if (nl.max_np <= 9)
+                if constexpr (sizeof(CT) == 8) {  // complex64: warp-per-column form
+                    const auto *dB32 = reinterpret_cast<const BBlock<float2> *>(dB);
+                    if (nl.max_np <= 9)
+                        k_nl_project_zb_c64<9><<<pg, 256, 0, st>>>(dB32, dG, in, nl.img_atom,
+                            nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, nl.chi32,
+                            nl.ip_displ, nl.gamma64, ctx->dV);
+                    else
+                        k_nl_project_zb_c64<18><<<pg, 256, 0, st>>>(dB32, dG, in, nl.img_atom,
+                            nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, nl.chi32,
+                            nl.ip_displ, nl.gamma64, ctx->dV);
+                } else if (nl.max_np <= 9)
                     k_nl_project_zb<CT, 9><<<pg, 256, 0, st>>>(dB, dG, in, nl.img_atom,
                         nl.img_ndc, nl.img_off, nl.img_chi_off, nl.grid_pos, nl.chi64,
                         nl.ip_displ, nl.gamma64, ctx->dV);
@@ -943,6 +1168,16 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
             for (long w0 = 0; w0 < totcols; w0 += maxw) {
                 const long nw = std::min(maxw, totcols - w0);
                 ProfScope ps(ctx, SGPU_KERNEL_STENCIL, st);
+                if constexpr (sizeof(CT) == 8) {
+                    if (pairs) {
+                        k_stencil_zb_c64<R><<<dim3(tilesx, tilesy, (unsigned)(nw * nslab)),
+                                              dim3(PX2, PY), zsm, st>>>(
+                            reinterpret_cast<const BBlock<float2> *>(dB), dC, dW + w0, pg,
+                            ctx->veff32, Nd, m, j, in, out, zsel);
+                        ctx->launches++;
+                        continue;
+                    }
+                }
                 k_stencil_zb<CT, R><<<dim3(tilesx, tilesy, (unsigned)(nw * nslab)),
                                       dim3(BX, BY), zsm, st>>>(dB, dC, dW + w0, cs, j, in, out,
                                                                zsel);
@@ -988,7 +1223,7 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
 
     if (ctx->prof_on) return issue();  // per-launch events need plain launches
     std::vector<long> key = {(long)sizeof(CT), nblk, m, (long)(uintptr_t)tb, (long)(uintptr_t)W,
-                             (long)(uintptr_t)alpha, (long)hg.size(), nslab,
+                             (long)(uintptr_t)alpha, (long)hg.size(), nslab, (long)pairs,
                              (long)(uintptr_t)ctx->veff64, (long)(uintptr_t)ctx->veff32};
     for (int b = 0; b < nblk; b++) {
         key.push_back(blk[b].ncol);

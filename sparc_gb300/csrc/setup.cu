@@ -249,6 +249,34 @@ __global__ void __launch_bounds__(256) k_pseudocharge(
     if (threadIdx.x == 0 && tot != 0.0) atomicAdd(esc_acc, tot);
 }
 
+// Initial magnetization of a collinear-spin run: each atom's isolated-atom density rho_J
+// (within its rb-box and rchrg, as k_pseudocharge accumulates rho_at) weighted by
+// w[atom] = spin_z / Znucl (src/electrostatics.c:1031-1034).
+__global__ void __launch_bounds__(256) k_mag_at(const PcImage *__restrict__ imgs, PsdDevSet P,
+                                                int FDn, int Nx, int Ny, double dx, double dy,
+                                                double dz, const double *__restrict__ w,
+                                                double *__restrict__ mag)
+{
+    const PcImage im = imgs[blockIdx.y];
+    const long npts = (long)im.nx * im.ny * im.nz;
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    const double wa = w[im.atom];
+    if (wa == 0.0) return;
+    const PsdDev &ps = P.t[im.type];
+    const int i = (int)(p % im.nx);
+    const int j = (int)((p / im.nx) % im.ny);
+    const int k = (int)(p / ((long)im.nx * im.ny));
+    const double xc = (i + FDn) * dx - (im.x0 - dx * (im.xs - FDn));
+    const double yc = (j + FDn) * dy - (im.y0 - dy * (im.ys - FDn));
+    const double zc = (k + FDn) * dz - (im.z0 - dz * (im.zs - FDn));
+    const double R0 = sqrt(xc * xc + yc * yc + zc * zc);
+    if (R0 > ps.rchrg) return;
+    const double rho = spline_at(ps.grid, ps.rhoiso, ps.yd_rhoiso, ps.size, ps.uniform, R0);
+    const long g = (long)(im.zs + k) * Nx * Ny + (long)(im.ys + j) * Nx + (im.xs + i);
+    atomicAdd(&mag[g], wa * rho);
+}
+
 struct D1Weights {
     double d[3 * (kMaxFDn + 1)];  // first-derivative weights per offset and direction (x, y, z)
 };
@@ -935,6 +963,67 @@ int sgpu_Generate_PseudoChargeDensity(sgpu_ctx *ctx, const double *cell, const i
     cudaFreeAsync(buf, st);
     if (cudaStreamSynchronize(st) != cudaSuccess && rc == SGPU_OK) {
         set_error("sgpu_Generate_PseudoChargeDensity: CUDA error");
+        rc = SGPU_ERR_CUDA;
+    }
+    return rc;
+}
+
+int sgpu_Generate_InitialMagnetization(sgpu_ctx *ctx, const double *cell, const int *nAtomv,
+                                       const double *atom_pos, const double *cutoff,
+                                       const double *atom_spin_z, double *mag_at)
+{
+    if (!ctx || !cell || !nAtomv || !atom_pos || !atom_spin_z || !mag_at) {
+        set_error("sgpu_Generate_InitialMagnetization: bad arguments");
+        return SGPU_ERR_ARG;
+    }
+    SetupState *s;
+    SGPU_TRY(get_setup(ctx, &s));
+    SGPU_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    double h[3];
+    grid_spacing(ctx, cell, h);
+    std::vector<PcImage> imgs;
+    long maxpts = 0;
+    SGPU_TRY(pc_images(ctx, *s, cell, h, nAtomv, atom_pos, cutoff,
+                       "sgpu_Generate_InitialMagnetization", imgs, &maxpts));
+    int n_atom = 0;
+    for (size_t t = 0; t < s->types.size(); t++) n_atom += nAtomv[t];
+    std::vector<double> w(n_atom);
+    for (size_t t = 0, a = 0; t < s->types.size(); t++)
+        for (int i = 0; i < nAtomv[t]; i++, a++) w[a] = atom_spin_z[a] / (double)s->types[t].Znucl;
+    const long Nd = ctx->Nd;
+    double *buf = nullptr;
+    SGPU_CUDA_TRY(cudaMallocAsync(&buf, sizeof(double) * (Nd + n_atom + 1), st));
+    PcImage *dimg = nullptr;
+    int rc = SGPU_OK;
+    do {
+        if (cudaMemsetAsync(buf, 0, sizeof(double) * Nd, st) != cudaSuccess ||
+            cudaMemcpyAsync(buf + Nd, w.data(), sizeof(double) * n_atom, cudaMemcpyHostToDevice,
+                            st) != cudaSuccess) {
+            rc = SGPU_ERR_CUDA; break;
+        }
+        if (!imgs.empty()) {
+            if (cudaMallocAsync(&dimg, sizeof(PcImage) * imgs.size(), st) != cudaSuccess ||
+                cudaMemcpyAsync(dimg, imgs.data(), sizeof(PcImage) * imgs.size(),
+                                cudaMemcpyHostToDevice, st) != cudaSuccess) {
+                rc = SGPU_ERR_CUDA; break;
+            }
+            for (size_t i0 = 0; i0 < imgs.size(); i0 += 65535) {
+                const unsigned ny = (unsigned)std::min<size_t>(65535, imgs.size() - i0);
+                dim3 grid((unsigned)((maxpts + 255) / 256), ny);
+                ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+                k_mag_at<<<grid, 256, 0, st>>>(dimg + i0, device_views(*s), ctx->FDn, ctx->Nx,
+                                               ctx->Ny, h[0], h[1], h[2], buf + Nd, buf);
+            }
+            if (cudaGetLastError() != cudaSuccess) { rc = SGPU_ERR_CUDA; break; }
+        }
+        rc = deliver(buf, mag_at, Nd, st);
+    } while (0);
+    if (rc == SGPU_ERR_CUDA) set_error("sgpu_Generate_InitialMagnetization: CUDA error");
+    if (dimg) cudaFreeAsync(dimg, st);
+    cudaFreeAsync(buf, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == SGPU_OK) {
+        set_error("sgpu_Generate_InitialMagnetization: CUDA error");
         rc = SGPU_ERR_CUDA;
     }
     return rc;

@@ -174,6 +174,8 @@ struct sgpu_ctx {
                         // kernels (rr_tc.cu): 1 (default) for FP32 blocks (FP32-accurate) and
                         // the mixed SCF's FP64 phase (FP64-accurate), 2 also for plain FP64
                         // calls; 0 cuBLAS
+    int zpair_on = 1;   // complex64 stencil: the two-points-per-thread kernel (1) or the
+                        // one-point kernel (0) (sgpu_set_zstencil_pairs)
     double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
     double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings

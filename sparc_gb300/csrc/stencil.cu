@@ -18,6 +18,7 @@
 // prefetched into registers one plane ahead.
 #include "sgpu_internal.h"
 #include "mbarrier.cuh"
+#include "cpasync.cuh"
 
 namespace sgpu {
 namespace {
@@ -300,30 +301,6 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
 {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all()
-{
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
-
-// the same copies to a shared-space byte address
-__device__ __forceinline__ void cp_async4s(unsigned sa, const void *gmem)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8s(unsigned sa, const void *gmem)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async16s(unsigned sa, const void *gmem)  // L2 only
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group()
-{
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 template <bool VEC>

@@ -131,6 +131,23 @@ class CellSystem:
         return self.ctx.scf(params, f["b"], r0, f["rho_core"] if self.nlcc else None,
                             fields=fields)
 
+    def initial_magnetization(self, atom_spin_z):
+        """The reference's initial magnetization for per-atom spins (type-major, as the
+        atoms): sum over atoms of spin / Znucl times the isolated-atom density."""
+        return self.ctx.Generate_InitialMagnetization(self.L, self.nAtomv, self.atom_pos,
+                                                      atom_spin_z)
+
+    def scf_kpt(self, params, kpts, kpt_wts, atom_spin_z=None, rho_init=None, fields=None):
+        """k-point SCF (Context.scf_kpt) from the superposition of atomic densities (or
+        rho_init); with atom_spin_z, collinear spin from the reference's initial
+        magnetization of those moments."""
+        f = self.fields
+        r0 = f["rho_at"] if rho_init is None else rho_init
+        mag = None if atom_spin_z is None else self.initial_magnetization(atom_spin_z)
+        return self.ctx.scf_kpt(params, kpts, kpt_wts, f["b"], r0,
+                                f["rho_core"] if self.nlcc else None, fields=fields,
+                                mag_init=mag)
+
     def forces(self, fields, occ, occfac=2.0):
         """Atomic forces (n_atom, 3) in Ha/Bohr after an SCF that filled fields (psi, phi,
         vxc) and returned occ: local + nonlocal (+ core correction) with the mean removed, as

@@ -83,3 +83,35 @@ def test_batched_rejects_host_arrays_and_bad_spin(gpu_available):
     with pytest.raises(sg.SgpuError):
         ctx.ChebyshevFiltering_batched([dict(spin=3, k=(0, 0, 0), X=xd, Y=xd.clone(), a=0.5,
                                              b=40.0, a0=-1.0)], 4)
+
+
+def test_complex64_pair_stencil_matches_one_point_kernel(gpu_available):
+    """The complex64 stencil with two points per thread and tabulated Bloch factors against the
+    one-point kernel, single-block and batched (FP32 rounding of the factors only)."""
+    import torch
+    d, grid, nl = load_kpt()
+    ctx = make_ctx(d, grid, nl)
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev)
+    Nd = ctx.Nd
+    outs = {}
+    for on in (True, False):
+        ctx.set_zstencil_pairs(on)
+        gen.manual_seed(5)  # the same inputs for both forms
+        blocks = []
+        for b, k in enumerate(d["kpts"][:2]):
+            x = torch.complex(torch.rand((5, Nd), generator=gen, device=dev, dtype=torch.float32),
+                              torch.rand((5, Nd), generator=gen, device=dev, dtype=torch.float32))
+            blocks.append(dict(spin=0, k=list(k), X=x, Y=torch.empty_like(x), a=0.5, b=40.0,
+                               a0=-0.8))
+        ctx.ChebyshevFiltering_batched(blocks, 7, precision=sg.SGPU_PREC_FP32)
+        # the single-block call takes complex128 arrays and filters them in complex64
+        rng = np.random.default_rng(6)
+        xs = rng.uniform(-1, 1, (3, Nd)) + 1j * rng.uniform(-1, 1, (3, Nd))
+        ys = np.zeros_like(xs)
+        ctx.ChebyshevFiltering_kpt(d["kpts"][1], xs, ys, 7, 0.5, 40.0, -0.8,
+                                   precision=sg.SGPU_PREC_FP32)
+        outs[on] = [bl["Y"].cpu().numpy() for bl in blocks] + [ys]
+    ctx.set_zstencil_pairs(True)
+    for a, b in zip(outs[True], outs[False]):
+        assert rel_err(a, b) < 2e-6

@@ -145,3 +145,37 @@ def test_spin_scf_kpt_matches_reference_program(gpu_available, precision):
     assert abs(fields["mag"].sum() * grid["dV"] - ref["net_mag"]) < 1e-3
     assert abs(rho.sum() * grid["dV"] - float(d["Nelectron"])) < 1e-8
     assert abs(res["scf_iters"] - ref["scf_iters"]) <= (1 if precision == 64 else 2)
+
+
+def test_own_setup_spin_scf_matches_reference_program(gpu_available):
+    """Al4 collinear spin from the library's own set-up (psp8 tables -> pseudocharges, atomic
+    and core densities, projectors, the initial magnetization of the seeded moments) through
+    sgpu_scf_kpt, against the reference program's run and its initial fields."""
+    import os
+    import sys
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, golden)
+    import systems
+    from sparc_gb300.psp8 import load_tables
+    from sparc_gb300.setup import CellSystem
+    d, grid, nl, ref = load_scf("Al4_spin_kpt")
+    sysd = systems.al4_spin_kpt()
+    N = (grid["Nx"], grid["Ny"], grid["Nz"])
+    cs = CellSystem(sysd["L"], N, sysd["species"],
+                    {"Al": load_tables(os.path.join(golden, "psp_Al.npz"))})
+    spins = sysd["spins"]["Al"]
+    mag = cs.initial_magnetization(spins)
+    assert np.abs(mag - d["mag0"]).max() <= 1e-10 * np.abs(d["mag0"]).max()
+    assert np.abs(cs.fields["rho_at"] - d["rho3_0"][0]).max() <= 1e-10 * d["rho3_0"][0].max()
+    p = ref["params"]
+    prm = cs.scf_params(Nstates=int(d["Nstates"]), cheb_degree=int(p["ChebDegree"]),
+                        smearing=1.0 / p["Beta"])
+    res, rho, lam, occ = cs.scf_kpt(prm, d["kpts"], d["kpt_wts"], atom_spin_z=spins)
+    assert res["converged"] == 1
+    assert abs(res["Etot"] / cs.n_atom - ref["Etot_per_atom"]) < 1e-5
+    nk, Ns = d["kpts"].shape[0], int(d["Nstates"])
+    lam_ref = np.array(ref["lambda"]).reshape(2 * nk, Ns)
+    occupied = np.array(ref["occ"]).reshape(2 * nk, Ns) > 1e-3
+    assert np.abs(lam[occupied] - lam_ref[occupied]).max() < 1e-5
+    assert abs(res["net_mag"] - ref["net_mag"]) < 1e-3
+    cs.close()
