@@ -23,11 +23,17 @@ def grid_from_mesh(L, mesh_spacing, FDn=6):
     return tuple(max(int(math.ceil(Li / mesh_spacing)), FDn) for Li in L)
 
 
-def ion_coordinates(pos, L=None):
-    """Coordinates as a 12-decimal .ion file carries them; with the cell lengths L, mapped
-    into [0, L) per direction as the reference does for periodic directions
-    (src/initialization.c:2013-2023: x = fmod(x, L) + (x < 0) L when x < 0 or x >= L)."""
-    out = np.array([[float(f"{v:.12f}") for v in p] for p in np.asarray(pos)], dtype=np.float64)
+def ion_coordinates(pos, L=None, exact=False):
+    """Coordinates as a 12-decimal .ion file carries them (exact: as given, e.g. fractional
+    coordinates already multiplied by the cell lengths, as the reader does for COORD_FRAC,
+    src/readfiles.c:1665-1670); with the cell lengths L, mapped into [0, L) per direction as
+    the reference does for periodic directions (src/initialization.c:2013-2023:
+    x = fmod(x, L) + (x < 0) L when x < 0 or x >= L)."""
+    if exact:
+        out = np.array(pos, dtype=np.float64).copy()
+    else:
+        out = np.array([[float(f"{v:.12f}") for v in p] for p in np.asarray(pos)],
+                       dtype=np.float64)
     if L is not None:
         for d in range(3):
             for i in range(out.shape[0]):
@@ -43,9 +49,12 @@ class CellSystem:
     FD weights, nonlocal projectors) and the set-up fields an SCF starts from."""
 
     def __init__(self, L, N, species, tables, tol_scf=1e-6, ref_cutoff=0.5, net_charge=0,
-                 FDn=6, device=0):
+                 FDn=6, device=0, exact_coords=False):
         """species: list of (symbol, positions (n, 3) Bohr); tables: {symbol: read_psp8
-        dict}. Atoms are ordered type by type, as the reference orders them."""
+        dict}. Atoms are ordered type by type, as the reference orders them. Positions are
+        taken as a 12-decimal Cartesian .ion file carries them, or as given with exact_coords
+        (fractional coordinates times the cell lengths)."""
+        self.exact_coords = exact_coords
         self.N = tuple(int(n) for n in N)
         self.FDn = FDn
         self.tables = [tables[s] for s, _ in species]
@@ -73,7 +82,8 @@ class CellSystem:
             self.ctx.set_grid_coeffs(self.cx, self.cy, self.cz, self.dV)
         self.nAtomv = np.array([len(p) for _, p in species], dtype=np.int32)
         self.n_atom = int(self.nAtomv.sum())
-        self.atom_pos = np.concatenate([ion_coordinates(p, self.L) for _, p in species], axis=0)
+        self.atom_pos = np.concatenate([ion_coordinates(p, self.L, self.exact_coords)
+                                        for _, p in species], axis=0)
         self.Nelectron = float(sum(int(t["Znucl"]) * n for t, n in zip(self.tables,
                                                                        self.nAtomv))) - self.net_charge
         self.cutoff = self.ctx.Calculate_PseudochargeCutoff(self.L, 1e-3 * self.tol_scf)
@@ -84,9 +94,10 @@ class CellSystem:
 
     def scf_params(self, Nstates, cheb_degree, smearing=1e-3, precision=SGPU_PREC_FP64,
                    fp64_switch_error=1e-4, graded_tail=0, tail_fp64_degrees=0, seed=1,
-                   verbose=0, maxit_scf=100):
-        """sgpu_scf_params with the reference's defaults for this cell (Fermi-Dirac smearing
-        in Ha, density mixing with Kerker preconditioning, Pulay history 7)."""
+                   verbose=0, maxit_scf=100, elec_T_type=0):
+        """sgpu_scf_params with the reference's defaults for this cell (smearing in Ha,
+        Fermi-Dirac (elec_T_type 0) or Gaussian (1), density mixing with Kerker
+        preconditioning, Pulay history 7)."""
         h_eff = float(self.h[0]) if np.ptp(self.h) < 1e-12 else \
             math.sqrt(3.0 / float(np.sum(1.0 / self.h ** 2)))
         p = ScfParams()
@@ -94,7 +105,7 @@ class CellSystem:
         p.n_atom = self.n_atom
         p.Nelectron = self.Nelectron
         p.Beta = 1.0 / smearing
-        p.elec_T_type = 0
+        p.elec_T_type = int(elec_T_type)
         p.cheb_degree = int(cheb_degree)
         p.rho_trigger = 4
         p.nchefsi = 1

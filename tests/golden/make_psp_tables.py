@@ -14,7 +14,8 @@ sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from oracle.refpath import reference_root  # noqa: E402
 from sparc_gb300.psp8 import read_psp8, save_tables  # noqa: E402
 
-FILES = {"Si": "14_Si_4_1.9_1.9_pbe_n_v1.0.psp8", "Al": "13_Al_3_1.9_1.9_pbe_n_v1.0.psp8"}
+FILES = {"Si": "14_Si_4_1.9_1.9_pbe_n_v1.0.psp8", "Al": "13_Al_3_1.9_1.9_pbe_n_v1.0.psp8",
+         "C": "06_C_4_1.2_1.2_pbe_n_v1.0.psp8"}
 
 
 def main():
