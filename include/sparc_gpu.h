@@ -626,6 +626,13 @@ int sgpu_set_rr_products(sgpu_ctx *ctx, int mode);
  * operation sequence per point up to the rounding of the Bloch factors. */
 int sgpu_set_zstencil_pairs(sgpu_ctx *ctx, int on);
 
+/* Rayleigh-Ritz step of sgpu_CheFSI_batched / sgpu_scf_kpt: 1 (default) batches blocks of one
+ * width and leading dimensions (batched ZGEMM / CGEMM products, batched Cholesky reduction,
+ * one cusolverDnXsyevBatched call for all standard eigenproblems, batched back-substitution
+ * and rotation); 0 one block at a time (ZGEMM / CGEMM and zhegvd per block). Both solve the
+ * same generalized problems Hp q = lambda Mp q (zhegvd reduces them the same way). */
+int sgpu_set_rr_batched(sgpu_ctx *ctx, int on);
+
 /* How sgpu_Solve_Generalized_EigenProblem and the SCF solve Hp q = lambda Mp q
  * (DP_Solve_Generalized_EigenProblem, src/eigenSolver.c:1262; LAPACKE_dsygvd at :1318):
  * mode 0 (default): cuSOLVER dsygvd; 1: the same reduction as separate calls (dpotrf, two

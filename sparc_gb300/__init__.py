@@ -29,7 +29,7 @@ EXPORTED = [
     "sgpu_Calculate_elecstPotential", "sgpu_Mixing_init", "sgpu_Mixing_periodic_pulay",
     "sgpu_Evaluate_scf_error", "sgpu_scf", "sgpu_scf_kpt", "sgpu_Vnl_vec_mult_noalloc",
     "sgpu_Calculate_Vxc_LSDA_PW", "sgpu_Mixing_init_spin", "sgpu_Mixing_periodic_pulay_spin",
-    "sgpu_Generate_InitialMagnetization", "sgpu_set_zstencil_pairs",
+    "sgpu_Generate_InitialMagnetization", "sgpu_set_zstencil_pairs", "sgpu_set_rr_batched",
     "sgpu_set_kpoint_geometry", "sgpu_Lap_plus_diag_vec_mult_orth_kpt", "sgpu_Vnl_vec_mult_kpt",
     "sgpu_Hamiltonian_vectors_mult_kpt", "sgpu_ChebyshevFiltering_kpt", "sgpu_set_psd",
     "sgpu_Calculate_PseudochargeCutoff", "sgpu_Generate_PseudoChargeDensity",
@@ -691,6 +691,9 @@ class Context:
 
     def set_stencil_variant(self, variant):
         _check(lib().sgpu_set_stencil_variant(self._h, int(variant)))
+
+    def set_rr_batched(self, on):
+        _check(lib().sgpu_set_rr_batched(self._h, int(bool(on))))
 
     def set_zstencil_pairs(self, on):
         _check(lib().sgpu_set_zstencil_pairs(self._h, int(bool(on))))

@@ -247,6 +247,16 @@ int sgpu_set_rr_products(sgpu_ctx *ctx, int mode)
     return SGPU_OK;
 }
 
+int sgpu_set_rr_batched(sgpu_ctx *ctx, int on)
+{
+    if (!ctx || (on != 0 && on != 1)) {
+        set_error("sgpu_set_rr_batched: need a context and 0 or 1");
+        return SGPU_ERR_ARG;
+    }
+    ctx->rr_batched = on;
+    return SGPU_OK;
+}
+
 int sgpu_set_zstencil_pairs(sgpu_ctx *ctx, int on)
 {
     if (!ctx || (on != 0 && on != 1)) {

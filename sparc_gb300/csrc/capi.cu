@@ -238,6 +238,8 @@ int sgpu_destroy(sgpu_ctx *ctx)
         if (w.ptr) cudaFree(w.ptr);
     if (ctx->cublas) cublasDestroy(ctx->cublas);
     if (ctx->cusolver) cusolverDnDestroy(ctx->cusolver);
+    if (ctx->xparams) cusolverDnDestroyParams(ctx->xparams);
+    free(ctx->xhost);
     for (auto e : ctx->prof_pool) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

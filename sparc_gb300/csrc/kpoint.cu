@@ -1372,14 +1372,193 @@ int rotate_z(sgpu_ctx *ctx, int ncol, const CT *Y, long ldy, const double2 *Q, C
     return SGPU_OK;
 }
 
+// Rayleigh-Ritz step of nblk blocks of equal width n in batched calls: H Y per block, then
+// Hp = Yᴴ HY and Mp = Yᴴ Y for all blocks (batched ZGEMM / CGEMM), the generalized Hermitian
+// eigenproblems Hp q = lambda Mp q reduced as zhegvd does (Mp = Uᴴ U by batched Cholesky,
+// C = U⁻ᴴ Hp U⁻¹ by two batched triangular solves), all standard eigenproblems in one
+// cusolverDnXsyevBatched call, Q = U⁻¹ V, and X = Y Q (batched). Ritz values land in lambda
+// (host), block after block.
+template <typename CT>
+static int rr_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, double *lambda,
+                      cudaStream_t st)
+{
+    const int n = blk[0].ncol;
+    const long n2 = (long)n * n;
+    SGPU_TRY(ensure_solver_handles(ctx));
+    SGPU_CUBLAS_TRY(cublasSetStream(ctx->cublas, st));
+    cusolverDnSetStream(ctx->cusolver, st);
+    // workspace: Hp, Mp (complex128, nblk n x n each), complex64 staging for CGEMM results,
+    // eigenvalues, infos, pointer arrays
+    char *ws = nullptr;
+    const size_t zbytes = sizeof(double2) * 2 * (size_t)nblk * n2;
+    const size_t cbytes = sizeof(CT) == 8 ? sizeof(float2) * 2 * (size_t)nblk * n2 : 0;
+    const size_t wbytes = sizeof(double) * (size_t)nblk * n;
+    const size_t ibytes = sizeof(int) * (size_t)(2 * nblk + 8);
+    const size_t pbytes = sizeof(void *) * (size_t)(12 * nblk);
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t total = al(zbytes) + al(cbytes) + al(wbytes) + al(ibytes) + al(pbytes);
+    SGPU_TRY(ws_get(ctx, WS_EIG, total, (void **)&ws));
+    double2 *Hp = reinterpret_cast<double2 *>(ws), *Mp = Hp + (size_t)nblk * n2;
+    char *q = ws + al(zbytes);
+    float2 *Hc = reinterpret_cast<float2 *>(q), *Mc = Hc + (size_t)nblk * n2;
+    q += al(cbytes);
+    double *W = reinterpret_cast<double *>(q);
+    q += al(wbytes);
+    int *info = reinterpret_cast<int *>(q);
+    q += al(ibytes);
+    void **dptr = reinterpret_cast<void **>(q);
+    // pointer arrays: Y, X (as HY and as the rotation output), Hp, Mp (or their complex64
+    // staging), then the complex128 Hp, Mp for the solves
+    std::vector<void *> hp(12 * (size_t)nblk);
+    for (int b = 0; b < nblk; b++) {
+        hp[b] = blk[b].Y;
+        hp[nblk + b] = blk[b].X;
+        hp[2 * nblk + b] = sizeof(CT) == 8 ? (void *)(Hc + b * n2) : (void *)(Hp + b * n2);
+        hp[3 * nblk + b] = sizeof(CT) == 8 ? (void *)(Mc + b * n2) : (void *)(Mp + b * n2);
+        hp[4 * nblk + b] = Hp + b * n2;
+        hp[5 * nblk + b] = Mp + b * n2;
+    }
+    SGPU_CUDA_TRY(cudaMemcpyAsync(dptr, hp.data(), sizeof(void *) * 6 * nblk,
+                                  cudaMemcpyHostToDevice, st));
+    // H Y into X, block by block (each block's own k-point and spin)
+    for (int b = 0; b < nblk; b++) {
+        const sgpu_filter_block &f = blk[b];
+        SGPU_TRY(set_phases(ctx, f.k, st));
+        SGPU_TRY(hamiltonian_z<CT>(ctx, f.spin, f.k, n, 0.0, reinterpret_cast<CT *>(f.Y), f.ldo,
+                                   reinterpret_cast<CT *>(f.X), f.ldi, 1.0, 0.0, nullptr, 0, st));
+    }
+    const int Nd = (int)ctx->Nd;
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        if constexpr (sizeof(CT) == 16) {
+            const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+            auto P = [&](int i) { return reinterpret_cast<cuDoubleComplex **>(dptr + (size_t)i * nblk); };
+            SGPU_CUBLAS_TRY(cublasZgemmBatched(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, Nd,
+                                               &one, P(0), blk[0].ldo, P(0), blk[0].ldo, &zero,
+                                               P(3), n, nblk));
+            SGPU_CUBLAS_TRY(cublasZgemmBatched(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, Nd,
+                                               &one, P(0), blk[0].ldo, P(1), blk[0].ldi, &zero,
+                                               P(2), n, nblk));
+        } else {
+            const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+            auto P = [&](int i) { return reinterpret_cast<cuComplex **>(dptr + (size_t)i * nblk); };
+            SGPU_CUBLAS_TRY(cublasCgemmBatched(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, Nd,
+                                               &one, P(0), blk[0].ldo, P(0), blk[0].ldo, &zero,
+                                               P(3), n, nblk));
+            SGPU_CUBLAS_TRY(cublasCgemmBatched(ctx->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, Nd,
+                                               &one, P(0), blk[0].ldo, P(1), blk[0].ldi, &zero,
+                                               P(2), n, nblk));
+        }
+    }
+    if constexpr (sizeof(CT) == 8) {  // complex64 products to complex128 for the solves
+        SGPU_TRY(convert_cols<float, double>(reinterpret_cast<float *>(Hc), 4 * nblk * n2,
+                                             reinterpret_cast<double *>(Hp), 4 * nblk * n2,
+                                             4 * nblk * n2, 1, st));
+    }
+    auto PZ = [&](int i) { return reinterpret_cast<cuDoubleComplex **>(dptr + (size_t)i * nblk); };
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        // Mp = Uᴴ U
+        if (cusolverDnZpotrfBatched(ctx->cusolver, CUBLAS_FILL_MODE_UPPER, n, PZ(5), n, info,
+                                    nblk) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnZpotrfBatched failed to launch");
+            return SGPU_ERR_CUDA;
+        }
+        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0);
+        // C = U⁻ᴴ Hp U⁻¹
+        SGPU_CUBLAS_TRY(cublasZtrsmBatched(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER,
+                                           CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one, PZ(5), n,
+                                           PZ(4), n, nblk));
+        SGPU_CUBLAS_TRY(cublasZtrsmBatched(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER,
+                                           CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one, PZ(5), n,
+                                           PZ(4), n, nblk));
+        // C V = V diag(lambda), all blocks in one call
+        if (!ctx->xparams && cusolverDnCreateParams(&ctx->xparams) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnCreateParams failed");
+            return SGPU_ERR_CUDA;
+        }
+        size_t dws = 0, hws = 0;
+        if (cusolverDnXsyevBatched_bufferSize(ctx->cusolver, ctx->xparams, CUSOLVER_EIG_MODE_VECTOR,
+                                              CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, Hp, n,
+                                              CUDA_R_64F, W, CUDA_C_64F, &dws, &hws,
+                                              nblk) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnXsyevBatched_bufferSize failed");
+            return SGPU_ERR_CUDA;
+        }
+        void *dwork = nullptr;
+        SGPU_TRY(ws_get(ctx, WS_MISC, dws + 16, &dwork));
+        if (ctx->xhost_bytes < hws) {
+            free(ctx->xhost);
+            ctx->xhost = hws ? malloc(hws) : nullptr;
+            ctx->xhost_bytes = ctx->xhost ? hws : 0;
+            if (hws && !ctx->xhost) {
+                set_error("host workspace allocation failed");
+                return SGPU_ERR_NOMEM;
+            }
+        }
+        if (cusolverDnXsyevBatched(ctx->cusolver, ctx->xparams, CUSOLVER_EIG_MODE_VECTOR,
+                                   CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, Hp, n, CUDA_R_64F, W,
+                                   CUDA_C_64F, dwork, dws, ctx->xhost, hws, info + nblk,
+                                   nblk) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnXsyevBatched failed to launch");
+            return SGPU_ERR_CUDA;
+        }
+        // Q = U⁻¹ V
+        SGPU_CUBLAS_TRY(cublasZtrsmBatched(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER,
+                                           CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one, PZ(5), n,
+                                           PZ(4), n, nblk));
+    }
+    // X = Y Q
+    {
+        ProfScope ps(ctx, SGPU_KERNEL_OTHER, st);
+        if constexpr (sizeof(CT) == 16) {
+            const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+            auto P = [&](int i) { return reinterpret_cast<cuDoubleComplex **>(dptr + (size_t)i * nblk); };
+            SGPU_CUBLAS_TRY(cublasZgemmBatched(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, Nd, n, n,
+                                               &one, P(0), blk[0].ldo, P(4), n, &zero, P(1),
+                                               blk[0].ldi, nblk));
+        } else {
+            SGPU_TRY(convert_cols<double, float>(reinterpret_cast<double *>(Hp), 2 * nblk * n2,
+                                                 reinterpret_cast<float *>(Hc), 2 * nblk * n2,
+                                                 2 * nblk * n2, 1, st));
+            const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+            auto P = [&](int i) { return reinterpret_cast<cuComplex **>(dptr + (size_t)i * nblk); };
+            SGPU_CUBLAS_TRY(cublasCgemmBatched(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, Nd, n, n,
+                                               &one, P(0), blk[0].ldo, P(2), n, &zero, P(1),
+                                               blk[0].ldi, nblk));
+        }
+    }
+    std::vector<int> hinfo(2 * nblk);
+    SGPU_CUDA_TRY(cudaMemcpyAsync(lambda, W, sizeof(double) * (size_t)nblk * n,
+                                  cudaMemcpyDeviceToHost, st));
+    SGPU_CUDA_TRY(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * 2 * nblk,
+                                  cudaMemcpyDeviceToHost, st));
+    SGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int b = 0; b < 2 * nblk; b++) {
+        if (hinfo[b] != 0) {
+            set_error(std::string(b < nblk ? "batched Cholesky of Mp" : "batched eigensolve") +
+                      ": info = " + std::to_string(hinfo[b]) + " in block " +
+                      std::to_string(b % nblk));
+            return SGPU_ERR_LINALG;
+        }
+    }
+    return SGPU_OK;
+}
+
 // One CheFSI pass over all (k, spin) blocks: the batched filter, then per block H Y into X,
 // the projection, the eigenproblem and the rotation into X; lambda (host) receives each
-// block's Ritz values, blocks one after another.
+// block's Ritz values, blocks one after another. Blocks of one width with common leading
+// dimensions take the batched Rayleigh-Ritz step (ctx->rr_batched), others one block at a time.
 template <typename CT>
 int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
                    double *lambda, cudaStream_t st)
 {
     SGPU_TRY(chebyshev_batched<CT>(ctx, nblk, blk, m, st));
+    bool uniform = ctx->rr_batched && nblk > 0;
+    for (int b = 1; b < nblk && uniform; b++)
+        uniform = blk[b].ncol == blk[0].ncol && blk[b].ldi == blk[0].ldi &&
+                  blk[b].ldo == blk[0].ldo;
+    if (uniform && blk[0].ncol > 0) return rr_batched<CT>(ctx, nblk, blk, lambda, st);
     int nmax = 0;
     for (int b = 0; b < nblk; b++) nmax = std::max(nmax, blk[b].ncol);
     char *buf = nullptr;

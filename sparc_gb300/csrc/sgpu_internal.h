@@ -152,6 +152,11 @@ struct sgpu_ctx {
     bool has_nl = false;
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
+    cusolverDnParams_t xparams = nullptr;   // 64-bit cuSOLVER API parameters (batched syev)
+    void *xhost = nullptr;                  // its host workspace
+    size_t xhost_bytes = 0;
+    int rr_batched = 1;                     // k-point CheFSI pass: batched Rayleigh-Ritz step
+                                            // for blocks of one width (sgpu_set_rr_batched)
     sgpu::Workspace ws[16];    // grow-only scratch slots (see enum WsSlot)
     sgpu::MixState *mix = nullptr;
     sgpu::KpointState *kp = nullptr;  // cell lengths and image coordinates (k-point calls)

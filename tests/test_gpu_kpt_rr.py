@@ -98,3 +98,41 @@ def test_batched_chefsi_converges_to_dense_eigenvalues(gpu_available, si2k, prec
     for slot in (0, 1):
         _, ev = dense[slot]
         assert np.abs(lam[slot][:want] - ev[:want]).max() < tol, (slot, lam[slot][:want] - ev[:want])
+
+
+@pytest.mark.parametrize("precision,tol", [(sg.SGPU_PREC_FP64, 1e-11),
+                                           (sg.SGPU_PREC_FP32, 2e-5)])
+def test_batched_rayleigh_ritz_matches_per_block(gpu_available, si2k, precision, tol):
+    """The batched Rayleigh-Ritz step (batched products, batched Cholesky reduction, one
+    batched Hermitian eigensolve) against one zhegvd per block, on the same filtered blocks:
+    the same Ritz values and the same Ritz subspaces (projector difference)."""
+    import torch
+    d, ctx, dense, Nd = si2k
+    ncol = 10
+    cdt = torch.complex128 if precision == sg.SGPU_PREC_FP64 else torch.complex64
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(23)
+    X0 = [torch.complex(torch.rand((ncol, Nd), generator=gen, device="cuda", dtype=torch.float64),
+                        torch.rand((ncol, Nd), generator=gen, device="cuda", dtype=torch.float64)
+                        ).to(cdt) - (0.5 + 0.5j) for _ in range(3)]
+    res = {}
+    for mode in (1, 0):
+        ctx.set_rr_batched(mode)
+        blocks = []
+        for b, slot in enumerate((0, 1, 0)):
+            _, ev = dense[slot]
+            blocks.append(dict(spin=0, k=list(d["kpts"][slot]), X=X0[b].clone(),
+                               Y=torch.empty_like(X0[b]), a=float(ev[ncol]) + 0.05,
+                               b=float(ev[-1]) * 1.01, a0=float(ev[0]) - 0.1))
+        lam = ctx.CheFSI_batched(blocks, 9, precision=precision)
+        res[mode] = (lam, [bl["X"].to(torch.complex128).cpu().numpy() for bl in blocks])
+    ctx.set_rr_batched(1)
+    for b in range(3):
+        la, lb = res[1][0][b], res[0][0][b]
+        assert np.abs(la - lb).max() < tol * max(1.0, np.abs(lb).max())
+        # the Ritz vectors agree up to phases (and rotations inside degenerate groups): the
+        # principal angles between the two spans are zero
+        Qa, _ = np.linalg.qr(res[1][1][b].T)
+        Qb, _ = np.linalg.qr(res[0][1][b].T)
+        sv = np.linalg.svd(Qa.conj().T @ Qb, compute_uv=False)
+        assert np.abs(1.0 - sv).max() < 100 * tol
