@@ -73,6 +73,8 @@ def parse():
                          "fp32_eager, fp32_bf16_split, fp64)")
     ap.add_argument("--fp64-only", action="store_true",
                     help="only the FP64 filter steps, no tuning or side blocks (profiling)")
+    ap.add_argument("--fp32-only", action="store_true",
+                    help="only the tuned FP32 filter steps and their kernel times (profiling)")
     ap.add_argument("--c3-prec", type=int, default=0, choices=[0, 32, 64],
                     help="C3 block: only this precision (0: both)")
     ap.add_argument("--c3-filter-only", action="store_true",
@@ -84,7 +86,7 @@ def parse():
                     help="use this FP32 stencil variant instead of the tuned one (profiling)")
     ap.add_argument("--nl-apply", type=int, default=None,
                     help="use this nonlocal apply form instead of the tuned one (profiling)")
-    ap.add_argument("--nl-fuse", type=int, default=None, choices=[0, 2, 4],
+    ap.add_argument("--nl-fuse", type=int, default=None, choices=[0, 2, 3, 4],
                     help="force the projections carried across filter degrees off (0) or on "
                          "with 2 or 4 columns per thread")
     ap.add_argument("--nl-project", type=int, default=None,
@@ -707,6 +709,7 @@ def main():
         ctx.set_nonlocal_fuse(args.nl_fuse != 0, args.nl_fuse or None)
     forms = ctx.variants()
     fuse_on, fuse_cpl, fuse_ms = ctx.nonlocal_fuse()
+    fuse_tc_avail, fuse_tc_ms = ctx.nonlocal_fuse_tc()
     kernel_name = STENCIL_NAMES[variant]
     nls = nonlocal_stats(nl)
 
@@ -781,6 +784,29 @@ def main():
                 "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_src,
                 "traffic": traffic, "algorithmic_bytes_per_launch": int(alg_bytes),
                 "ms_per_launch": round(launch_ms, 4)}
+
+    if args.fp32_only:  # the tuned FP32 filter alone: kernel times, forms, rooflines
+        X, Y = X0.clone(), torch.empty_like(X0)
+
+        def step32_only():
+            with torch.cuda.stream(stream):
+                X.copy_(X0)
+            ctx.ChebyshevFiltering_f32(X, Y, M, a, b, a0)
+
+        ms32, k32_step, k32_launch, _ = profiled(step32_only, args.steps, args.warmup)
+        nl_b = (2 * nls["ncov"] * ncol + nls["nnz"]) * 4.0
+        out = {"fp32_only": True, "ms_per_filter": round(ms32, 3),
+               "GBs": round(filter_bytes(Nd, ncol, M, 4) / (ms32 / 1e3) / 1e9, 1),
+               "kernels_per_step_ms": k32_step,
+               "ms_per_launch": {k: (round(v, 4) if v else None) for k, v in k32_launch.items()},
+               "fused_form": fuse_cpl if fuse_on else 0, "fused_ms_cuda_cores": fuse_ms,
+               "fused_ms_tensor_cores": fuse_tc_ms if fuse_tc_avail else None,
+               "tuning_ms": ctx.tuning(), "stencil": kernel_name}
+        if k32_launch["nl_apply"]:
+            out["nl_apply_roofline"] = hbm_roofline("nl_apply", nl_b, k32_launch["nl_apply"],
+                                                    None)
+        print(json.dumps(out), flush=True)
+        return
 
     # ---------------- headline: the plain FP64 filter (the drop-in), device-resident blocks
     X64_0 = X0.double()
@@ -867,8 +893,9 @@ def main():
                                     traffic_of(kernel_name, "fp32_bytes_per_launch_at_bench"))}
     rl32["stencil"]["share_of_step"] = round(k32_step["stencil"] / ms32, 4)
     if k32_launch["nl_apply"]:
-        nlname = ("k_nl_apply_project_range (apply + next projection)" if fuse_on
-                  else "nonlocal apply")
+        nlname = ("nonlocal apply" if not fuse_on else
+                  "k_nl_apply_project_tc (apply + next projection, tensor cores)"
+                  if fuse_cpl == 3 else "k_nl_apply_project_range (apply + next projection)")
         nl_b = (2 * nls["ncov"] * ncol + nls["nnz"]) * 4.0
         rl32["nl_apply"] = hbm_roofline(nlname, nl_b, k32_launch["nl_apply"],
                                         traffic_of(nlname, "fp32_bytes_per_launch_at_bench"))
@@ -943,8 +970,12 @@ def main():
                     "autotune_ms": {k: [round(float(v), 4) for v in vs]
                                     for k, vs in ctx.tuning().items()},
                     "projection_carried": fuse_on,
-                    "fused_columns_per_thread": fuse_cpl,
-                    "fused_apply_project_ms": [round(v, 4) for v in fuse_ms]}}
+                    "fused_form": {0: "off", 2: "CUDA cores, 2 columns per thread",
+                                   3: "tensor cores (tcgen05, three-slice BF16 products)",
+                                   4: "CUDA cores, 4 columns per thread"}[fuse_cpl],
+                    "fused_apply_project_ms": [round(v, 4) for v in fuse_ms],
+                    "fused_apply_project_tc_ms": round(fuse_tc_ms, 4) if fuse_tc_avail
+                    else None}}
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms64, 3),

@@ -640,18 +640,26 @@ int sgpu_set_rr_batched(sgpu_ctx *ctx, int on);
  * results agree to the eigensolvers' accuracy. */
 int sgpu_set_eig_solver(sgpu_ctx *ctx, int mode);
 
-/* FP32 filter with the projections carried across degrees (mode 1, 2 or 4) or not (0). When
- * on, every degree's nonlocal apply is the range form with the projection of the iterate it
- * finishes fused in (alpha of the next degree is formed from the finished values while they
- * are in shared memory), so a filter of degree m launches one projection instead of m. The
- * fused kernel has two forms, 2 or 4 columns per thread (mode 2 or 4; mode 1 keeps the
- * current one). The apply results are bit-identical to form 4 in both; the projections agree
- * with the separate ones to FP32 rounding (atomic summation order). Needs the range tables of
- * FP32 projector sets; off otherwise. sgpu_autotune times both forms and turns fusion on when
- * the faster beats the fastest separate apply plus projection. */
+/* FP32 filter with the projections carried across degrees (mode 1, 2, 3 or 4) or not (0).
+ * When on, every degree's nonlocal apply is the range form with the projection of the iterate
+ * it finishes fused in (alpha of the next degree is formed from the finished values while
+ * they are on chip), so a filter of degree m launches one projection instead of m. The fused
+ * kernel has three forms: on the CUDA cores with 2 or 4 columns per thread (mode 2 or 4; the
+ * apply results bit-identical to form 4), and on the tensor cores (mode 3: per range of at
+ * most 128 covered points and 64 projector rows, the apply and the projection as tcgen05
+ * products of three-slice BF16 splits, FP32-accurate, accumulated in FP32); mode 1 keeps the
+ * current form. The projections agree with the separate ones to FP32 rounding. Needs the
+ * range tables of FP32 projector sets; mode 3 also the tensor-core tables (built unless a
+ * covered point needs more than 64 rows: SGPU_ERR_STATE then). sgpu_autotune times every form
+ * and turns fusion on when the fastest beats the fastest separate apply plus projection. */
 int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int mode);
 
-/* The fused form in use (*mode: 0 off, else 2 or 4 columns per thread) and the last tuned
+/* Whether the tensor-core fused form is available for the installed projector set
+ * (*available 0/1) and its last tuned time of one launch (*tc_ms, 0 before tuning); either
+ * pointer may be NULL. */
+int sgpu_get_nonlocal_fuse_tc(sgpu_ctx *ctx, int *available, double *tc_ms);
+
+/* The fused form in use (*mode: 0 off, 2 or 4 columns per thread, 3 tensor cores) and the last tuned
  * times of one fused launch of each form (fused_ms[2]: 2 and 4 columns, 0 before tuning);
  * either pointer may be NULL. */
 int sgpu_get_nonlocal_fuse(sgpu_ctx *ctx, int *mode, double *fused_ms);

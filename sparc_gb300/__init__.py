@@ -42,7 +42,7 @@ EXPORTED = [
     "sgpu_get_tuning", "sgpu_Calculate_local_forces", "sgpu_Calculate_nonlocal_forces",
     "sgpu_Calculate_forces_xc", "sgpu_Gradient_vectors_dir", "sgpu_Symmetrize_forces",
     "sgpu_kernel_status", "sgpu_check_wait_bound", "sgpu_set_nonlocal_fuse",
-    "sgpu_get_nonlocal_fuse", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
+    "sgpu_get_nonlocal_fuse", "sgpu_get_nonlocal_fuse_tc", "sgpu_ChebyshevFiltering_y", "sgpu_Project_Hamiltonian_f32",
     "sgpu_Subspace_Rotation_f32", "sgpu_set_gemm_emulation", "sgpu_measure_fp64_rate",
     "sgpu_set_rr_products", "sgpu_set_eig_solver", "sgpu_Project_Hamiltonian_kpt",
     "sgpu_Solve_Generalized_EigenProblem_kpt", "sgpu_Subspace_Rotation_kpt", "sgpu_CheFSI_batched",
@@ -736,9 +736,18 @@ class Context:
 
     def set_nonlocal_fuse(self, on, cpl=None):
         """Carry the nonlocal projections across filter degrees (fused range apply) or not;
-        cpl = 2 or 4 fixes the fused kernel's columns per thread."""
+        cpl = 2 or 4 fixes the CUDA-core kernel's columns per thread, cpl = 3 selects the
+        tensor-core kernel."""
         mode = 0 if not on else (int(cpl) if cpl else 1)
         _check(lib().sgpu_set_nonlocal_fuse(self._h, mode))
+
+    def nonlocal_fuse_tc(self):
+        """(whether the tensor-core fused form is available, ms of one launch at the last
+        tuning)."""
+        av = ctypes.c_int()
+        ms = ctypes.c_double()
+        _check(lib().sgpu_get_nonlocal_fuse_tc(self._h, ctypes.byref(av), ctypes.byref(ms)))
+        return bool(av.value), float(ms.value)
 
     def nonlocal_fuse(self):
         """(on, columns per thread of the fused form or 0, [ms of one fused launch with 2 and

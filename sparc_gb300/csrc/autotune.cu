@@ -131,7 +131,11 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
                 if (cudaMallocAsync(&anext, abytes, st) != cudaSuccess) rc = SGPU_ERR_CUDA;
                 float fbest = 1e30f;
                 int cbest = 2;
-                for (int cpl = 2; cpl <= 4 && rc == SGPU_OK; cpl += 2) {  // columns per lane
+                ctx->tune_fused_tc_ms = 0.0;
+                // the CUDA-core kernel with 2 and 4 columns per lane, and the tensor-core kernel
+                for (int cpl : {2, 4, 3}) {
+                    if (rc != SGPU_OK) break;
+                    if (cpl == 3 && !nonlocal_tc_ready(ctx)) continue;
                     ctx->nl_fuse_cpl = cpl;
                     float t = 0.f, tmin = 1e30f;
                     for (int rep = 0; rep < 3 && rc == SGPU_OK; rep++) {
@@ -151,7 +155,12 @@ static int tune_stencil(sgpu_ctx *ctx, int ncol, int *best, double *ms)
                         }
                         if (rep > 0) tmin = std::min(tmin, t);  // the first is a warm-up
                     }
-                    if (rc == SGPU_OK) ctx->tune_fused_cpl_ms[cpl / 2 - 1] = tmin;
+                    if (rc == SGPU_OK) {
+                        if (cpl == 3)
+                            ctx->tune_fused_tc_ms = tmin;
+                        else
+                            ctx->tune_fused_cpl_ms[cpl / 2 - 1] = tmin;
+                    }
                     if (rc == SGPU_OK && tmin < fbest) { fbest = tmin; cbest = cpl; }
                 }
                 ctx->nl_fuse_cpl = cbest;
@@ -269,12 +278,28 @@ int sgpu_set_zstencil_pairs(sgpu_ctx *ctx, int on)
 
 int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int mode)
 {
-    if (!ctx || (mode != 0 && mode != 1 && mode != 2 && mode != 4)) {
-        set_error("sgpu_set_nonlocal_fuse: need a context and mode 0, 1, 2 or 4");
+    if (!ctx || mode < 0 || mode > 4) {
+        set_error("sgpu_set_nonlocal_fuse: need a context and mode 0, 1, 2, 3 or 4");
         return SGPU_ERR_ARG;
     }
+    if (mode == 3 && !sgpu::nonlocal_tc_ready(ctx)) {
+        set_error("sgpu_set_nonlocal_fuse: no tensor-core range tables for this projector set "
+                  "(a covered point needs more than 64 projector rows, or none is set)");
+        return SGPU_ERR_STATE;
+    }
     ctx->nl_fuse = mode != 0;
-    if (mode == 2 || mode == 4) ctx->nl_fuse_cpl = mode;
+    if (mode >= 2) ctx->nl_fuse_cpl = mode;
+    return SGPU_OK;
+}
+
+int sgpu_get_nonlocal_fuse_tc(sgpu_ctx *ctx, int *available, double *tc_ms)
+{
+    if (!ctx) {
+        set_error("sgpu_get_nonlocal_fuse_tc: null context");
+        return SGPU_ERR_ARG;
+    }
+    if (available) *available = sgpu::nonlocal_tc_ready(ctx) ? 1 : 0;
+    if (tc_ms) *tc_ms = ctx->tune_fused_tc_ms;
     return SGPU_OK;
 }
 

@@ -53,6 +53,31 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned a, unsigned parity,
     return mbar_test(a, parity) || mbar_wait_slow(a, parity, limit);
 }
 
+// the same wait with the waiting warp suspended inside try_wait (up to suspend_ns per try)
+// instead of spinning: for waits on long asynchronous work (tensor-core MMAs), where spinning
+// warps would take issue slots from the warps doing the other work of the SM
+__device__ __forceinline__ bool mbar_test_suspend(unsigned a, unsigned parity, unsigned suspend_ns)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n"
+                 " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+                 " selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(a), "r"(parity), "r"(suspend_ns)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_suspend(unsigned a, unsigned parity,
+                                                  long long limit = kWaitCycles)
+{
+    if (mbar_test_suspend(a, parity, 100000u)) return true;
+    const long long t0 = clock64();
+#pragma unroll 1
+    while (!mbar_test_suspend(a, parity, 100000u))
+        if (clock64() - t0 > limit) return false;
+    return true;
+}
+
 __device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes,
                                          unsigned mbar)
 {

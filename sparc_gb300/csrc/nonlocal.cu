@@ -1054,6 +1054,9 @@ int launch_nonlocal_apply_project(sgpu_ctx *ctx, int ncol, const float *alpha, l
         set_error("nonlocal: the fused apply needs the range tables (none built)");
         return SGPU_ERR_STATE;
     }
+    if (ctx->nl_fuse_cpl == 3)
+        return launch_nonlocal_apply_project_tc(ctx, ncol, alpha, lda, scale, out, ldo,
+                                                alpha_next, st);
     const int cpl = ctx->nl_fuse_cpl == 4 ? 4 : 2;
     const size_t rsm = sizeof(float) * ((size_t)nl.max_range_ent * nl.range_jp +
                                         (size_t)kRangePts * (64 + cpl)) +
@@ -1104,7 +1107,8 @@ void nonlocal_free(Nonlocal &nl)
                     nl.seg_start, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows,
                     nl.rng_pt0,  nl.rng_ent0, nl.rng_item0, nl.item_e0, nl.item_row,
                     nl.item_wsplit,
-                    nl.pe_lp,    nl.pe_chi32};
+                    nl.pe_lp,    nl.pe_chi32, nl.tc_pt0, nl.tc_row0, nl.tc_rows, nl.tc_ent0,
+                    nl.tc_ent,   nl.tc_chi};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     nl = Nonlocal();
@@ -1341,6 +1345,7 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(pe_lp, pe_lp.data(), pe_lp.size());
     UP(pe_chi32, pe_chi.data(), pe_chi.size());
 #undef UP
+    if (rc == SGPU_OK) rc = nonlocal_tc_build(nl, covptr, ent_chi, ent_meta, chi);
     if (rc != SGPU_OK) {
         nonlocal_free(nl);
         return rc;

@@ -96,6 +96,16 @@ struct Nonlocal {
     int2 *item_row = nullptr;   // nitem: (first projector row, projector count)
     int *pe_lp = nullptr;       // entries in range order: point index within the range
     float *pe_chi32 = nullptr;  // entries in range order: Chi values, range_jp per entry
+    // fused apply + projection on the tensor cores (nonlocal_tc.cu): ranges of at most 128
+    // covered points whose atoms own at most 64 projector rows, one merged entry per
+    // (point, atom); tc_nrange 0 when a covered point alone needs more rows
+    int tc_nrange = 0;
+    int *tc_pt0 = nullptr;      // tc_nrange + 1: first covered point of each range
+    int *tc_row0 = nullptr;     // tc_nrange + 1: first row-list entry of each range
+    int *tc_rows = nullptr;     // alpha row of every range row
+    int *tc_ent0 = nullptr;     // tc_nrange + 1: first merged entry of each range
+    int *tc_ent = nullptr;      // point | row offset << 7 | projector count << 14
+    float *tc_chi = nullptr;    // Chi values of the merged entries, range_jp per entry
 };
 
 struct Workspace {
@@ -169,7 +179,8 @@ struct sgpu_ctx {
     int nl_project_variant = 0;  // FP32 projection: 0 per image segment, 1 per point range
     bool nl_fuse = false;  // FP32 filter: project each new iterate inside the range apply that
                            // finishes it (one projection launch per filter, not per degree)
-    int nl_fuse_cpl = 2;   // fused apply: columns per lane (2 or 4), chosen by the tuner
+    int nl_fuse_cpl = 2;   // fused apply form, chosen by the tuner: columns per lane of the
+                           // CUDA-core kernel (2 or 4), or 3 for the tensor-core kernel
     int gemm_mode = 0;  // FP32-block products: 0 cuBLAS FP32 GEMM (BF16x9 emulation where
                         // cuBLAS expects a gain), 1 the same with eager emulation, 2 the
                         // library's three-part BF16 split on the tensor cores (cuBLAS GEMMs)
@@ -183,6 +194,7 @@ struct sgpu_ctx {
                         // one-point kernel (0) (sgpu_set_zstencil_pairs)
     double tune_fused_ms = 0.0;  // last timing of the fused apply + projection (chosen form)
     double tune_fused_cpl_ms[2] = {0, 0};  // last timings of the 2- and 4-column forms
+    double tune_fused_tc_ms = 0.0;         // last timing of the tensor-core form
     double tune_apply_ms[5] = {0, 0, 0, 0, 0}, tune_project_ms[2] = {0, 0};  // last timings
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int *kstatus = nullptr;    // device word: bits set by kernel waits that ran out
@@ -265,6 +277,15 @@ int launch_nonlocal_apply(sgpu_ctx *ctx, int ncol, const T *alpha, long lda, dou
 int launch_nonlocal_apply_project(sgpu_ctx *ctx, int ncol, const float *alpha, long lda,
                                   double scale, float *out, long ldo, float *alpha_next,
                                   cudaStream_t st);
+// the same with the tensor-core kernel (nonlocal_tc.cu); needs the tensor-core range tables
+int launch_nonlocal_apply_project_tc(sgpu_ctx *ctx, int ncol, const float *alpha, long lda,
+                                     double scale, float *out, long ldo, float *alpha_next,
+                                     cudaStream_t st);
+bool nonlocal_tc_ready(const sgpu_ctx *ctx);
+// builds the tensor-core range tables from the point CSR of nonlocal_upload
+int nonlocal_tc_build(Nonlocal &nl, const std::vector<int> &covptr,
+                      const std::vector<long> &ent_chi, const std::vector<int4> &ent_meta,
+                      const double *chi);
 int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double *gamma,
                     int nimg, const int *img_atom, const int *img_ndc, const int *grid_pos,
                     const double *chi);

@@ -276,13 +276,14 @@ def test_bounded_wait_reports_and_context_stays_usable(gpu_available):
 
 
 @pytest.mark.parametrize("lmax,m,cpl", [(2, 20, 2), (2, 20, 4), (3, 7, 2), (3, 7, 4), (2, 1, 4),
-                                        (2, 2, 2)])
+                                        (2, 2, 2), (2, 20, 3), (3, 7, 3), (2, 1, 3)])
 def test_fp32_filter_with_carried_projections(gpu_available, lmax, m, cpl):
     """Nonlocal projections carried across filter degrees (each degree's range apply also
     projects the iterate it finishes): the FP32 filter matches the FP64 oracle within the FP32
     filter tolerance, and the filter that launches the range apply and the range projection
     separately to FP32 rounding (the two sum the projections in other atomic orders).
-    67 columns: two column groups, the second ragged, an odd last pair."""
+    67 columns: two column groups, the second ragged, an odd last pair. cpl 3 is the
+    tensor-core form (three-slice BF16 products, FP32-accurate)."""
     shape = (40, 36, 30)
     rng = np.random.default_rng(77 + lmax)
     h = (0.41, 0.37, 0.45)
@@ -296,6 +297,8 @@ def test_fp32_filter_with_carried_projections(gpu_available, lmax, m, cpl):
     x = rng.uniform(-1, 1, (67, Nd))
     ctx.set_nonlocal_apply_variant(4)
     ctx.set_nonlocal_project_variant(1)
+    if cpl == 3:
+        assert ctx.nonlocal_fuse_tc()[0]  # at most 64 projector rows at any covered point
     outs = {}
     for fuse in (False, True):
         ctx.set_nonlocal_fuse(fuse, cpl)
@@ -355,11 +358,11 @@ def test_host_arrays_stream_through_column_chunks(gpu_available, precision, ncol
 
 
 @pytest.mark.parametrize("ncol", [1, 2, 63, 64, 65, 128])
-@pytest.mark.parametrize("cpl", [2, 4])
+@pytest.mark.parametrize("cpl", [2, 4, 3])
 def test_carried_projections_column_edges(gpu_available, ncol, cpl):
     """The fused range apply + projection at column counts that end a 64-column group
-    exactly, one short, one over, a single column and an odd last pair (each form), against
-    the oracle within the FP32 filter tolerance."""
+    exactly, one short, one over, a single column and an odd last pair (each form, cpl 3 the
+    tensor-core kernel), against the oracle within the FP32 filter tolerance."""
     grid, nl, veff, rng = _random_case((32, 26, 22), seed=41 + ncol, natom=6)
     Nd = 32 * 26 * 22
     ctx = make_ctx(grid, nl, veff)
