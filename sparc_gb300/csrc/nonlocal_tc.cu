@@ -192,6 +192,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     };
 
     gather(g0 * kTcCols);  // in flight while the Chi tile is built
+    // this thread's first merged entry, loaded before the tile is zeroed (12 values per entry,
+    // the layout of sets with at most 9 projectors per atom; others load in the loop below)
+    const bool pre = T.jp == 12 && e0 + t < e1;
+    int meta_pre = 0;
+    float4 chi_pre[3];
+    if (pre) {
+        meta_pre = __ldg(T.ent + e0 + t);
+        const float4 *c4 = reinterpret_cast<const float4 *>(T.chi + (long)(e0 + t) * 12);
+#pragma unroll
+        for (int q = 0; q < 3; q++) chi_pre[q] = __ldg(c4 + q);
+    }
     if (t == 0) {
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -210,18 +221,28 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     __syncthreads();
     load_alpha(g0 * kTcCols);
     // the Chi tile: merged entries (one per point and atom) into the three slices
-    for (int e = e0 + t; e < e1; e += kTcThreads) {
+    auto put_chi = [&](int lp, int row, float x) {
+        unsigned short hs, ms, ls;
+        split3(x, hs, ms, ls);
+        const unsigned o = cd_off(lp, row);
+        *reinterpret_cast<unsigned short *>(smem + o) = hs;
+        *reinterpret_cast<unsigned short *>(smem + kCdSlice + o) = ms;
+        *reinterpret_cast<unsigned short *>(smem + 2 * kCdSlice + o) = ls;
+    };
+    if (pre) {
+        const int lp = meta_pre & 127, ro = (meta_pre >> 7) & 127, np = meta_pre >> 14;
+        const float cv[12] = {chi_pre[0].x, chi_pre[0].y, chi_pre[0].z, chi_pre[0].w,
+                              chi_pre[1].x, chi_pre[1].y, chi_pre[1].z, chi_pre[1].w,
+                              chi_pre[2].x, chi_pre[2].y, chi_pre[2].z, chi_pre[2].w};
+#pragma unroll
+        for (int j = 0; j < 12; j++)
+            if (j < np) put_chi(lp, ro + j, cv[j]);
+    }
+    for (int e = e0 + t + (pre ? kTcThreads : 0); e < e1; e += kTcThreads) {
         const int meta = T.ent[e];
         const int lp = meta & 127, ro = (meta >> 7) & 127, np = meta >> 14;
         const float *cv = T.chi + (long)e * T.jp;
-        for (int j = 0; j < np; j++) {
-            unsigned short hs, ms, ls;
-            split3(__ldg(cv + j), hs, ms, ls);
-            const unsigned o = cd_off(lp, ro + j);
-            *reinterpret_cast<unsigned short *>(smem + o) = hs;
-            *reinterpret_cast<unsigned short *>(smem + kCdSlice + o) = ms;
-            *reinterpret_cast<unsigned short *>(smem + 2 * kCdSlice + o) = ls;
-        }
+        for (int j = 0; j < np; j++) put_chi(lp, ro + j, __ldg(cv + j));
     }
     tc_smem_to_async();
     tc_before_sync();
