@@ -78,7 +78,7 @@ __device__ __forceinline__ void stencil_z_body(const StencilZParams<CT> &p, int 
     // complex64 works with FP32 copies of the weights (no FP64 conversion per use); complex128
     // reads them from the kernel parameters directly
     constexpr bool F32 = sizeof(RT) == 4;
-    ZW<CT> w;
+    ZW<CT> w{};  // filled for complex64 blocks only
     if constexpr (F32) {
 #pragma unroll
         for (int r = 0; r <= R; r++) {
@@ -366,7 +366,8 @@ __device__ __forceinline__ void nl_apply_z_body(
 // points, CB columns); the alpha rows of the chunk's atoms are staged in shared memory (each
 // row padded by 16 bytes, so distinct rows read by one warp start four banks apart), and
 // each entry's contribution is (e^{-i theta_g} Chi_j) alpha_j, with the phase-scaled Chi value
-// formed once per projector.
+// formed once per projector in the block's own precision (complex64 blocks read the FP32 Chi
+// values and round the phase once per entry, so no FP64 arithmetic runs per projector).
 constexpr int kApplyChunkZ = kApplyChunkPts;    // the chunking of the nonlocal upload
 constexpr size_t kZStageMax = 96 * 1024;         // staged rows must fit this (bytes)
 template <typename CT, int CB>
@@ -376,7 +377,7 @@ __device__ __forceinline__ void nl_apply_z_staged_body(
     int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
     const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
     const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
-    const int *__restrict__ chunk_rows, const double *__restrict__ chi,
+    const int *__restrict__ chunk_rows, const typename Real<CT>::type *__restrict__ chi,
     const double2 *__restrict__ img_phase, int ncol, const CT *__restrict__ alpha, long lda,
     double scale, CT *__restrict__ out, long ldo, int c, int n0, CT *S)
 {
@@ -403,14 +404,15 @@ __device__ __forceinline__ void nl_apply_z_staged_body(
     for (int e = e0; e < e1; e++) {
         const int4 meta = ent_meta[e];
         const int np = meta.y, ndc = meta.z;
-        const double *__restrict__ ch = chi + ent_chi[e];
+        const RT *__restrict__ ch = chi + ent_chi[e];
         const CT *srow = S + (long)ent_slot[e] * LDS;
         const double2 ph = img_phase[meta.w];  // e^{-i theta} = (cos, -sin)
+        const RT phx = (RT)ph.x, phy = (RT)ph.y;
 #pragma unroll
         for (int j = 0; j < NPMAX; j++) {
             if (j >= np) break;
-            const double cv = __ldg(ch + (long)j * ndc);
-            const CT t{(RT)(cv * ph.x), (RT)(-cv * ph.y)};
+            const RT cv = __ldg(ch + (long)j * ndc);
+            const CT t{cv * phx, -cv * phy};
 #pragma unroll
             for (int q = 0; q < CB; q++) acc[q] = cadd(acc[q], cmul(t, srow[j * LDS + q]));
         }
@@ -429,7 +431,8 @@ __global__ void __launch_bounds__(kApplyChunkZ)
     k_nl_apply_z_staged(int ncov, const int *__restrict__ cov_pt, const int *__restrict__ cov_ptr,
                         const long *__restrict__ ent_chi, const int4 *__restrict__ ent_meta,
                         const int *__restrict__ ent_slot, const int *__restrict__ chunk_row_ptr,
-                        const int *__restrict__ chunk_rows, const double *__restrict__ chi,
+                        const int *__restrict__ chunk_rows,
+                        const typename Real<CT>::type *__restrict__ chi,
                         const double2 *__restrict__ img_phase, int ncol,
                         const CT *__restrict__ alpha, long lda, double scale,
                         CT *__restrict__ out, long ldo)
@@ -619,6 +622,16 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// the Chi table in a block's real precision
+template <typename CT>
+const typename Real<CT>::type *chi_z(const Nonlocal &nl)
+{
+    if constexpr (sizeof(CT) == 8)
+        return nl.chi32;
+    else
+        return nl.chi64;
+}
+
 // staged, grouped: grid (chunk, column block, block); blocks with fewer columns return early
 template <typename CT, int NPMAX>
 __global__ void __launch_bounds__(kApplyChunkZ)
@@ -627,7 +640,8 @@ __global__ void __launch_bounds__(kApplyChunkZ)
                          const int *__restrict__ cov_ptr, const long *__restrict__ ent_chi,
                          const int4 *__restrict__ ent_meta, const int *__restrict__ ent_slot,
                          const int *__restrict__ chunk_row_ptr,
-                         const int *__restrict__ chunk_rows, const double *__restrict__ chi)
+                         const int *__restrict__ chunk_rows,
+                         const typename Real<CT>::type *__restrict__ chi)
 {
     extern __shared__ __align__(16) unsigned char zsmem[];
     constexpr int CB = zapply_cb<CT>();
@@ -870,8 +884,8 @@ static int nonlocal_z(sgpu_ctx *ctx, int ncol, const CT *x, long ldx, CT *out, l
                                                    (int)std::max<size_t>(stage, 16)));
                 kern<<<sg, kApplyChunkZ, std::max<size_t>(stage, 16), st>>>(
                     nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi, nl.ent_meta, nl.ent_slot,
-                    nl.chunk_row_ptr, nl.chunk_rows, nl.chi64, ks->img_phase, ncol, alpha, lda,
-                    scale, out, ldo);
+                    nl.chunk_row_ptr, nl.chunk_rows, chi_z<CT>(nl), ks->img_phase, ncol, alpha,
+                    lda, scale, out, ldo);
                 return SGPU_OK;
             };
             if (nl.max_np <= 9)
@@ -1193,11 +1207,11 @@ static int chebyshev_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b
                     if (nl.max_np <= 9)
                         k_nl_apply_zb_staged<CT, 9><<<sg, kApplyChunkZ, sm, st>>>(
                             dB, dC, m, j, out, nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi,
-                            nl.ent_meta, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows, nl.chi64);
+                            nl.ent_meta, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows, chi_z<CT>(nl));
                     else
                         k_nl_apply_zb_staged<CT, 18><<<sg, kApplyChunkZ, sm, st>>>(
                             dB, dC, m, j, out, nl.ncov, nl.cov_pt, nl.cov_ptr, nl.ent_chi,
-                            nl.ent_meta, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows, nl.chi64);
+                            nl.ent_meta, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows, chi_z<CT>(nl));
                 } else {
                     const dim3 ag((nl.ncov + 255) / 256, nblk);
                     if (nl.max_np <= 9)
