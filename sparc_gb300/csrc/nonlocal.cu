@@ -1107,8 +1107,8 @@ void nonlocal_free(Nonlocal &nl)
                     nl.seg_start, nl.ent_slot, nl.chunk_row_ptr, nl.chunk_rows,
                     nl.rng_pt0,  nl.rng_ent0, nl.rng_item0, nl.item_e0, nl.item_row,
                     nl.item_wsplit,
-                    nl.pe_lp,    nl.pe_chi32, nl.tc_pt0, nl.tc_row0, nl.tc_rows, nl.tc_ent0,
-                    nl.tc_ent,   nl.tc_chi};
+                    nl.pe_lp,    nl.pe_chi32, nl.tc_pt0, nl.tc_pts, nl.tc_row0, nl.tc_rows,
+                    nl.tc_ent0,  nl.tc_ent,   nl.tc_chi};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     nl = Nonlocal();
@@ -1345,7 +1345,8 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     UP(pe_lp, pe_lp.data(), pe_lp.size());
     UP(pe_chi32, pe_chi.data(), pe_chi.size());
 #undef UP
-    if (rc == SGPU_OK) rc = nonlocal_tc_build(nl, covptr, ent_chi, ent_meta, chi);
+    if (rc == SGPU_OK)
+        rc = nonlocal_tc_build(nl, ctx->Nx, ctx->Ny, covpts, covptr, ent_chi, ent_meta, chi);
     if (rc != SGPU_OK) {
         nonlocal_free(nl);
         return rc;

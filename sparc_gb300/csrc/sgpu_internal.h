@@ -97,10 +97,11 @@ struct Nonlocal {
     int *pe_lp = nullptr;       // entries in range order: point index within the range
     float *pe_chi32 = nullptr;  // entries in range order: Chi values, range_jp per entry
     // fused apply + projection on the tensor cores (nonlocal_tc.cu): ranges of at most 128
-    // covered points whose atoms own at most 64 projector rows, one merged entry per
-    // (point, atom); tc_nrange 0 when a covered point alone needs more rows
+    // covered points (taken in compact-block order) whose atoms own at most 64 projector rows,
+    // one merged entry per (point, atom); tc_nrange 0 when a covered point alone needs more
     int tc_nrange = 0;
-    int *tc_pt0 = nullptr;      // tc_nrange + 1: first covered point of each range
+    int *tc_pt0 = nullptr;      // tc_nrange + 1: first point of each range in tc_pts
+    int *tc_pts = nullptr;      // grid point of every range point (ranges back to back)
     int *tc_row0 = nullptr;     // tc_nrange + 1: first row-list entry of each range
     int *tc_rows = nullptr;     // alpha row of every range row
     int *tc_ent0 = nullptr;     // tc_nrange + 1: first merged entry of each range
@@ -283,9 +284,9 @@ int launch_nonlocal_apply_project_tc(sgpu_ctx *ctx, int ncol, const float *alpha
                                      cudaStream_t st);
 bool nonlocal_tc_ready(const sgpu_ctx *ctx);
 // builds the tensor-core range tables from the point CSR of nonlocal_upload
-int nonlocal_tc_build(Nonlocal &nl, const std::vector<int> &covptr,
-                      const std::vector<long> &ent_chi, const std::vector<int4> &ent_meta,
-                      const double *chi);
+int nonlocal_tc_build(Nonlocal &nl, int Nx, int Ny, const std::vector<int> &covpts,
+                      const std::vector<int> &covptr, const std::vector<long> &ent_chi,
+                      const std::vector<int4> &ent_meta, const double *chi);
 int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double *gamma,
                     int nimg, const int *img_atom, const int *img_ndc, const int *grid_pos,
                     const double *chi);
