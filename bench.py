@@ -73,8 +73,9 @@ def parse():
                          "fp32_eager, fp32_bf16_split, fp64)")
     ap.add_argument("--fp64-only", action="store_true",
                     help="only the FP64 filter steps, no tuning or side blocks (profiling)")
-    ap.add_argument("--fp32-only", action="store_true",
-                    help="only the tuned FP32 filter steps and their kernel times (profiling)")
+    ap.add_argument("--fp32-only", "--no-fp64", dest="fp32_only", action="store_true",
+                    help="only the tuner and the tuned FP32 filter steps with their kernel times, "
+                         "no FP64 headline or side blocks (profiling)")
     ap.add_argument("--c3-prec", type=int, default=0, choices=[0, 32, 64],
                     help="C3 block: only this precision (0: both)")
     ap.add_argument("--c3-filter-only", action="store_true",
