@@ -357,6 +357,39 @@ def test_host_arrays_stream_through_column_chunks(gpu_available, precision, ncol
     assert ctx.kernel_status() == 0
 
 
+@pytest.mark.parametrize("natom,rc", [(20, 3.0), (6, 2.0)])
+def test_tensor_core_fused_form_availability(gpu_available, natom, rc):
+    """The tensor-core fused form needs every covered point's atoms to own at most 64
+    projector rows. With 16 rows per atom (lmax 3) and points inside five or more spheres no
+    tables are built: mode 3 is refused and the tuner keeps a CUDA-core form. Otherwise the
+    tables exist and the form is tuned beside the others. Either way the filter matches the
+    oracle."""
+    rng = np.random.default_rng(5)
+    shape, h = (24, 24, 24), 0.4
+    grid = dict(Nx=shape[0], Ny=shape[1], Nz=shape[2], FDn=6, cx=fd_d2_coeffs(6, h),
+                cy=fd_d2_coeffs(6, h), cz=fd_d2_coeffs(6, h), dV=h ** 3)
+    Nd = shape[0] * shape[1] * shape[2]
+    veff = rng.normal(0.0, 1.0, Nd)
+    nl = synthetic_nonlocal(rng, shape, h, natom=natom, rc=rc, lmax=3)
+    cover = np.bincount(nl["grid_pos"], minlength=Nd)  # one image per atom here
+    rows_max = 16 * int(cover.max())
+    ctx = make_ctx(grid, nl, veff)
+    avail, _ = ctx.nonlocal_fuse_tc()
+    assert avail == (rows_max <= 64), rows_max
+    if not avail:
+        with pytest.raises(sg.SgpuError):
+            ctx.set_nonlocal_fuse(True, 3)
+    ctx.autotune(ncol=16)
+    on, form, _ = ctx.nonlocal_fuse()
+    assert form in ((0, 2, 3, 4) if avail else (0, 2, 4))
+    x = rng.uniform(-1, 1, (16, Nd))
+    X = x.astype(np.float32); Y = np.zeros_like(X)
+    ctx.ChebyshevFiltering_f32(X, Y, 5, 0.5, 50.0, -1.0)
+    Xo, Yo = Oracle(grid, nl).chebyshev(veff, 5, 0.5, 50.0, -1.0, x)
+    assert rel_err(Y.astype(np.float64), Yo) < TOL32_FILTER
+    assert ctx.kernel_status() == 0
+
+
 @pytest.mark.parametrize("ncol", [1, 2, 63, 64, 65, 128])
 @pytest.mark.parametrize("cpl", [2, 4, 3])
 def test_carried_projections_column_edges(gpu_available, ncol, cpl):
