@@ -556,10 +556,13 @@ __global__ void __launch_bounds__(256)
 // complex64 projection: block = (image g, group of kProjCols columns of one block), eight warps
 // of four columns each. Lane = 8 c + p: column c of the warp, point phase p, so one load
 // instruction reads eight consecutive points of four columns (coalesced) and one Chi row
-// segment of eight points serves all four columns. Each lane accumulates every projector;
-// three shuffle steps sum the eight point phases (every lane ends with the totals) and lane p
-// adds projectors p, p+8, p+16: alpha[row, n] += e^{i theta_g} dV Gamma_row sum (atomic across
-// the images of one atom).
+// segment of eight points serves all four columns. The image's grid positions and Chi rows
+// pass through shared memory in chunks of kProjChunk points (coalesced loads by the whole
+// block), so the orbital loads wait on no other global load and several are in flight per
+// lane. Each lane accumulates every projector; three shuffle steps sum the eight point phases
+// (every lane ends with the totals) and lane p adds projectors p, p+8, p+16:
+// alpha[row, n] += e^{i theta_g} dV Gamma_row sum (atomic across the images of one atom).
+constexpr int kProjChunk = 256;  // points per staged chunk of the complex64 projection
 template <int MAXJ>
 __global__ void __launch_bounds__(256)
     k_nl_project_zb_c64(const BBlock<float2> *__restrict__ blocks, const int2 *__restrict__ cg,
@@ -582,18 +585,28 @@ __global__ void __launch_bounds__(256)
     const int n = bc.y + wid * 4 + c;
     const bool on = n < B.ncol;
     const float2 *__restrict__ xc = B.buf[in_sel] + (long)(on ? n : bc.y) * B.ld[in_sel];
+    __shared__ int sgp[kProjChunk];
+    __shared__ float sch[MAXJ][kProjChunk];
     float2 acc[MAXJ];
 #pragma unroll
     for (int jj = 0; jj < MAXJ; jj++) acc[jj] = make_float2(0.f, 0.f);
-#pragma unroll 2
-    for (int ii = p; ii < ndc; ii += 8) {
-        const float2 xv = on ? __ldg(xc + __ldg(gp + ii)) : make_float2(0.f, 0.f);
+    for (int c0 = 0; c0 < ndc; c0 += kProjChunk) {
+        const int cn = min(kProjChunk, ndc - c0);
+        __syncthreads();  // the previous chunk is consumed
+        for (int i = threadIdx.x; i < cn; i += 256) sgp[i] = __ldg(gp + c0 + i);
+        for (int jj = 0; jj < np; jj++)
+            for (int i = threadIdx.x; i < cn; i += 256) sch[jj][i] = __ldg(ch + (long)jj * ndc + c0 + i);
+        __syncthreads();
+#pragma unroll 4
+        for (int ii = p; ii < cn; ii += 8) {
+            const float2 xv = on ? __ldg(xc + sgp[ii]) : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int jj = 0; jj < MAXJ; jj++) {
-            if (jj < np) {
-                const float cv = __ldg(ch + (long)jj * ndc + ii);
-                acc[jj].x = fmaf(cv, xv.x, acc[jj].x);
-                acc[jj].y = fmaf(cv, xv.y, acc[jj].y);
+            for (int jj = 0; jj < MAXJ; jj++) {
+                if (jj < np) {
+                    const float cv = sch[jj][ii];
+                    acc[jj].x = fmaf(cv, xv.x, acc[jj].x);
+                    acc[jj].y = fmaf(cv, xv.y, acc[jj].y);
+                }
             }
         }
     }
