@@ -650,7 +650,8 @@ int sgpu_set_eig_solver(sgpu_ctx *ctx, int mode);
  * products of three-slice BF16 splits, FP32-accurate, accumulated in FP32); mode 1 keeps the
  * current form. The projections agree with the separate ones to FP32 rounding. Needs the
  * range tables of FP32 projector sets; mode 3 also the tensor-core tables (built unless a
- * covered point needs more than 64 rows: SGPU_ERR_STATE then). sgpu_autotune times every form
+ * covered point needs more than 64 rows: SGPU_ERR_STATE then; a later sgpu_set_nonlocal whose
+ * set has none returns the fused form to 2 columns per thread). sgpu_autotune times every form
  * and turns fusion on when the fastest beats the fastest separate apply plus projection. */
 int sgpu_set_nonlocal_fuse(sgpu_ctx *ctx, int mode);
 

@@ -1354,6 +1354,9 @@ int nonlocal_upload(sgpu_ctx *ctx, int natom, const int *ip_displ, const double 
     nonlocal_free(ctx->nl);
     ctx->nl = nl;
     ctx->has_nl = true;
+    // a tensor-core fused form chosen for an earlier projector set needs tables this set may
+    // not have: the CUDA-core form then takes over until the next tuning
+    if (ctx->nl_fuse_cpl == 3 && nl.tc_nrange == 0) ctx->nl_fuse_cpl = 2;
     return SGPU_OK;
 }
 

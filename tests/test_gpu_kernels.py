@@ -387,6 +387,17 @@ def test_tensor_core_fused_form_availability(gpu_available, natom, rc):
     ctx.ChebyshevFiltering_f32(X, Y, 5, 0.5, 50.0, -1.0)
     Xo, Yo = Oracle(grid, nl).chebyshev(veff, 5, 0.5, 50.0, -1.0, x)
     assert rel_err(Y.astype(np.float64), Yo) < TOL32_FILTER
+    if avail:  # a projector set without tables replaces this one: the CUDA-core form takes over
+        ctx.set_nonlocal_fuse(True, 3)
+        nl2 = synthetic_nonlocal(np.random.default_rng(6), shape, h, natom=20, rc=3.0, lmax=3)
+        assert 16 * int(np.bincount(nl2["grid_pos"], minlength=Nd).max()) > 64
+        ctx.set_nonlocal(nl2["ip_displ"], nl2["gamma"], nl2["img_atom"], nl2["img_ndc"],
+                         nl2["grid_pos"], nl2["chi"])
+        assert not ctx.nonlocal_fuse_tc()[0] and ctx.nonlocal_fuse()[:2] == (True, 2)
+        X = x.astype(np.float32); Y = np.zeros_like(X)
+        ctx.ChebyshevFiltering_f32(X, Y, 5, 0.5, 50.0, -1.0)
+        Xo, Yo = Oracle(grid, nl2).chebyshev(veff, 5, 0.5, 50.0, -1.0, x)
+        assert rel_err(Y.astype(np.float64), Yo) < TOL32_FILTER
     assert ctx.kernel_status() == 0
 
 
