@@ -558,13 +558,13 @@ __global__ void __launch_bounds__(256)
 // instruction reads eight consecutive points of four columns (coalesced) and one Chi row
 // segment of eight points serves all four columns. The image's grid positions and Chi rows
 // pass through shared memory in chunks of kProjChunk points (coalesced loads by the whole
-// block), so the orbital loads wait on no other global load and several are in flight per
-// lane. Each lane accumulates every projector; three shuffle steps sum the eight point phases
+// block; Chi stored point-major so a lane reads a point's values in 16-byte pieces), so the
+// orbital loads wait on no other global load and several are in flight per lane. Each lane accumulates every projector; three shuffle steps sum the eight point phases
 // (every lane ends with the totals) and lane p adds projectors p, p+8, p+16:
 // alpha[row, n] += e^{i theta_g} dV Gamma_row sum (atomic across the images of one atom).
 constexpr int kProjChunk = 256;  // points per staged chunk of the complex64 projection
 template <int MAXJ>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     k_nl_project_zb_c64(const BBlock<float2> *__restrict__ blocks, const int2 *__restrict__ cg,
                         int in_sel, const int *__restrict__ img_atom,
                         const int *__restrict__ img_ndc, const long *__restrict__ img_off,
@@ -585,8 +585,13 @@ __global__ void __launch_bounds__(256)
     const int n = bc.y + wid * 4 + c;
     const bool on = n < B.ncol;
     const float2 *__restrict__ xc = B.buf[in_sel] + (long)(on ? n : bc.y) * B.ld[in_sel];
+    // Chi of a chunk point-major, rows padded to a multiple of four floats: a lane reads one
+    // point's values in 16-byte pieces, and the eight points a warp reads at once (rows
+    // MAXJP floats apart, MAXJP = 4 mod 8) fall on distinct banks
+    constexpr int MAXJP = (MAXJ + 3) / 4 * 4;
+    static_assert(MAXJP % 8 == 4, "row pitch of the staged Chi values");
     __shared__ int sgp[kProjChunk];
-    __shared__ float sch[MAXJ][kProjChunk];
+    __shared__ __align__(16) float sch[kProjChunk * MAXJP];
     float2 acc[MAXJ];
 #pragma unroll
     for (int jj = 0; jj < MAXJ; jj++) acc[jj] = make_float2(0.f, 0.f);
@@ -594,18 +599,25 @@ __global__ void __launch_bounds__(256)
         const int cn = min(kProjChunk, ndc - c0);
         __syncthreads();  // the previous chunk is consumed
         for (int i = threadIdx.x; i < cn; i += 256) sgp[i] = __ldg(gp + c0 + i);
-        for (int jj = 0; jj < np; jj++)
-            for (int i = threadIdx.x; i < cn; i += 256) sch[jj][i] = __ldg(ch + (long)jj * ndc + c0 + i);
+        for (int jj = 0; jj < MAXJP; jj++)
+            for (int i = threadIdx.x; i < cn; i += 256)
+                sch[i * MAXJP + jj] = jj < np ? __ldg(ch + (long)jj * ndc + c0 + i) : 0.f;
         __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
         for (int ii = p; ii < cn; ii += 8) {
             const float2 xv = on ? __ldg(xc + sgp[ii]) : make_float2(0.f, 0.f);
+            const float4 *cr = reinterpret_cast<const float4 *>(sch + ii * MAXJP);
 #pragma unroll
-            for (int jj = 0; jj < MAXJ; jj++) {
-                if (jj < np) {
-                    const float cv = sch[jj][ii];
-                    acc[jj].x = fmaf(cv, xv.x, acc[jj].x);
-                    acc[jj].y = fmaf(cv, xv.y, acc[jj].y);
+            for (int u = 0; u < MAXJP / 4; u++) {
+                const float4 c4 = cr[u];
+                const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                for (int w = 0; w < 4; w++) {
+                    const int jj = 4 * u + w;
+                    if (jj < MAXJ && jj < np) {
+                        acc[jj].x = fmaf(cv[w], xv.x, acc[jj].x);
+                        acc[jj].y = fmaf(cv[w], xv.y, acc[jj].y);
+                    }
                 }
             }
         }
