@@ -90,6 +90,9 @@ def parse():
     ap.add_argument("--nl-fuse", type=int, default=None, choices=[0, 2, 3, 4],
                     help="force the projections carried across filter degrees off (0) or on "
                          "with 2 or 4 columns per thread")
+    ap.add_argument("--switch-error", type=float, default=1e-4,
+                    help="SCF error below which the mixed SCF blocks (C3, C4) move to FP64 / "
+                         "complex128")
     ap.add_argument("--nl-project", type=int, default=None,
                     help="use this FP32 projection form instead of the tuned one (profiling)")
     return ap.parse_args()
@@ -261,7 +264,7 @@ def scf_block(sg, device=0, repeats=2):
     return out
 
 
-def scf_c4_block(sg, torch=None, device=0):
+def scf_c4_block(sg, torch=None, device=0, switch_error=1e-4):
     """SCF time-to-solution on the 216-atom Si cell (3x3x3 diamond cells, a = 30.78 Bohr,
     77^3 grid, 520 states, degree 24, LDA, TOL_SCF 1e-6), set up on the device from the Si
     psp8 tables (sparc_gb300.setup): plain FP64 CheFSI (the reference's settings, 4 filter
@@ -297,7 +300,8 @@ def scf_c4_block(sg, torch=None, device=0):
                             "walltime_s": ref.get("walltime_s"),
                             "where": ref.get("where", "reference program, x86 build host")}
     from sparc_gb300.learned_density import DensityMLP, energy_reached, initial_density
-    mixed = dict(precision=32, fp64_switch_error=1e-4, graded_tail=1, tail_fp64_degrees=0)
+    mixed = dict(precision=32, fp64_switch_error=switch_error, graded_tail=1,
+                 tail_fp64_degrees=0)
     runs = {"fp64": (dict(precision=64), 4, False),
             "mixed": (mixed, 4, False),
             "mixed_rt8": (mixed, 8, False),
@@ -387,11 +391,13 @@ C3_KRED = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (1, 1, 0), (2, 1, 0), (2, 2, 0), (1,
 C3_KWTS = [1, 6, 3, 12, 12, 3, 8, 12, 6, 1]
 
 
-def scf_c3_block(sg, device=0):
+def scf_c3_block(sg, device=0, switch_error=1e-4):
     """Spin-polarised k-point SCF of the C3 system: Al32 (34^3 grid), the 10 weighted
     k-points, collinear spin from seeded +-0.2 moments, 64 states per (k, spin) block (20
     blocks), degree 18, from the library's own set-up. Plain complex128 against the
-    complex64-first mixed mode (complex128 below an SCF error of 1e-4); wall time to TOL_SCF
+    complex64-first mixed mode (complex128 below an SCF error of switch_error) and the graded
+    mixed mode (after the switch a complex64 filter with a complex128 Rayleigh-Ritz step and
+    density); wall time to TOL_SCF
     and the difference of the two energies. (The SCF machinery is pinned to the reference
     program on the Al4 spin k-point run; the reference has no cubic-symmetry k-reduction, so
     this 10-point set has no reference run.)"""
@@ -406,9 +412,11 @@ def scf_c3_block(sg, device=0):
     wts = np.array(C3_KWTS, dtype=np.float64)
     out = {"system": "Al32, 34^3, 10 k (cubic-reduced 4x4x4) x 2 spins, 64 states, degree 18, "
                      "smearing 0.003 Ha, TOL_SCF 1e-6", "net_moment_start": float(spins.sum())}
-    for tag, prec in (("complex128", sg.SGPU_PREC_FP64), ("complex64_first", sg.SGPU_PREC_FP32)):
+    for tag, prec, graded in (("complex128", sg.SGPU_PREC_FP64, 0),
+                              ("complex64_first", sg.SGPU_PREC_FP32, 0),
+                              ("complex64_graded", sg.SGPU_PREC_FP32, 1)):
         prm = cs.scf_params(Nstates=64, cheb_degree=18, smearing=0.003, precision=prec,
-                            fp64_switch_error=1e-4)
+                            fp64_switch_error=switch_error, graded_tail=graded)
         res, rho, lam, occ = cs.scf_kpt(prm, kpts, wts, atom_spin_z=spins)
         out[tag] = {"time_s": round(res["time_s"], 3), "scf_iters": res["scf_iters"],
                     "converged": res["converged"], "Etot_per_atom": res["Etot"] / cs.n_atom,
@@ -418,6 +426,10 @@ def scf_c3_block(sg, device=0):
     out["dE_per_atom_mixed_vs_complex128"] = abs(out["complex64_first"]["Etot_per_atom"] -
                                                  out["complex128"]["Etot_per_atom"])
     out["speedup_mixed"] = round(out["complex128"]["time_s"] / out["complex64_first"]["time_s"], 3)
+    out["dE_per_atom_graded_vs_complex128"] = abs(out["complex64_graded"]["Etot_per_atom"] -
+                                                  out["complex128"]["Etot_per_atom"])
+    out["speedup_graded"] = round(out["complex128"]["time_s"] /
+                                  out["complex64_graded"]["time_s"], 3)
     cs.close()
     return out
 
@@ -663,7 +675,7 @@ def main():
         c3 = batched_c3_block(sg, torch, dev, device=local, steps=args.steps,
                               prec_only=args.c3_prec, filter_only=args.c3_filter_only)
         if not args.no_scf:
-            c3["scf"] = scf_c3_block(sg, device=local)
+            c3["scf"] = scf_c3_block(sg, device=local, switch_error=args.switch_error)
         print(json.dumps({"batched_c3": c3}), flush=True)
         return
     if args.rr_gemm:
@@ -952,12 +964,12 @@ def main():
     if rank == 0 and not args.no_scf:
         scf = scf_block(sg, device=local)
         if not args.no_c4:
-            scf_c4 = scf_c4_block(sg, torch, device=local)
+            scf_c4 = scf_c4_block(sg, torch, device=local, switch_error=args.switch_error)
     c3 = None
     if rank == 0 and not args.no_c3:
         c3 = batched_c3_block(sg, torch, dev, device=local)
         if not args.no_scf:
-            c3["scf"] = scf_c3_block(sg, device=local)
+            c3["scf"] = scf_c3_block(sg, device=local, switch_error=args.switch_error)
 
     if rank == 0:
         tune = {"stencil_variant": {"chosen": kernel_name,

@@ -414,8 +414,9 @@ typedef struct {
                                    (also left early when the FP32 error stops falling) */
     int graded_tail;            /* mixed mode after the switch: 0 = plain FP64 CheFSI; 1 = FP32
                                    filter whose last tail_fp64_degrees degrees run in FP64,
-                                   with the Rayleigh-Ritz step in FP64 */
-    int tail_fp64_degrees;      /* 0 .. cheb_degree-1 (graded_tail = 1) */
+                                   with the Rayleigh-Ritz step in FP64 (sgpu_scf_kpt: complex64
+                                   filter, complex128 Rayleigh-Ritz step and density) */
+    int tail_fp64_degrees;      /* 0 .. cheb_degree-1 (graded_tail = 1; 0 for sgpu_scf_kpt) */
     unsigned long long seed;    /* initial orbitals and Lanczos start vector */
     int verbose;
     double *history;            /* optional host array of 3 * maxit_scf: per SCF iteration the
@@ -462,8 +463,10 @@ int sgpu_scf(sgpu_ctx *ctx, const sgpu_scf_params *prm, const double *b,
  * k-point geometry of the context (sgpu_set_kpoint_geometry or
  * sgpu_CalculateNonlocalProjectors). Each filter pass runs all k-points through one batched
  * filter and then each k-point's Rayleigh-Ritz step (sgpu_CheFSI_batched). precision
- * SGPU_PREC_FP32 runs complex64 orbitals until the error falls below fp64_switch_error;
- * graded_tail must be 0. lambda_out and occ_out (nkpt * Nstates) are k-point after k-point;
+ * SGPU_PREC_FP32 runs complex64 orbitals until the error falls below fp64_switch_error (or
+ * stops falling), then complex128 orbitals, or with graded_tail = 1 a complex64 filter whose
+ * output is widened for a complex128 Rayleigh-Ritz step and density (tail_fp64_degrees must
+ * be 0). lambda_out and occ_out (nkpt * Nstates) are k-point after k-point;
  * psi_out, when set, receives nkpt blocks of Nd x Nstates complex128 (interleaved). */
 int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const double *kpts,
                  const double *kpt_wts, const double *b, const double *rho_init,

@@ -1589,10 +1589,9 @@ static int rr_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, dou
 // block's Ritz values, blocks one after another. Blocks of one width with common leading
 // dimensions take the batched Rayleigh-Ritz step (ctx->rr_batched), others one block at a time.
 template <typename CT>
-int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
-                   double *lambda, cudaStream_t st)
+int rayleigh_ritz_blocks(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, double *lambda,
+                         cudaStream_t st)
 {
-    SGPU_TRY(chebyshev_batched<CT>(ctx, nblk, blk, m, st));
     bool uniform = ctx->rr_batched && nblk > 0;
     for (int b = 1; b < nblk && uniform; b++)
         uniform = blk[b].ncol == blk[0].ncol && blk[b].ldi == blk[0].ldi &&
@@ -1626,10 +1625,42 @@ int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
     return SGPU_OK;
 }
 
+template <typename CT>
+int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
+                   double *lambda, cudaStream_t st)
+{
+    SGPU_TRY(chebyshev_batched<CT>(ctx, nblk, blk, m, st));
+    return rayleigh_ritz_blocks<CT>(ctx, nblk, blk, lambda, st);
+}
+
 template int chefsi_batched<double2>(sgpu_ctx *, int, const sgpu_filter_block *, int, double *,
                                      cudaStream_t);
 template int chefsi_batched<float2>(sgpu_ctx *, int, const sgpu_filter_block *, int, double *,
                                     cudaStream_t);
+
+// Graded pass: the complex64 filter of b32 (X -> Y), its result widened into b64's Y, the
+// complex128 Rayleigh-Ritz step on b64 (Ritz vectors into b64's X), and those narrowed into
+// b32's X for the next filter. The two descriptor sets describe the same blocks (same ncol,
+// k-point and spin).
+int chefsi_batched_graded(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b32,
+                          const sgpu_filter_block *b64, int m, double *lambda, cudaStream_t st)
+{
+    SGPU_TRY(chebyshev_batched<float2>(ctx, nblk, b32, m, st));
+    for (int b = 0; b < nblk; b++)
+        if (b32[b].ncol > 0)
+            SGPU_TRY((convert_cols<float, double>(
+                reinterpret_cast<const float *>(b32[b].Y), 2L * b32[b].ldo,
+                reinterpret_cast<double *>(b64[b].Y), 2L * b64[b].ldo, 2L * ctx->Nd,
+                b32[b].ncol, st)));
+    SGPU_TRY(rayleigh_ritz_blocks<double2>(ctx, nblk, b64, lambda, st));
+    for (int b = 0; b < nblk; b++)
+        if (b32[b].ncol > 0)
+            SGPU_TRY((convert_cols<double, float>(
+                reinterpret_cast<const double *>(b64[b].X), 2L * b64[b].ldi,
+                reinterpret_cast<float *>(b32[b].X), 2L * b32[b].ldi, 2L * ctx->Nd,
+                b32[b].ncol, st)));
+    return SGPU_OK;
+}
 
 }  // namespace sgpu
 

@@ -20,7 +20,10 @@
 // k-points and degrees) followed by each k-point's Rayleigh-Ritz step (chefsi_batched); the
 // reference filters its k-points one after another. Mixed precision (SGPU_PREC_FP32) keeps
 // complex64 orbitals with complex64 projection / rotation products and the complex128
-// eigensolve while the SCF error is above fp64_switch_error, then widens them to complex128.
+// eigensolve while the SCF error is above fp64_switch_error, then widens them to complex128;
+// with graded_tail the filter stays complex64 after the switch and only the Rayleigh-Ritz step
+// (H Y, projection, eigensolve, rotation) and the density run on complex128 copies, as in the
+// Gamma-point driver's graded tail.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -64,8 +67,13 @@ int scf_kpt_check(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const dou
         set_error("sgpu_scf_kpt: precision must be SGPU_PREC_FP64 or SGPU_PREC_FP32");
         return SGPU_ERR_ARG;
     }
-    if (prm->graded_tail != 0) {
-        set_error("sgpu_scf_kpt: graded_tail is a Gamma-point option; set it to 0");
+    if (prm->graded_tail != 0 && prm->graded_tail != 1) {
+        set_error("sgpu_scf_kpt: graded_tail must be 0 or 1");
+        return SGPU_ERR_ARG;
+    }
+    if (prm->graded_tail && prm->tail_fp64_degrees != 0) {
+        set_error("sgpu_scf_kpt: FP64 filter degrees in the graded tail are a Gamma-point "
+                  "option; set tail_fp64_degrees to 0");
         return SGPU_ERR_ARG;
     }
     if (prm->spin_typ != 0 && prm->spin_typ != 1) {
@@ -198,7 +206,8 @@ int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const doub
         for (int n = 0; n < Ns; n++) wocc[(size_t)bk * Ns + n] = occfac * wk[bk % nkpt];
     std::vector<double> lam((size_t)nblk * Ns, 0.0), occ((size_t)nblk * Ns, 0.0);
     std::vector<double> eigmin(nblk, 0.0), eigmax(nblk, 0.0);
-    std::vector<sgpu_filter_block> blk(nblk);
+    std::vector<sgpu_filter_block> blk(nblk), blk64(nblk);
+    bool graded = false;  // after the switch with graded_tail: complex64 filter, complex128 RR
     double efermi = 0.0, error = prm->tol_scf + 1.0, net_mag = 0.0;
     double Etot = 0, Eband = 0, E1 = 0, E2 = 0, E3 = 0, Exc = 0, Entropy = 0;
     int scf = 0, switch_iter = mixed ? -1 : 0;
@@ -238,8 +247,9 @@ int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const doub
                 sgpu_filter_block &f = blk[bk];
                 f.spin = sp;
                 f.k[0] = kv[0]; f.k[1] = kv[1]; f.k[2] = kv[2];
-                f.X = mixed ? (void *)(X32 + nb * bk) : (void *)(X64 + nb * bk);
-                f.Y = mixed ? (void *)(Y32 + nb * bk) : (void *)(Y64 + nb * bk);
+                const bool c64 = mixed || graded;  // the filter runs on complex64 blocks
+                f.X = c64 ? (void *)(X32 + nb * bk) : (void *)(X64 + nb * bk);
+                f.Y = c64 ? (void *)(Y32 + nb * bk) : (void *)(Y64 + nb * bk);
                 f.ldi = f.ldo = (int)N;
                 f.ncol = Ns;
                 f.a = cutoff;
@@ -252,10 +262,19 @@ int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const doub
                 }
             }
             SGPU_CUDA_TRY(cudaEventRecord(ctx->ev0, st));
-            if (mixed)
+            if (graded) {
+                for (int bk = 0; bk < nblk; bk++) {
+                    blk64[bk] = blk[bk];
+                    blk64[bk].X = X64 + nb * bk;
+                    blk64[bk].Y = Y64 + nb * bk;
+                }
+                SGPU_TRY(chefsi_batched_graded(ctx, nblk, blk.data(), blk64.data(), m,
+                                               lam.data(), st));
+            } else if (mixed) {
                 SGPU_TRY(chefsi_batched<float2>(ctx, nblk, blk.data(), m, lam.data(), st));
-            else
+            } else {
                 SGPU_TRY(chefsi_batched<double2>(ctx, nblk, blk.data(), m, lam.data(), st));
+            }
             SGPU_CUDA_TRY(cudaEventRecord(ctx->ev1, st));
             SGPU_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
             float ms = 0.f;
@@ -367,7 +386,9 @@ int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const doub
         scf++;
         if (prm->verbose)
             printf("sgpu_scf_kpt: iter %3d  Etot/atom %.10f  error %.3e  %s%s\n", scf,
-                   Etot / std::max(1, prm->n_atom), error, mixed ? "complex64" : "complex128",
+                   Etot / std::max(1, prm->n_atom), error,
+                   mixed ? "complex64" : graded ? "complex64 filter, complex128 Rayleigh-Ritz"
+                                                : "complex128",
                    spin ? "  (collinear spin)" : "");
         if (error < prm->tol_scf && scf >= prm->minit_scf) break;
         if (mixed) {
@@ -380,6 +401,7 @@ int sgpu_scf_kpt(sgpu_ctx *ctx, const sgpu_scf_params *prm, int nkpt, const doub
                                                      reinterpret_cast<double *>(X64), 2 * ncplx,
                                                      2 * ncplx, 1, st));
                 mixed = false;
+                graded = prm->graded_tail == 1;  // X32 keeps the Ritz vectors for the filter
                 switch_iter = scf;
             }
         }

@@ -381,6 +381,10 @@ int kpoint_set_phases(sgpu_ctx *ctx, const double *k, cudaStream_t st);
 template <typename CT>
 int chefsi_batched(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *blk, int m,
                    double *lambda, cudaStream_t st);
+// complex64 filter of b32, complex128 Rayleigh-Ritz step on b64 (the same blocks in complex128
+// storage), Ritz vectors narrowed back into b32's X
+int chefsi_batched_graded(sgpu_ctx *ctx, int nblk, const sgpu_filter_block *b32,
+                          const sgpu_filter_block *b64, int m, double *lambda, cudaStream_t st);
 
 // ---- elementwise helpers (util.cu)
 template <typename T>

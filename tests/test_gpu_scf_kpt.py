@@ -24,11 +24,14 @@ def make_kctx(d, grid, nl):
     return ctx
 
 
-@pytest.mark.parametrize("precision", [64, 32])
-def test_scf_kpt_matches_reference_program(gpu_available, precision):
+@pytest.mark.parametrize("precision,graded", [(64, 0), (32, 0), (32, 1)])
+def test_scf_kpt_matches_reference_program(gpu_available, precision, graded):
+    """graded: after the switch the filter stays complex64 and the Rayleigh-Ritz step and the
+    density run in complex128."""
     d, grid, nl, ref = load_scf("Si2_kpt")
     ctx = make_kctx(d, grid, nl)
     prm = scf_params(sg, d, ref, precision=precision, switch=1e-4)
+    prm.graded_tail = graded
     res, rho, lam, occ = ctx.scf_kpt(prm, d["kpts"], d["kpt_wts"], d["b"], d["rho0"],
                                      d["rho_core"])
     n_atom = int(d["n_atom"])
@@ -75,7 +78,7 @@ def test_scf_kpt_rejects_bad_input(gpu_available):
         ctx.scf_kpt(prm, d["kpts"], -d["kpt_wts"], d["b"], d["rho0"], d["rho_core"])
     prm.graded_tail = 1
     prm.tail_fp64_degrees = 2
-    with pytest.raises(sg.SgpuError):  # the graded tail is a Gamma-point option
+    with pytest.raises(sg.SgpuError):  # FP64 filter degrees in the tail: Gamma-point only
         ctx.scf_kpt(prm, d["kpts"], d["kpt_wts"], d["b"], d["rho0"], d["rho_core"])
     ctx3 = sg.Context(grid["Nx"], grid["Ny"], grid["Nz"], grid["FDn"], grid["cx"], grid["cy"],
                       grid["cz"], grid["dV"])
@@ -117,15 +120,17 @@ def test_spin_mixing_matches_reference(gpu_available):
         ctx.Mixing_periodic_pulay(9, d["mix_outputs"][0].copy())
 
 
-@pytest.mark.parametrize("precision", [64, 32])
-def test_spin_scf_kpt_matches_reference_program(gpu_available, precision):
+@pytest.mark.parametrize("precision,graded", [(64, 0), (32, 0), (32, 1)])
+def test_spin_scf_kpt_matches_reference_program(gpu_available, precision, graded):
     """Collinear-spin k-point SCF (Al4, 4 k-points x 2 spins = 8 blocks) against the
     reference program: free energy, Fermi level, occupied eigenvalues of every (spin, k)
-    block, net magnetization."""
+    block, net magnetization (graded: complex64 filter with a complex128 Rayleigh-Ritz step
+    after the switch)."""
     d, grid, nl, ref = load_scf("Al4_spin_kpt")
     p = ref["params"]
     ctx = make_kctx(d, grid, nl)
     prm = scf_params(sg, d, ref, precision=precision, switch=1e-4)
+    prm.graded_tail = graded
     prm.mixing_param_mag = p["MixingParameterMag"]
     prm.mixing_param_simple_mag = p["MixingParameterSimpleMag"]
     fields = {}
