@@ -2,8 +2,9 @@
 //
 // The FP32 Chebyshev filter applies Vnl at every degree (src/nlocVecRoutines.c:798-886,
 // called from src/eigenSolver.c:722-798) and projects the iterate it finishes for the next
-// degree. Over a range of at most 128 consecutive covered grid points whose atoms own at most
-// 64 projector rows in all, both are small dense products with one shared matrix, the range's
+// degree. Over a range of at most 128 covered grid points (consecutive in the order of compact
+// blocks of the grid) whose atoms own at most 64 projector rows in all, both are small dense
+// products with one shared matrix, the range's
 // Chi tile C[point][row] (the Chi values of every atom image covering the point, images of one
 // atom summed):
 //     apply       T[point][col] += scale C[point][:] . alpha[:][col]       (M = 128 points)
@@ -12,8 +13,8 @@
 // with T the range's output tile (64 columns at a time). Each FP32 operand is written as the
 // sum of three BF16 slices (hi, mid, lo: 24 significant bits), and the six slice products
 // with i + j <= 2 are accumulated in FP32 in tensor memory, so the products are FP32-accurate
-// (the dropped terms are below 2^-24 of |C| |x|) and the accumulation is FP32 as on the CUDA
-// cores.
+// (the split residuals and the dropped slice products are of order 2^-24 |C| |x|) and the
+// accumulation is FP32 as on the CUDA cores.
 //
 // Per range (one CTA of 256 threads, two CTAs per SM): the Chi tile's three slices are built
 // once in shared memory from the range's entries; then per group of 64 columns
@@ -82,7 +83,8 @@ __device__ __forceinline__ unsigned tl_off(int pt, int colblk)
     return (unsigned)(colblk * 2048 + (pt >> 3) * 128 + (pt & 7) * 16);
 }
 
-// x = hi + mid + lo + e, |e| <= 2^-26 |x| (round-to-nearest slices; the differences are exact)
+// x = hi + mid + lo + e, |e| <= 2^-24 |x| (round-to-nearest slices of 8 significant bits, each
+// at most 2^-8 of the remainder it rounds; the differences are exact)
 __device__ __forceinline__ void split3(float x, unsigned short &h, unsigned short &m,
                                        unsigned short &l)
 {
